@@ -1,0 +1,308 @@
+"""Seeded synthetic meshes written in the reference's own input formats.
+
+The reference reads a command file (keywords parsed in
+``SourceFiles/Solver/fioFile.cpp:69-462``) that names a mesh file in the
+``.lis`` layout read by ``datModel::readdata`` (``SourceFiles/Solver/datModel.cpp:58-326``):
+
+    title
+    label line
+    <2D|3D> <problem type>
+    E nu rho KIc sig_ult
+    numNode numEle
+    <id x y z>                          x numNode
+    <id algo n1..n4 | n1..n8>           x numEle   (algo 1 = PD, 2 = FE)
+    ====Essential BCs====
+    numEBC
+    <numNode UX|UY|UZ value>            x numEBC
+    <node ids>                          per EBC
+    ====Natural BCs====
+    numNBC  (<numEle value> headers, then 2 or 4 node ids per element)
+    ====NO FAIL region====
+    numNoFail  ids...
+    ====pre-exist crack====
+    numCrack   (2D: 2 points x 3 coords, 3D: 3 points x 3 coords)
+
+Structured Q4 (2D) and Hex8 (3D) grids are generated with node index
+``i + nx*(j + ny*k)`` (x fastest), holes are made by deleting elements and
+then dropping orphan nodes (a node without element has zero volume, which
+the reference divides by), and PD zones are element sets with algo type 1.
+
+Coordinates are written with 17 significant digits so that the mesh read
+back is bit-identical to the generated arrays.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+from typing import Callable, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+DOF_NAMES = ("UX", "UY", "UZ")
+
+
+@dataclasses.dataclass
+class EBC:
+    dof: int                     # 0 = UX, 1 = UY, 2 = UZ
+    value: float
+    nodes: np.ndarray            # 1-based node ids
+    velocity: Optional[float] = None   # VEBC velocity (command file)
+
+
+@dataclasses.dataclass
+class NBC:
+    value: float
+    elems: np.ndarray            # (numEle, 2|4) 1-based node ids
+    velocity: Optional[float] = None
+
+
+@dataclasses.dataclass
+class Mesh:
+    title: str
+    dim: int
+    protype: int                 # 1 plane stress, 2 plane strain (2D)
+    E: float
+    nu: float
+    rho: float
+    KIc: float
+    sigult: float
+    X: np.ndarray                # (N, 3)
+    elems: np.ndarray            # (E, 4|8) 1-based
+    algo: np.ndarray             # (E,) 1 PD, 2 FE
+    ebcs: List[EBC]
+    nbcs: List[NBC]
+    nofail: np.ndarray           # 1-based ids
+    cracks: List[np.ndarray]     # each (2,3) in 2D or (3,3) in 3D
+
+    @property
+    def n_node(self) -> int:
+        return int(self.X.shape[0])
+
+    @property
+    def n_elem(self) -> int:
+        return int(self.elems.shape[0])
+
+
+def _fmt(v: float) -> str:
+    return repr(float(v))
+
+
+def write_lis(mesh: Mesh, path: str) -> None:
+    """Write ``mesh`` in the ``.lis`` layout (``datModel.cpp:58-326``)."""
+    lines: List[str] = []
+    lines.append(mesh.title)
+    lines.append("***" + mesh.title + "***")
+    lines.append(f"{mesh.dim}D\t{mesh.protype}")
+    lines.append("\t".join(_fmt(v) for v in (mesh.E, mesh.nu, mesh.rho, mesh.KIc, mesh.sigult)))
+    lines.append(f"{mesh.n_node}\t{mesh.n_elem}")
+    X = mesh.X
+    for i in range(mesh.n_node):
+        lines.append(f"{i + 1}\t{_fmt(X[i, 0])}\t{_fmt(X[i, 1])}\t{_fmt(X[i, 2])}")
+    for e in range(mesh.n_elem):
+        conn = " ".join(str(int(v)) for v in mesh.elems[e])
+        lines.append(f"{e + 1}\t{int(mesh.algo[e])}\t{conn}")
+    lines.append("=============================Essential BCs====================================")
+    lines.append(str(len(mesh.ebcs)))
+    for b in mesh.ebcs:
+        lines.append(f"{len(b.nodes)}\t{DOF_NAMES[b.dof]}\t{_fmt(b.value)}")
+    for b in mesh.ebcs:
+        lines.append(" ".join(str(int(v)) for v in b.nodes))
+    lines.append("=============================Natural BCs====================================")
+    lines.append(str(len(mesh.nbcs)))
+    for b in mesh.nbcs:
+        lines.append(f"{len(b.elems)}\t{_fmt(b.value)}")
+    for b in mesh.nbcs:
+        for row in b.elems:
+            lines.append(" ".join(str(int(v)) for v in row))
+    lines.append("=============================NO FAIL region=================================")
+    lines.append(str(len(mesh.nofail)))
+    if len(mesh.nofail):
+        lines.append(" ".join(str(int(v)) for v in mesh.nofail))
+    lines.append("=============================pre-exist crack=================================")
+    lines.append(str(len(mesh.cracks)))
+    npt = 2 if mesh.dim == 2 else 3
+    for c in mesh.cracks:
+        lines.append("\t".join(_fmt(v) for v in np.asarray(c, dtype=np.float64)[:npt].ravel()))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_cmd(path: str, mesh_file: str, mesh: Mesh, *, solver: str, dt: float,
+              nsteps: int, save: int, factor: float, nlf: float,
+              newmark: Optional[Tuple[float, float]] = None, lumped: bool = True,
+              fc: Optional[str] = None, precision: Optional[str] = None,
+              extra: Sequence[str] = (), vtk: str = "BINARY") -> None:
+    """Write a command file with the reference's keywords (``fioFile.cpp:69-462``).
+
+    ``fc`` is the text after the ``FC`` keyword; ``FC 3 s0 [seed] [pert]`` is the
+    critical-stretch extension (the reference parses flag 3 but never acts on it).
+    """
+    out = [f"MSHFILE {mesh_file}", f"SOLVER {solver}",
+           f"SETSOLVING {_fmt(dt)} {nsteps} {save} {_fmt(factor)} {_fmt(nlf)}"]
+    if newmark is not None:
+        out.append(f"NEWMARK ON {_fmt(newmark[0])} {_fmt(newmark[1])}")
+    else:
+        out.append("NEWMARK OFF")
+    out.append("LUMPMASS " + ("ON" if lumped else "OFF"))
+    for i, b in enumerate(mesh.ebcs):
+        if b.velocity is not None:
+            out.append(f"VEBC {i} {_fmt(b.velocity)}")
+    for i, b in enumerate(mesh.nbcs):
+        if b.velocity is not None:
+            out.append(f"VNBC {i} {_fmt(b.velocity)}")
+    if fc is not None:
+        out.append(f"FC {fc}")
+    if precision is not None:
+        out.append(f"PRECISION {precision}")
+    out.extend(extra)
+    out.append(f"VTKFORMAT {vtk}")
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
+# --------------------------------------------------------------------------
+# structured grids
+# --------------------------------------------------------------------------
+
+def _compact(X: np.ndarray, elems0: np.ndarray, algo: np.ndarray):
+    """Drop orphan nodes; return (X, elems 1-based, algo, old->new map)."""
+    used = np.zeros(X.shape[0], dtype=bool)
+    used[elems0.ravel()] = True
+    newid = -np.ones(X.shape[0], dtype=np.int64)
+    newid[used] = np.arange(int(used.sum()))
+    return X[used], newid[elems0] + 1, algo, newid
+
+
+def grid2d(nx: int, ny: int, h: float, x0: float = 0.0, y0: float = 0.0):
+    """Node coordinates and Q4 connectivity (0-based, CCW) of an nx x ny grid."""
+    ii, jj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    X = np.zeros((nx * ny, 3))
+    X[:, 0] = x0 + ii.ravel() * h
+    X[:, 1] = y0 + jj.ravel() * h
+    ei, ej = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), indexing="xy")
+    ei = ei.ravel(); ej = ej.ravel()
+    n0 = ei + nx * ej
+    elems = np.stack([n0, n0 + 1, n0 + 1 + nx, n0 + nx], axis=1)
+    centers = np.stack([x0 + (ei + 0.5) * h, y0 + (ej + 0.5) * h], axis=1)
+    return X, elems, centers
+
+
+def grid3d(nx: int, ny: int, nz: int, h: float):
+    """Node coordinates and Hex8 connectivity (0-based) of an nx x ny x nz grid."""
+    kk, jj, ii = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    X = np.stack([ii.ravel() * h, jj.ravel() * h, kk.ravel() * h], axis=1).astype(np.float64)
+    ek, ej, ei = np.meshgrid(np.arange(nz - 1), np.arange(ny - 1), np.arange(nx - 1), indexing="ij")
+    ei = ei.ravel(); ej = ej.ravel(); ek = ek.ravel()
+    n0 = ei + nx * (ej + ny * ek)
+    sxy = nx * ny
+    bot = np.stack([n0, n0 + 1, n0 + 1 + nx, n0 + nx], axis=1)
+    elems = np.concatenate([bot, bot + sxy], axis=1)
+    centers = np.stack([(ei + 0.5) * h, (ej + 0.5) * h, (ek + 0.5) * h], axis=1)
+    return X, elems, centers
+
+
+def plate2d(nx: int, ny: int, h: float, *, pd_mask: Callable[[np.ndarray], np.ndarray],
+            hole: Optional[Tuple[float, float, float]] = None,
+            cracks: Sequence[np.ndarray] = (), title: str = "plate",
+            material=(72e9, 0.22, 2440.0, 1.0e6, 1.0e8), protype: int = 1,
+            top_velocity: Optional[float] = 0.05, top_value: float = 0.0) -> Mesh:
+    """Plate of nx x ny nodes: bottom edge fixed (UX, UY), top edge UY driven."""
+    X, elems, centers = grid2d(nx, ny, h)
+    keep = np.ones(len(elems), dtype=bool)
+    if hole is not None:
+        cx, cy, r = hole
+        keep &= (centers[:, 0] - cx) ** 2 + (centers[:, 1] - cy) ** 2 >= r * r
+    elems, centers = elems[keep], centers[keep]
+    algo = np.where(pd_mask(centers), 1, 2).astype(np.int64)
+    Xc, el1, algo, newid = _compact(X, elems, algo)
+    ids = np.arange(nx * ny)
+    jrow = ids // nx
+    bottom = newid[ids[jrow == 0]]; bottom = bottom[bottom >= 0] + 1
+    top = newid[ids[jrow == ny - 1]]; top = top[top >= 0] + 1
+    ebcs = [EBC(0, 0.0, bottom), EBC(1, 0.0, bottom),
+            EBC(1, top_value, top, velocity=top_velocity)]
+    E, nu, rho, KIc, sig = material
+    return Mesh(title, 2, protype, E, nu, rho, KIc, sig, Xc, el1, algo, ebcs, [],
+                np.zeros(0, dtype=np.int64), [np.asarray(c, dtype=np.float64) for c in cracks])
+
+
+def box3d(nx: int, ny: int, nz: int, h: float, *, pd_mask: Callable[[np.ndarray], np.ndarray],
+          hole: Optional[Tuple[float, float, float]] = None,
+          cracks: Sequence[np.ndarray] = (), title: str = "box",
+          material=(200e9, 0.3, 7850.0, 1.0e6, 1.0e8), x_velocity: Optional[float] = 0.1,
+          pin_rigid: bool = False) -> Mesh:
+    """Box of nx x ny x nz nodes pulled on both x faces (UX = -v, +v)."""
+    X, elems, centers = grid3d(nx, ny, nz, h)
+    keep = np.ones(len(elems), dtype=bool)
+    if hole is not None:
+        cx, cy, r = hole
+        keep &= (centers[:, 0] - cx) ** 2 + (centers[:, 1] - cy) ** 2 >= r * r
+    elems, centers = elems[keep], centers[keep]
+    algo = np.where(pd_mask(centers), 1, 2).astype(np.int64)
+    Xc, el1, algo, newid = _compact(X, elems, algo)
+    ids = np.arange(nx * ny * nz)
+    ix = ids % nx
+    left = newid[ids[ix == 0]]; left = left[left >= 0] + 1
+    right = newid[ids[ix == nx - 1]]; right = right[right >= 0] + 1
+    vl = None if x_velocity is None else -x_velocity
+    ebcs = [EBC(0, 0.0, left, velocity=vl), EBC(0, 0.0, right, velocity=x_velocity)]
+    if pin_rigid:
+        # fix UY/UZ on the x = 0 face so that the static problem is well posed
+        ebcs.append(EBC(1, 0.0, left))
+        ebcs.append(EBC(2, 0.0, left))
+    E, nu, rho, KIc, sig = material
+    return Mesh(title, 3, -1, E, nu, rho, KIc, sig, Xc, el1, algo, ebcs, [],
+                np.zeros(0, dtype=np.int64), [np.asarray(c, dtype=np.float64) for c in cracks])
+
+
+# --------------------------------------------------------------------------
+# named workloads
+# --------------------------------------------------------------------------
+
+def plate_strip_crack(n: int = 101, L: float = 0.05, strip_frac: float = 0.4,
+                      crack_len: float = 0.01, title: str = "plateStrip") -> Mesh:
+    """n x n node square plate, central vertical PD strip, edge pre-crack in the strip.
+
+    The strip covers the central ``strip_frac`` of the width (41 node columns for
+    n = 101).  The crack starts a quarter element inside the strip's left
+    edge, runs ``crack_len`` in +x at mid-height, and sits half an element above
+    a node row so that no node lies on it.
+    """
+    h = L / (n - 1)
+    ne = n - 1
+    c0 = int(round(ne * (1.0 - strip_frac) / 2.0))
+    c1 = ne - c0
+    xs0 = c0 * h
+    y_c = (ne // 2) * h + 0.5 * h
+
+    def pd_mask(cent):
+        return (cent[:, 0] > xs0) & (cent[:, 0] < c1 * h)
+
+    crack = np.array([[xs0 + 0.25 * h, y_c, 0.0], [xs0 + 0.25 * h + crack_len, y_c, 0.0]])
+    return plate2d(n, n, h, pd_mask=pd_mask, cracks=[crack], title=title)
+
+
+def box_hole(nx: int = 121, ny: int = 61, nz: int = 21, h: float = 1e-3,
+             radius: float = 8e-3, pd_x: int = 40, pd_y: int = 40,
+             title: str = "boxHole") -> Mesh:
+    """Hex8 box with a central cylindrical hole and a pd_x x pd_y element PD zone."""
+    cx = (nx - 1) * h / 2.0
+    cy = (ny - 1) * h / 2.0
+    x0 = cx - pd_x * h / 2.0; x1 = cx + pd_x * h / 2.0
+    y0 = cy - pd_y * h / 2.0; y1 = cy + pd_y * h / 2.0
+
+    def pd_mask(cent):
+        return (cent[:, 0] > x0) & (cent[:, 0] < x1) & (cent[:, 1] > y0) & (cent[:, 1] < y1)
+
+    return box3d(nx, ny, nz, h, pd_mask=pd_mask, hole=(cx, cy, radius), title=title)
+
+
+def write_case(mesh: Mesh, outdir: str, name: str, **cmd) -> str:
+    """Write ``<name>.lis`` and ``<name>.in`` into outdir; return the command path."""
+    os.makedirs(outdir, exist_ok=True)
+    lis = os.path.join(outdir, name + ".lis")
+    write_lis(mesh, lis)
+    cmd_path = os.path.join(outdir, name + ".in")
+    write_cmd(cmd_path, name + ".lis", mesh, **cmd)
+    return cmd_path

@@ -1,0 +1,152 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Builds the reference's own sources (unmodified, against the shims in
+oracle/ref/shim) into oracle/_ref/ref_driver, writes small seeded cases with
+the project's mesh generator, runs the reference on them and packs its
+full-precision (FP64) dumps into ``<case>_<mode>.npz`` next to this script.
+The case inputs (.lis/.in) are copied here too, so the tests can rebuild the
+same models without the reference.
+
+Needs the reference tree (default /root/reference) and SciPy; it is run by
+hand, not by the tests:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "pdlsm-fem_mpi_gb300"))
+import meshgen  # noqa: E402
+
+REF = os.environ.get("PDX_REFERENCE", "/root/reference")
+DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
+
+
+def build_driver() -> None:
+    subprocess.run(["make", "-j8", f"REF={REF}"], cwd=os.path.join(REPO, "oracle", "ref"), check=True)
+
+
+def load_dump(d: str) -> dict:
+    out = {}
+    for line in open(os.path.join(d, "manifest.txt")):
+        parts = line.split()
+        name, dtype, shape = parts[0], parts[1], tuple(int(s) for s in parts[2:])
+        arr = np.fromfile(os.path.join(d, name + ".bin"), dtype=np.float64 if dtype == "f64" else np.int64)
+        out[name] = arr.reshape(shape)
+    return out
+
+
+def run(case_dir: str, cmd: str, mode: str, *extra: str) -> dict:
+    out = tempfile.mkdtemp(prefix="golden_")
+    env = dict(os.environ, PDX_SPSOLVE_SCRIPT=os.path.join(REPO, "oracle", "ref", "spsolve.py"))
+    os.makedirs(os.path.join(case_dir, "Results"), exist_ok=True)
+    subprocess.run([DRIVER, mode, cmd, out, *extra], cwd=case_dir, env=env, check=True,
+                   stdout=subprocess.DEVNULL)
+    d = load_dump(out)
+    shutil.rmtree(out)
+    return d
+
+
+def save(name: str, d: dict) -> None:
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+
+
+def copy_inputs(case_dir: str, name: str) -> None:
+    dst = os.path.join(HERE, "cases", name)
+    os.makedirs(dst, exist_ok=True)
+    for f in os.listdir(case_dir):
+        if f.endswith(".lis") or f.endswith(".in"):
+            shutil.copy(os.path.join(case_dir, f), dst)
+
+
+def plate_case():
+    m = meshgen.plate_strip_crack(n=21, L=0.05, title="p21")
+    m.ebcs[2].velocity = 2.0
+    return m
+
+
+def box_case():
+    m = meshgen.box_hole(nx=13, ny=9, nz=4, h=1e-3, radius=1.5e-3, pd_x=8, pd_y=6, title="b13")
+    m.ebcs[0].velocity = -2.0
+    m.ebcs[1].velocity = 2.0
+    return m
+
+
+def main() -> None:
+    build_driver()
+    work = tempfile.mkdtemp(prefix="golden_cases_")
+    rng = np.random.default_rng(0)
+
+    # ---- 2D plate with PD strip and pre-crack --------------------------
+    m = plate_case()
+    d2 = os.path.join(work, "p21")
+    meshgen.write_case(m, d2, "p21_explicit", solver="DYNAMIC", dt=5e-8, nsteps=60, save=20,
+                       factor=3.015, nlf=1.0, fc="3 2e-4")
+    meshgen.write_case(m, d2, "p21_static", solver="STATIC", dt=1.0, nsteps=1, save=1,
+                       factor=3.015, nlf=1.0, lumped=False)
+    # static load: top edge UY prescribed to 1e-5 through the EBC value
+    ms = plate_case(); ms.ebcs[2].value = 1e-5; ms.ebcs[2].velocity = None
+    meshgen.write_case(ms, d2, "p21s", solver="STATIC", dt=1.0, nsteps=1, save=1,
+                       factor=3.015, nlf=1.0, lumped=False)
+    mn = plate_case(); mn.ebcs[2].velocity = 0.5
+    meshgen.write_case(mn, d2, "p21_newmark", solver="DYNAMIC", dt=2e-7, nsteps=5, save=5,
+                       factor=3.015, nlf=1.0, lumped=False, newmark=(0.5, 0.25))
+    mq = plate_case(); mq.ebcs[2].velocity = 1e-6
+    meshgen.write_case(mq, d2, "p21_quasi", solver="QUASI-STATIC", dt=1.0, nsteps=3, save=3,
+                       factor=3.015, nlf=1.0, lumped=False, fc="0")
+    copy_inputs(d2, "p21")
+
+    save("p21_setup", run(d2, "p21_explicit.in", "setup"))
+    save("p21_coeffs", run(d2, "p21_explicit.in", "coeffs"))
+    n_node = m.n_node
+    u = rng.standard_normal((n_node, 2)) * 1e-6
+    ufile = os.path.join(work, "u_p21.bin")
+    u.astype(np.float64).tofile(ufile)
+    fr = run(d2, "p21_explicit.in", "force", ufile)
+    fr["u_all"] = u
+    save("p21_force", fr)
+    save("p21_explicit", run(d2, "p21_explicit.in", "explicit", "2e-4", "1"))
+    save("p21_static", run(d2, "p21s.in", "static"))
+    save("p21_newmark", run(d2, "p21_newmark.in", "newmark"))
+    save("p21_quasi", run(d2, "p21_quasi.in", "quasi"))
+
+    # ---- 3D box with hole and PD zone -----------------------------------
+    b = box_case()
+    d3 = os.path.join(work, "b13")
+    meshgen.write_case(b, d3, "b13_explicit", solver="DYNAMIC", dt=2e-8, nsteps=30, save=10,
+                       factor=3.015, nlf=1.0, fc="3 2e-4")
+    bs = box_case()
+    bs.ebcs[0].velocity = None; bs.ebcs[1].velocity = None
+    bs.ebcs[0].value = -1e-6; bs.ebcs[1].value = 1e-6
+    bs.ebcs.append(meshgen.EBC(1, 0.0, bs.ebcs[0].nodes))
+    bs.ebcs.append(meshgen.EBC(2, 0.0, bs.ebcs[0].nodes))
+    meshgen.write_case(bs, d3, "b13s", solver="STATIC", dt=1.0, nsteps=1, save=1,
+                       factor=3.015, nlf=1.0, lumped=False)
+    bn = box_case()
+    bn.ebcs[0].velocity = -0.2; bn.ebcs[1].velocity = 0.2
+    meshgen.write_case(bn, d3, "b13_newmark", solver="DYNAMIC", dt=2e-7, nsteps=4, save=4,
+                       factor=3.015, nlf=1.0, lumped=False, newmark=(0.5, 0.25))
+    copy_inputs(d3, "b13")
+    save("b13_setup", run(d3, "b13_explicit.in", "setup"))
+    save("b13_coeffs", run(d3, "b13_explicit.in", "coeffs"))
+    u3 = rng.standard_normal((b.n_node, 3)) * 1e-6
+    u3file = os.path.join(work, "u_b13.bin")
+    u3.astype(np.float64).tofile(u3file)
+    fr3 = run(d3, "b13_explicit.in", "force", u3file)
+    fr3["u_all"] = u3
+    save("b13_force", fr3)
+    save("b13_explicit", run(d3, "b13_explicit.in", "explicit", "2e-4", "1"))
+    save("b13_static", run(d3, "b13s.in", "static"))
+    save("b13_newmark", run(d3, "b13_newmark.in", "newmark"))
+    shutil.rmtree(work)
+
+
+if __name__ == "__main__":
+    main()
