@@ -1,0 +1,152 @@
+/*
+ * pdx.h - C ABI of the GB300 PDLSM-FEM hot path.
+ *
+ * The reference (QibangLiu/PDLSM-FEM_mpi) is one MPI executable with no
+ * library API.  This header is the seam a host program binds instead of the
+ * reference's internals; every entry point names the reference function it
+ * replaces.  Plain C types only: the caller owns every host pointer, the
+ * library owns the device buffers of a model.  Errors are returned as
+ * pdx_status codes (the reference prints and exit()s); pdx_last_error() gives
+ * the message of the last failing call on the calling thread.  All compute
+ * runs on one GPU; a model is used from one host thread at a time and its work
+ * is ordered on the model's own CUDA stream.
+ */
+#ifndef PDX_H
+#define PDX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pdx_status {
+  PDX_OK = 0,
+  PDX_ERR_IO = 1,           /* a file cannot be opened or written */
+  PDX_ERR_PARSE = 2,        /* malformed command or mesh file, bad keyword value */
+  PDX_ERR_UNSUPPORTED = 3,  /* input outside this library's scope (Tri3/Tet4, FC 1/2, ...) */
+  PDX_ERR_INVALID = 4,      /* bad argument (null pointer, wrong size, wrong state) */
+  PDX_ERR_CUDA = 5,         /* a CUDA runtime call failed */
+  PDX_ERR_SINGULAR = 6,     /* a PDLSM moment matrix is singular (reference: dgesv info > 0) */
+  PDX_ERR_NOCONV = 7,       /* Krylov solve did not reach the tolerance */
+  PDX_ERR_NODEVICE = 8,     /* compute requested on a model created without a device */
+  PDX_ERR_NUMERIC = 9       /* NaN or Inf detected in the state */
+} pdx_status;
+
+typedef struct pdx_model pdx_model;
+
+typedef struct pdx_options {
+  int device;      /* CUDA device ordinal; -1 builds the host setup only (no compute) */
+  int precision;   /* -1: PRECISION keyword of the command file; 0 FP64; 1 mixed (FP32 forces) */
+  int lanes;       /* lanes per family in the step kernel (4, 8, 16, 32); 0 = autotuned */
+  int verbose;
+} pdx_options;
+
+typedef struct pdx_model_info {
+  int dim, n_node, n_elem, n_eq, n_fam, n_pdbe, n_fe, n_fe_classes;
+  int64_t n_bond, nnz;
+  int solver;      /* 0 dynamic, 1 static, 2 quasi-static (SOLVER keyword) */
+  int newmark, lumped, fail_flag, precision, nsteps, save_freq, lanes;
+  double dt, min_delta, max_delta, s0, s0_pert;
+} pdx_model_info;
+
+typedef struct pdx_solve_opts {
+  int method;      /* 0 Jacobi PCG, 1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 mixed PCG + FP64 refinement */
+  double rtol;     /* relative true residual ||b - A x|| / ||b|| */
+  int max_iter;
+  int use_x0;      /* 1: x holds the initial guess */
+} pdx_solve_opts;
+
+typedef struct pdx_solve_info {
+  int iterations;
+  double rel_residual;   /* true FP64 residual ||b - A x|| / ||b|| */
+  double seconds;        /* device time of the solve */
+  int converged;
+} pdx_solve_info;
+
+const char* pdx_last_error(void);
+const char* pdx_version(void);
+
+/* Reads the command file and the mesh it names, then builds the model exactly
+ * as pdsolve::pdsolve + setDatModel do (SourceFiles/Solver/pdsolve.cpp:20-151,
+ * fioFile.cpp:54-462, datModel.cpp:58-326): DOF numbering, volumes, block hash,
+ * PD/FE split with crack-cut elements, PD boundary elements, families by the
+ * union rule, pre-crack bond states and the CSR pattern.  With a device it
+ * uploads the model and builds every bond's PDLSM coefficients on the GPU. */
+pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* opts, pdx_model** out);
+void pdx_model_destroy(pdx_model* m);
+pdx_status pdx_model_get_info(const pdx_model* m, pdx_model_info* info);
+
+/* Host setup arrays, by name (count in elements): "eq" (int32, N*d), "vol_node",
+ * "vol_elem" (f64), "node_type", "fam_off" (int64, reference member layout,
+ * member 0 = the node itself), "fam_members" (int32, 0-based), "fam_horizon",
+ * "fam_cdv" (f64), "bond_state0" (uint8, member layout), "pdbe" (int32, n*4),
+ * "pde_idx", "fe_idx" (int32), "csr_ia", "csr_ja" (int64), "mass" (f64, lumped
+ * per equation), "u0" (f64, N*d initial DOF values), "geom" (f64: min delta,
+ * max delta, block size, lbc[3], rtc[3]). */
+pdx_status pdx_model_array_len(const pdx_model* m, const char* name, int64_t* count);
+pdx_status pdx_model_array(const pdx_model* m, const char* name, void* dst, int64_t count);
+
+/* PDLSM moment matrices and bond coefficients computed on the GPU
+ * (shapTens2D/3D pdsolve.cpp:1938-2064, vec_gd2D/3D :2174-2232, matG2D/3D
+ * :2277-2347).  A: n_fam*na*na (na = 5 or 9), g: n_bond*d, dvec: n_bond*(3|6),
+ * G: n_bond*d*d, all with bond state 1.  Any pointer may be NULL. */
+pdx_status pdx_bond_coefficients(pdx_model* m, double* A, double* g, double* dvec, double* G);
+
+/* Internal force of a displacement field, replacing
+ * pdsolve::calinternalForce_CSRformat (pdsolve.cpp:5819-5840) in its explicit
+ * form: F[eq] = -(K u)[eq] over PD bonds, PD boundary elements and FE elements,
+ * u_all = every DOF's value (N*d, prescribed ones included), f_eq = n_eq values.
+ * Uses the model's current bond states. */
+pdx_status pdx_internal_force(pdx_model* m, const double* u_all, double* f_eq);
+
+/* Explicit central-difference solve (pdfemDynamicSolver_CSRformat,
+ * pdsolve.cpp:5842-6090, lumped mass) with critical-stretch bond breaking
+ * (FC 3).  pdx_explicit_init resets the state to the mesh's initial values and
+ * the pre-crack bond states; pdx_explicit_advance runs n steps on the device
+ * (the first call runs step 0, u1 = u0 + dt^2/2 a0).  Steps are launched as a
+ * CUDA graph; no host synchronisation inside. */
+pdx_status pdx_explicit_init(pdx_model* m);
+pdx_status pdx_explicit_advance(pdx_model* m, int nsteps);
+/* Same as advance, timed with CUDA events on the model's stream (ms). */
+pdx_status pdx_explicit_advance_timed(pdx_model* m, int nsteps, double* ms);
+/* One explicit step through host buffers, the contract of timeIntegration_LM
+ * (pdsolve.cpp:5113-5132): u_n and u_nm1 (n_eq, active DOFs) in, u_np1 out;
+ * prescribed values and bond states are the model's.  Copies are inside. */
+pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1);
+int64_t pdx_explicit_step_count(const pdx_model* m);
+
+/* Current state: u_all (N*d), node stress sigma (N*6, slots xx yy zz xy yz zx as
+ * calGlobalNodeStresses pdsolve.cpp:9540-9604), damage phi (N, calLocalDamage
+ * :7338-7373) and bond states in the reference's member layout.  Stress and
+ * damage are recomputed on the GPU from the current state.  NULL skips. */
+pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi, uint8_t* bond_state);
+
+/* Stiffness assembly in the reference's CSR layout and order through a
+ * precomputed scatter map (pdfemAssembleEquasSys_CSRformat :5480-5504,
+ * pdfemQuasiStaticAssembleEquasSys_CSRformat :6434-6462,
+ * pdfemAssembleKNFR_CSRformat :6327-6397).  mode 1 static: F = f_ext - K_pp u_p;
+ * mode 2 quasi-static: F = f_ext - K u_all; mode 3 Newmark: a = beta dt^2 K + M,
+ * F = f_ext - K v.  v_all: N*d DOF values (NULL = model state).  Outputs: ia
+ * (n_eq+1), ja (nnz), a (nnz), f (n_eq); any may be NULL. */
+pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t* ia, int64_t* ja,
+                            double* a, double* f);
+
+/* Sparse solve replacing calMatrixOperations::cluster_PARDISO_64Solver
+ * (calMatrixOperations.cpp:378-498): zero-based CSR, real unsymmetric, one
+ * right-hand side, caller-owned host arrays.  The reference factorises with
+ * MKL PARDISO; this is a Krylov solve on the GPU judged by the true FP64
+ * residual. */
+pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const double* a,
+                         const double* rhs, double* x, const pdx_solve_opts* opts, pdx_solve_info* info);
+
+/* Runs the solver the command file selects (pdsolve::pdfemSolver,
+ * pdsolve.cpp:5073-5103) and writes the reference's outputs under
+ * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM). */
+pdx_status pdx_run(pdx_model* m, const char* results_dir);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PDX_H */

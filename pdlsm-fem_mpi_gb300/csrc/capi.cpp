@@ -1,0 +1,702 @@
+// C ABI (include/pdx.h): model lifecycle, upload, PDLSM coefficient build,
+// internal force, explicit stepping, state export, CSR assembly, sparse solve.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "model_impl.h"
+
+namespace pdx {
+
+const int kEqTemps = 8;
+bool prepare_model(pdx_model* m, Error& err);
+
+namespace {
+thread_local std::string g_err;
+
+template <typename T>
+T* upload(pdx_model* m, const std::vector<T>& h) {
+  T* d = m->buf.alloc<T>(h.size());
+  if (d && !h.empty()) cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, m->stream);
+  return d;
+}
+
+int nv_of(int dim) { return dim == 2 ? 3 : 6; }
+
+std::vector<float> to_f32(const std::vector<double>& v) {
+  std::vector<float> r(v.size());
+  for (size_t i = 0; i < v.size(); i++) r[i] = (float)v[i];
+  return r;
+}
+
+// NBC value after r increments, r = 0..nsteps+1 (rows of the table)
+std::vector<double> nbc_table(const pdx_model* m, int rows) {
+  const auto& nb = m->mesh.nbcs;
+  std::vector<double> t((size_t)rows * nb.size(), 0.0);
+  for (size_t b = 0; b < nb.size(); b++) {
+    double v = nb[b].value;
+    for (int r = 0; r < rows; r++) {
+      t[(size_t)r * nb.size() + b] = v;
+      if (nb[b].varying) v = v + m->cmd.dt * nb[b].velocity;
+    }
+  }
+  return t;
+}
+
+}  // namespace
+
+pdx_status set_error(pdx_status code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+pdx_status cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return PDX_OK;
+  return set_error(PDX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static pdx_status upload_model(pdx_model* m) {
+  const Setup& s = m->setup;
+  const Prepared& p = m->prep;
+  const Mesh& me = m->mesh;
+  const int D = me.dim, N = me.n_node;
+  DevView& v = m->view;
+  v = DevView{};
+  v.dim = D;
+  v.n_node = N;
+  v.n_fam = (int)s.fam_node.size();
+  v.n_feonly = (int)p.feonly.size();
+  v.n_eq = s.n_eq;
+  v.n_bond = (int64_t)p.nbr.size();
+  v.n_corr_bond = (int)p.n_corr;
+  v.X = upload(m, me.X);
+  std::vector<float4> xf(N);
+  for (int k = 0; k < N; k++)
+    xf[k] = make_float4((float)me.X[3 * k], (float)me.X[3 * k + 1], (float)me.X[3 * k + 2], 0.f);
+  v.Xf = upload(m, xf);
+  v.eq = upload(m, s.eq);
+  v.mass = upload(m, p.mass_node);
+  v.bcflag = upload(m, p.bcflag);
+  v.dtv = upload(m, p.dtv);
+  v.fam_node = upload(m, s.fam_node);
+  v.fam_ptr = upload(m, p.fam_ptr);
+  v.fam_corr = upload(m, p.fam_corr);
+  m->d_intact = upload(m, p.fam_intact);
+  v.fam_intact = m->d_intact;
+  v.feonly_node = upload(m, p.feonly);
+  v.nbr = upload(m, p.nbr);
+  m->d_state = upload(m, p.state_bits);
+  v.state = m->d_state;
+  const int NC = D == 2 ? 3 : 6;
+  double* coef64 = m->buf.alloc<double>((size_t)NC * v.n_bond);
+  float* coef32 = m->buf.alloc<float>((size_t)NC * v.n_bond);
+  double* corr64 = m->buf.alloc<double>((size_t)D * D * std::max<int64_t>(p.n_corr, 1));
+  float* corr32 = m->buf.alloc<float>((size_t)D * D * std::max<int64_t>(p.n_corr, 1));
+  double* cvec = m->buf.alloc<double>((size_t)D * v.n_bond);
+  v.coef64 = coef64; v.coef32 = coef32; v.corr64 = corr64; v.corr32 = corr32; v.cvec = cvec;
+  v.fe_conn = upload(m, p.fe_conn);
+  v.fe_cls = upload(m, p.fe_cls);
+  v.ke64 = upload(m, p.ke);
+  v.ke32 = upload(m, to_f32(p.ke));
+  m->d_me = upload(m, p.me);
+  v.fe_adj_ptr = upload(m, p.fe_adj_ptr);
+  v.fe_adj = upload(m, p.fe_adj);
+  v.n_nbc = (int)me.nbcs.size();
+  if (v.n_nbc) {
+    v.ext_ptr = upload(m, p.ext_ptr);
+    v.ext_nbc = upload(m, p.ext_nbc);
+    v.ext_f = upload(m, p.ext_f);
+    m->d_nbcval = upload(m, nbc_table(m, m->cmd.nsteps + 2));
+  }
+  v.s0 = m->cmd.s0;
+  v.s0_pert = m->cmd.s0_pert;
+  v.s0_seed = m->cmd.s0_seed;
+  v.fail3 = m->cmd.fail_flag == 3 ? 1 : 0;
+  m->d_D = upload(m, p.D);
+  m->d_bgp = upload(m, p.bgp);
+  m->d_L = upload(m, p.L);
+  m->d_fam_cdv = upload(m, s.fam_cdv);
+  m->d_ia = upload(m, s.csr_ia);
+  std::vector<int> ja32(s.csr_ja.begin(), s.csr_ja.end());
+  m->d_ja = upload(m, ja32);
+  m->d_rel_bond = upload(m, p.rel_bond);
+  m->d_rel_self = upload(m, p.rel_self);
+  m->d_rel_fe = upload(m, p.rel_fe);
+  for (int i = 0; i < 2; i++) {
+    m->d_u[i] = m->buf.alloc<double>((size_t)N * D);
+    m->d_uf[i] = m->buf.alloc<float4>((size_t)N);
+  }
+  m->d_sigma = m->buf.alloc<double>((size_t)N * 6);
+  m->d_phi = m->buf.alloc<double>((size_t)N);
+  m->d_tmp_all = m->buf.alloc<double>((size_t)N * D);
+  for (int i = 0; i < kEqTemps; i++) m->d_tmp_eq[i] = m->buf.alloc<double>((size_t)std::max(s.n_eq, 1));
+  m->d_Kval = m->buf.alloc<double>((size_t)std::max<int64_t>((int64_t)s.csr_ja.size(), 1));
+  // coefficients
+  CoeffArgs ca{};
+  ca.dim = D;
+  ca.n_fam = v.n_fam;
+  ca.n_bond = v.n_bond;
+  ca.n_corr = std::max<int64_t>(p.n_corr, 1);
+  ca.X = v.X;
+  ca.vol = upload(m, s.vol_node);
+  ca.fam_node = v.fam_node;
+  ca.fam_ptr = v.fam_ptr;
+  ca.nbr = v.nbr;
+  ca.fam_delta = upload(m, s.fam_delta);
+  ca.fam_cdv = m->d_fam_cdv;
+  ca.fam_corr = v.fam_corr;
+  ca.wd = upload(m, p.wd);
+  ca.fam_wd = upload(m, p.fam_wd);
+  ca.nlf = m->cmd.nlf;
+  ca.lambda = p.lambda;
+  ca.mu = p.mu;
+  ca.coef64 = coef64; ca.coef32 = coef32; ca.corr64 = corr64; ca.corr32 = corr32; ca.cvec = cvec;
+  int* derr = m->buf.alloc<int>(1);
+  cudaMemsetAsync(derr, 0, sizeof(int), m->stream);
+  ca.err = derr;
+  v.n_corr_bond = (int)ca.n_corr;
+  for (void* pp : m->buf.ptrs)
+    if (!pp) return set_error(PDX_ERR_CUDA, "device allocation failed");
+  pdx_status st = cuda_check(launch_coeff(ca, m->stream), "coefficient kernel launch");
+  if (st) return st;
+  int herr = 0;
+  cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+  st = cuda_check(cudaStreamSynchronize(m->stream), "coefficient kernel");
+  if (st) return st;
+  if (herr) {
+    const int f = herr - 1;
+    return set_error(PDX_ERR_SINGULAR, "moment matrix of family " + std::to_string(f) + " (node " +
+                                           std::to_string(m->setup.fam_node[f] + 1) + ") is singular");
+  }
+  return PDX_OK;
+}
+
+pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi) {
+  StressArgs a{};
+  a.v = m->view;
+  a.u = d_u_all;
+  a.D = m->d_D;
+  a.bgp = m->d_bgp;
+  a.L = m->d_L;
+  a.protype = m->mesh.protype;
+  a.nu = m->mesh.nu;
+  a.sigma = sigma ? m->d_sigma : nullptr;
+  a.phi = phi ? m->d_phi : nullptr;
+  return cuda_check(launch_stress(a, m->stream), "stress kernel");
+}
+
+static StepArgs step_args(pdx_model* m, int mode, int64_t step_index) {
+  StepArgs a{};
+  a.v = m->view;
+  a.u_n = m->d_u[m->cur];
+  a.u_next = m->d_u[1 - m->cur];
+  a.uf_n = m->d_uf[m->cur];
+  a.uf_next = m->d_uf[1 - m->cur];
+  a.dt = m->cmd.dt;
+  a.mode = mode;
+  if (m->view.n_nbc) {
+    int64_t row = std::min<int64_t>(step_index + 1, m->cmd.nsteps + 1);
+    a.nbc_val = m->d_nbcval + row * m->view.n_nbc;
+  }
+  return a;
+}
+
+pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index) {
+  StepArgs a = step_args(m, mode, step_index);
+  if (mode == 2) {
+    a.u_next = m->d_u[m->cur];   // not written in mode 2
+    a.uf_next = m->d_uf[m->cur];
+  }
+  pdx_status st = cuda_check(launch_step(a, m->mixed, m->lanes, m->stream), "explicit step kernel");
+  if (st) return st;
+  if (mode != 2) m->cur ^= 1;
+  return PDX_OK;
+}
+
+// K (mode 1, 2) or K_N = beta dt^2 K + M (mode 3) into d_Kval and
+// F = f_ext(row) - K_full v into d_tmp_eq[0]; d_v_all is already masked for mode 1.
+pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row) {
+  const int64_t nnz = (int64_t)m->setup.csr_ja.size();
+  cudaMemsetAsync(m->d_Kval, 0, nnz * 8, m->stream);
+  AsmArgs aa{};
+  aa.v = m->view;
+  aa.ia = m->d_ia;
+  aa.rel_bond = m->d_rel_bond;
+  aa.rel_self = m->d_rel_self;
+  aa.rel_fe = m->d_rel_fe;
+  aa.table = m->view.ke64;
+  aa.a = m->d_Kval;
+  aa.with_pd = 1;
+  aa.fam_cdv = m->d_fam_cdv;
+  pdx_status st = cuda_check(launch_assemble(aa, m->stream), "assembly kernel");
+  if (st) return st;
+  if (mode == 3) {
+    if (!m->d_Mval) {
+      m->d_Mval = m->buf.alloc<double>((size_t)std::max<int64_t>(nnz, 1));
+      cudaMemsetAsync(m->d_Mval, 0, nnz * 8, m->stream);
+      AsmArgs ma = aa;
+      ma.table = m->d_me;
+      ma.a = m->d_Mval;
+      ma.with_pd = 0;
+      ma.pd_diag_rho = m->mesh.rho;
+      st = cuda_check(launch_assemble(ma, m->stream), "mass assembly kernel");
+      if (st) return st;
+    }
+    // K_N = K * beta * dt * dt + M  (pdfemAssembleKNFR_CSRformat :6392-6395)
+    st = cuda_check(launch_newmark_matrix(nnz, m->d_Kval, m->d_Mval, m->cmd.beta, m->cmd.dt, m->stream), "K_N");
+    if (st) return st;
+  }
+  ForceArgs fa{};
+  fa.v = m->view;
+  fa.u = d_v_all;
+  fa.f_eq = m->d_tmp_eq[0];
+  if (m->view.n_nbc) fa.nbc_val = m->d_nbcval + (int64_t)nbc_row * m->view.n_nbc;
+  fa.ext_scale = 1.0;
+  return cuda_check(launch_force(fa, m->stream), "force kernel");
+}
+
+}  // namespace pdx
+
+using namespace pdx;
+
+extern "C" {
+
+const char* pdx_last_error(void) { return g_err.c_str(); }
+const char* pdx_version(void) { return "pdlsm-gb300 0.1"; }
+
+pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* opts, pdx_model** out) {
+  if (!cmd_path || !out) return set_error(PDX_ERR_INVALID, "null argument");
+  *out = nullptr;
+  pdx_options o{0, -1, 0, 0};
+  if (opts) o = *opts;
+  pdx_model* m = new pdx_model();
+  Error err{0, ""};
+  if (!read_command(cmd_path, m->cmd, m->mesh, m->base_dir, err) || !build_setup(m->mesh, m->cmd, m->setup, err) ||
+      !prepare_model(m, err)) {
+    delete m;
+    pdx_status code = err.code == 1 ? PDX_ERR_IO
+                      : err.code == 3 ? PDX_ERR_UNSUPPORTED
+                      : err.code == 6 ? PDX_ERR_SINGULAR
+                                      : PDX_ERR_PARSE;
+    return set_error(code, err.msg);
+  }
+  m->mixed = o.precision >= 0 ? o.precision : m->cmd.precision;
+  m->lanes = o.lanes > 0 ? o.lanes : (m->mesh.dim == 2 ? 4 : 8);
+  if (m->lanes != 4 && m->lanes != 8 && m->lanes != 16 && m->lanes != 32) {
+    delete m;
+    return set_error(PDX_ERR_INVALID, "lanes must be 4, 8, 16 or 32");
+  }
+  if (o.device >= 0) {
+    m->device = o.device;
+    pdx_status st = cuda_check(cudaSetDevice(o.device), "cudaSetDevice");
+    if (!st) st = cuda_check(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!st) st = upload_model(m);
+    if (st) {
+      std::string keep = g_err;
+      pdx_model_destroy(m);
+      g_err = keep;
+      return st;
+    }
+    m->has_device = true;
+    pdx_explicit_init(m);
+  }
+  *out = m;
+  return PDX_OK;
+}
+
+void pdx_model_destroy(pdx_model* m) {
+  if (!m) return;
+  if (m->has_device || m->stream) {
+    cudaSetDevice(m->device);
+    if (m->graph) cudaGraphExecDestroy(m->graph);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    m->buf.free_all();
+    if (m->stream) cudaStreamDestroy(m->stream);
+  }
+  delete m;
+}
+
+pdx_status pdx_model_get_info(const pdx_model* m, pdx_model_info* info) {
+  if (!m || !info) return set_error(PDX_ERR_INVALID, "null argument");
+  pdx_model_info i{};
+  i.dim = m->mesh.dim;
+  i.n_node = m->mesh.n_node;
+  i.n_elem = m->mesh.n_elem;
+  i.n_eq = m->setup.n_eq;
+  i.n_fam = (int)m->setup.fam_node.size();
+  i.n_pdbe = (int)m->setup.pdbe.size();
+  i.n_fe = (int)m->setup.fe.size();
+  i.n_fe_classes = m->prep.n_cls;
+  i.n_bond = (int64_t)m->prep.nbr.size();
+  i.nnz = (int64_t)m->setup.csr_ja.size();
+  i.solver = m->cmd.solver;
+  i.newmark = m->cmd.newmark;
+  i.lumped = m->cmd.lumped;
+  i.fail_flag = m->cmd.fail_flag;
+  i.precision = m->mixed;
+  i.nsteps = m->cmd.nsteps;
+  i.save_freq = m->cmd.save_freq;
+  i.lanes = m->lanes;
+  i.dt = m->cmd.dt;
+  i.min_delta = m->setup.min_delta;
+  i.max_delta = m->setup.max_delta;
+  i.s0 = m->cmd.s0;
+  i.s0_pert = m->cmd.s0_pert;
+  *info = i;
+  return PDX_OK;
+}
+
+static bool array_ref(const pdx_model* m, const std::string& n, const void** ptr, int64_t* count, size_t* esz,
+                      std::vector<double>* tmp) {
+  const Setup& s = m->setup;
+  const Prepared& p = m->prep;
+  auto set = [&](const void* q, size_t c, size_t e) { *ptr = q; *count = (int64_t)c; *esz = e; return true; };
+  if (n == "eq") return set(s.eq.data(), s.eq.size(), 4);
+  if (n == "vol_node") return set(s.vol_node.data(), s.vol_node.size(), 8);
+  if (n == "vol_elem") return set(s.vol_elem.data(), s.vol_elem.size(), 8);
+  if (n == "node_type") return set(s.node_type.data(), s.node_type.size(), 4);
+  if (n == "fam_off") return set(s.fam_off.data(), s.fam_off.size(), 8);
+  if (n == "fam_members") return set(s.fam_members.data(), s.fam_members.size(), 4);
+  if (n == "fam_horizon") return set(s.fam_delta.data(), s.fam_delta.size(), 8);
+  if (n == "fam_cdv") return set(s.fam_cdv.data(), s.fam_cdv.size(), 8);
+  if (n == "bond_state0") return set(s.bond_state.data(), s.bond_state.size(), 1);
+  if (n == "pdbe") return set(s.pdbe.data(), s.pdbe.size() * 4, 4);
+  if (n == "pde_idx") return set(s.pde.data(), s.pde.size(), 4);
+  if (n == "fe_idx") return set(s.fe.data(), s.fe.size(), 4);
+  if (n == "csr_ia") return set(s.csr_ia.data(), s.csr_ia.size(), 8);
+  if (n == "csr_ja") return set(s.csr_ja.data(), s.csr_ja.size(), 8);
+  if (n == "mass") return set(p.mass_eq.data(), p.mass_eq.size(), 8);
+  if (n == "u0") return set(p.u0.data(), p.u0.size(), 8);
+  if (n == "geom") {
+    tmp->assign({s.min_delta, s.max_delta, s.block_size, s.lbc[0], s.lbc[1], s.lbc[2], s.rtc[0], s.rtc[1], s.rtc[2]});
+    return set(tmp->data(), tmp->size(), 8);
+  }
+  if (n == "X") return set(m->mesh.X.data(), m->mesh.X.size(), 8);
+  if (n == "conn") return set(m->mesh.conn.data(), m->mesh.conn.size(), 4);
+  if (n == "elem_nn") return set(m->mesh.elem_nn.data(), m->mesh.elem_nn.size(), 4);
+  if (n == "bcflag") return set(p.bcflag.data(), p.bcflag.size(), 1);
+  if (n == "dtv") return set(p.dtv.data(), p.dtv.size(), 8);
+  if (n == "material") {
+    const Mesh& me = m->mesh;
+    tmp->assign({me.E, me.nu, me.rho, me.KIc, me.sigult, m->cmd.nlf, m->cmd.factor, (double)me.protype,
+                 m->cmd.dt, (double)m->cmd.nsteps, m->cmd.s0, (double)m->cmd.s0_seed, m->cmd.s0_pert});
+    return set(tmp->data(), tmp->size(), 8);
+  }
+  return false;
+}
+
+pdx_status pdx_model_array_len(const pdx_model* m, const char* name, int64_t* count) {
+  if (!m || !name || !count) return set_error(PDX_ERR_INVALID, "null argument");
+  const void* ptr;
+  size_t esz;
+  std::vector<double> tmp;
+  if (!array_ref(m, name, &ptr, count, &esz, &tmp)) return set_error(PDX_ERR_INVALID, std::string("unknown array ") + name);
+  return PDX_OK;
+}
+
+pdx_status pdx_model_array(const pdx_model* m, const char* name, void* dst, int64_t count) {
+  if (!m || !name || !dst) return set_error(PDX_ERR_INVALID, "null argument");
+  const void* ptr;
+  int64_t n;
+  size_t esz;
+  std::vector<double> tmp;
+  if (!array_ref(m, name, &ptr, &n, &esz, &tmp)) return set_error(PDX_ERR_INVALID, std::string("unknown array ") + name);
+  if (count != n) return set_error(PDX_ERR_INVALID, std::string("wrong count for ") + name);
+  if (n) std::memcpy(dst, ptr, (size_t)n * esz);
+  return PDX_OK;
+}
+
+#define NEED_DEVICE(m)                                                                    \
+  do {                                                                                    \
+    if (!(m)) return set_error(PDX_ERR_INVALID, "null model");                            \
+    if (!(m)->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");  \
+    cudaSetDevice((m)->device);                                                           \
+  } while (0)
+
+pdx_status pdx_bond_coefficients(pdx_model* m, double* A, double* g, double* dvec, double* G) {
+  NEED_DEVICE(m);
+  const int D = m->mesh.dim, NA = D == 2 ? 5 : 9, ND = D == 2 ? 3 : 6;
+  const int nf = m->view.n_fam;
+  const int64_t nb = m->view.n_bond;
+  DevBuf tmp;
+  double* dA = tmp.alloc<double>((size_t)nf * NA * NA);
+  double* dg = tmp.alloc<double>((size_t)nb * D);
+  double* dd = tmp.alloc<double>((size_t)nb * ND);
+  double* dG = tmp.alloc<double>((size_t)nb * D * D);
+  int* derr = tmp.alloc<int>(1);
+  if (!dA || !dg || !dd || !dG || !derr) { tmp.free_all(); return set_error(PDX_ERR_CUDA, "allocation failed"); }
+  // scratch outputs so the model's coefficients stay untouched
+  double* c64 = tmp.alloc<double>((size_t)(D == 2 ? 3 : 6) * nb);
+  double* cv = tmp.alloc<double>((size_t)D * nb);
+  double* cr = tmp.alloc<double>((size_t)D * D * std::max<int64_t>(m->prep.n_corr, 1));
+  CoeffArgs ca{};
+  ca.dim = D; ca.n_fam = nf; ca.n_bond = nb; ca.n_corr = std::max<int64_t>(m->prep.n_corr, 1);
+  ca.X = m->view.X;
+  DevBuf t2;
+  ca.vol = t2.alloc<double>(m->setup.vol_node.size());
+  cudaMemcpy((void*)ca.vol, m->setup.vol_node.data(), m->setup.vol_node.size() * 8, cudaMemcpyHostToDevice);
+  double* dl = t2.alloc<double>(m->setup.fam_delta.size());
+  cudaMemcpy(dl, m->setup.fam_delta.data(), m->setup.fam_delta.size() * 8, cudaMemcpyHostToDevice);
+  ca.fam_delta = dl;
+  ca.fam_node = m->view.fam_node; ca.fam_ptr = m->view.fam_ptr; ca.nbr = m->view.nbr;
+  ca.fam_cdv = m->d_fam_cdv;
+  ca.fam_corr = nullptr; ca.wd = nullptr; ca.fam_wd = nullptr;
+  ca.nlf = m->cmd.nlf; ca.lambda = m->prep.lambda; ca.mu = m->prep.mu;
+  ca.coef64 = c64; ca.coef32 = nullptr; ca.corr64 = cr; ca.corr32 = nullptr; ca.cvec = cv;
+  ca.A_out = dA; ca.g_out = dg; ca.d_out = dd; ca.G_out = dG;
+  cudaMemset(derr, 0, sizeof(int));
+  ca.err = derr;
+  pdx_status st = cuda_check(launch_coeff(ca, nullptr), "coefficient kernel");
+  if (!st) st = cuda_check(cudaDeviceSynchronize(), "coefficient kernel");
+  if (!st) {
+    if (A) cudaMemcpy(A, dA, (size_t)nf * NA * NA * 8, cudaMemcpyDeviceToHost);
+    if (g) cudaMemcpy(g, dg, (size_t)nb * D * 8, cudaMemcpyDeviceToHost);
+    if (dvec) cudaMemcpy(dvec, dd, (size_t)nb * ND * 8, cudaMemcpyDeviceToHost);
+    if (G) cudaMemcpy(G, dG, (size_t)nb * D * D * 8, cudaMemcpyDeviceToHost);
+  }
+  tmp.free_all();
+  t2.free_all();
+  return st;
+}
+
+pdx_status pdx_internal_force(pdx_model* m, const double* u_all, double* f_eq) {
+  NEED_DEVICE(m);
+  if (!u_all || !f_eq) return set_error(PDX_ERR_INVALID, "null argument");
+  const size_t nd = (size_t)m->mesh.n_node * m->mesh.dim;
+  cudaMemcpyAsync(m->d_tmp_all, u_all, nd * 8, cudaMemcpyHostToDevice, m->stream);
+  ForceArgs a{};
+  a.v = m->view;
+  a.u = m->d_tmp_all;
+  a.f_eq = m->d_tmp_eq[0];
+  a.nbc_val = nullptr;
+  a.ext_scale = 0.0;
+  pdx_status st = cuda_check(launch_force(a, m->stream), "force kernel");
+  if (st) return st;
+  cudaMemcpyAsync(f_eq, m->d_tmp_eq[0], (size_t)m->setup.n_eq * 8, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "internal force");
+}
+
+pdx_status pdx_explicit_init(pdx_model* m) {
+  NEED_DEVICE(m);
+  const size_t nd = (size_t)m->mesh.n_node * m->mesh.dim;
+  for (int i = 0; i < 2; i++)
+    cudaMemcpyAsync(m->d_u[i], m->prep.u0.data(), nd * 8, cudaMemcpyHostToDevice, m->stream);
+  launch_shadow(m->view, m->d_u[0], m->d_uf[0], m->stream);
+  launch_shadow(m->view, m->d_u[1], m->d_uf[1], m->stream);
+  cudaMemcpyAsync(m->d_state, m->prep.state_bits.data(), m->prep.state_bits.size() * 4, cudaMemcpyHostToDevice,
+                  m->stream);
+  cudaMemcpyAsync(m->d_intact, m->prep.fam_intact.data(), m->prep.fam_intact.size() * 4, cudaMemcpyHostToDevice,
+                  m->stream);
+  m->cur = 0;
+  m->steps_done = 0;
+  return cuda_check(cudaStreamSynchronize(m->stream), "explicit init");
+}
+
+static pdx_status build_graph(pdx_model* m, int gsteps) {
+  if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
+  cudaGraph_t g;
+  const int cur0 = m->cur;
+  pdx_status st = cuda_check(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+  if (st) return st;
+  for (int i = 0; i < gsteps; i++) {
+    StepArgs a = step_args(m, 1, 0);
+    launch_step(a, m->mixed, m->lanes, m->stream);
+    m->cur ^= 1;
+  }
+  st = cuda_check(cudaStreamEndCapture(m->stream, &g), "graph capture end");
+  m->cur = cur0;
+  if (st) return st;
+  st = cuda_check(cudaGraphInstantiate(&m->graph, g, 0), "graph instantiate");
+  cudaGraphDestroy(g);
+  m->graph_steps = gsteps;
+  m->graph_parity = cur0;
+  return st;
+}
+
+static pdx_status advance(pdx_model* m, int nsteps) {
+  const bool graphs = m->view.n_nbc == 0;
+  const int G = 64;
+  int done = 0;
+  pdx_status st = PDX_OK;
+  while (done < nsteps) {
+    const int left = nsteps - done;
+    if (m->steps_done > 0 && graphs && left >= G) {
+      if (!m->graph || m->graph_parity != m->cur) {
+        st = build_graph(m, G);
+        if (st) return st;
+      }
+      st = cuda_check(cudaGraphLaunch(m->graph, m->stream), "graph launch");
+      if (st) return st;
+      m->steps_done += G;
+      done += G;
+      continue;
+    }
+    st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
+    if (st) return st;
+    m->steps_done++;
+    done++;
+  }
+  return PDX_OK;
+}
+
+pdx_status pdx_explicit_advance(pdx_model* m, int nsteps) {
+  NEED_DEVICE(m);
+  if (nsteps < 0) return set_error(PDX_ERR_INVALID, "nsteps < 0");
+  pdx_status st = advance(m, nsteps);
+  if (st) return st;
+  return cuda_check(cudaStreamSynchronize(m->stream), "explicit advance");
+}
+
+pdx_status pdx_explicit_advance_timed(pdx_model* m, int nsteps, double* ms) {
+  NEED_DEVICE(m);
+  if (nsteps < 0 || !ms) return set_error(PDX_ERR_INVALID, "bad argument");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, m->stream);
+  pdx_status st = advance(m, nsteps);
+  cudaEventRecord(e1, m->stream);
+  if (!st) st = cuda_check(cudaEventSynchronize(e1), "explicit advance");
+  float f = 0;
+  cudaEventElapsedTime(&f, e0, e1);
+  *ms = f;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
+pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1) {
+  NEED_DEVICE(m);
+  if (!u_n || !u_nm1 || !u_np1) return set_error(PDX_ERR_INVALID, "null argument");
+  const size_t ne = (size_t)m->setup.n_eq;
+  cudaMemcpyAsync(m->d_tmp_eq[0], u_n, ne * 8, cudaMemcpyHostToDevice, m->stream);
+  cudaMemcpyAsync(m->d_tmp_eq[1], u_nm1, ne * 8, cudaMemcpyHostToDevice, m->stream);
+  launch_scatter_eq(m->view, m->d_tmp_eq[0], m->d_u[m->cur], m->stream);
+  launch_scatter_eq(m->view, m->d_tmp_eq[1], m->d_u[1 - m->cur], m->stream);
+  if (m->mixed) launch_shadow(m->view, m->d_u[m->cur], m->d_uf[m->cur], m->stream);
+  pdx_status st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
+  if (st) return st;
+  m->steps_done++;
+  launch_gather_eq(m->view, m->d_u[m->cur], m->d_tmp_eq[2], m->stream);
+  cudaMemcpyAsync(u_np1, m->d_tmp_eq[2], ne * 8, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "explicit step");
+}
+
+int64_t pdx_explicit_step_count(const pdx_model* m) { return m ? m->steps_done : -1; }
+
+pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi, uint8_t* bond_state) {
+  NEED_DEVICE(m);
+  const int N = m->mesh.n_node, D = m->mesh.dim;
+  // the reference computes node stress before the step's failure pass and
+  // damage after it (pdfemDynamicSolver_CSRformat :6060-6075)
+  pdx_status st = model_stress(m, m->d_u[m->cur], true, false);
+  if (st) return st;
+  if (m->steps_done > 0 && m->view.fail3) st = explicit_step_launch(m, 2, m->steps_done);
+  if (st) return st;
+  st = model_stress(m, m->d_u[m->cur], false, true);
+  if (st) return st;
+  if (u_all) cudaMemcpyAsync(u_all, m->d_u[m->cur], (size_t)N * D * 8, cudaMemcpyDeviceToHost, m->stream);
+  if (sigma) cudaMemcpyAsync(sigma, m->d_sigma, (size_t)N * 6 * 8, cudaMemcpyDeviceToHost, m->stream);
+  if (phi) cudaMemcpyAsync(phi, m->d_phi, (size_t)N * 8, cudaMemcpyDeviceToHost, m->stream);
+  std::vector<uint32_t> bits;
+  if (bond_state) {
+    bits.resize(m->prep.state_bits.size());
+    cudaMemcpyAsync(bits.data(), m->d_state, bits.size() * 4, cudaMemcpyDeviceToHost, m->stream);
+  }
+  st = cuda_check(cudaStreamSynchronize(m->stream), "get state");
+  if (st) return st;
+  if (bond_state) {
+    const auto& s = m->setup;
+    for (size_t f = 0; f < s.fam_node.size(); f++) {
+      bond_state[s.fam_off[f]] = 1;
+      for (int b = m->prep.fam_ptr[f]; b < m->prep.fam_ptr[f + 1]; b++)
+        bond_state[s.fam_off[f] + 1 + (b - m->prep.fam_ptr[f])] = (bits[b >> 5] >> (b & 31)) & 1u;
+    }
+  }
+  return PDX_OK;
+}
+
+pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t* ia, int64_t* ja, double* a,
+                            double* f) {
+  NEED_DEVICE(m);
+  if (mode < 1 || mode > 3) return set_error(PDX_ERR_INVALID, "mode must be 1, 2 or 3");
+  const int N = m->mesh.n_node, D = m->mesh.dim;
+  const int64_t nnz = (int64_t)m->setup.csr_ja.size();
+  const size_t nd = (size_t)N * D;
+  std::vector<double> v(nd);
+  if (v_all) std::memcpy(v.data(), v_all, nd * 8);
+  else cudaMemcpy(v.data(), m->d_u[m->cur], nd * 8, cudaMemcpyDeviceToHost);
+  if (mode == 1)
+    for (size_t i = 0; i < nd; i++)
+      if (m->setup.eq[i] >= 0) v[i] = 0.0;
+  cudaMemcpyAsync(m->d_tmp_all, v.data(), nd * 8, cudaMemcpyHostToDevice, m->stream);
+  pdx_status st = assemble_device(m, mode, m->d_tmp_all, 0);
+  if (st) return st;
+  if (ia) std::memcpy(ia, m->setup.csr_ia.data(), m->setup.csr_ia.size() * 8);
+  if (ja) std::memcpy(ja, m->setup.csr_ja.data(), nnz * 8);
+  if (a) cudaMemcpyAsync(a, m->d_Kval, nnz * 8, cudaMemcpyDeviceToHost, m->stream);
+  if (f) cudaMemcpyAsync(f, m->d_tmp_eq[0], (size_t)m->setup.n_eq * 8, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "assembly");
+}
+
+pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const double* a, const double* rhs,
+                         double* x, const pdx_solve_opts* opts, pdx_solve_info* info) {
+  if (n <= 0 || !ia || !ja || !a || !rhs || !x) return set_error(PDX_ERR_INVALID, "bad argument");
+  pdx_solve_opts o{2, 1e-8, 20000, 0};
+  if (opts) o = *opts;
+  const int64_t nnz = ia[n];
+  std::vector<int> ja32(ja, ja + nnz);
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    return set_error(PDX_ERR_CUDA, "no CUDA device");
+  DevBuf b;
+  int64_t* dia = b.alloc<int64_t>(n + 1);
+  int* dja = b.alloc<int>(nnz);
+  double* da = b.alloc<double>(nnz);
+  double* db = b.alloc<double>(n);
+  double* dx = b.alloc<double>(n);
+  if (!dia || !dja || !da || !db || !dx) {
+    b.free_all();
+    cudaStreamDestroy(s);
+    return set_error(PDX_ERR_CUDA, "allocation failed");
+  }
+  cudaMemcpyAsync(dia, ia, (n + 1) * 8, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dja, ja32.data(), nnz * 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(da, a, nnz * 8, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(db, rhs, n * 8, cudaMemcpyHostToDevice, s);
+  if (o.use_x0) cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, s);
+  else cudaMemsetAsync(dx, 0, n * 8, s);
+  DevCsr A;
+  A.n = n; A.nnz = nnz; A.ia = dia; A.ja = dja; A.a = da;
+  KrylovResult kr;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  cudaError_t ce = krylov_solve(A, db, dx, o.method, o.rtol, o.max_iter, 3, s, &kr);
+  cudaEventRecord(e1, s);
+  cudaMemcpyAsync(x, dx, n * 8, cudaMemcpyDeviceToHost, s);
+  cudaError_t ce2 = cudaStreamSynchronize(s);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b.free_all();
+  cudaStreamDestroy(s);
+  if (ce != cudaSuccess || ce2 != cudaSuccess)
+    return set_error(PDX_ERR_CUDA, std::string("Krylov solve: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ce2));
+  if (info) {
+    info->iterations = kr.iterations;
+    info->rel_residual = kr.rel_residual;
+    info->seconds = ms * 1e-3;
+    info->converged = kr.converged;
+  }
+  if (!kr.converged)
+    return set_error(PDX_ERR_NOCONV, "Krylov solve stopped at relative residual " + std::to_string(kr.rel_residual));
+  return PDX_OK;
+}
+
+}  // extern "C"

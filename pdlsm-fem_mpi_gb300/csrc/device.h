@@ -1,0 +1,163 @@
+// Device-resident model: structure-of-arrays layouts in HBM for nodes, PD
+// families and bonds, FE elements and the CSR stiffness pattern, plus the
+// launch wrappers of the kernels in k_*.cu.  Bond arrays are component-major
+// (coef[c * n_bond + b]) so that the lanes working on one family read
+// consecutive addresses.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace pdx {
+
+constexpr int kMaxFeAdj = 8;      // FE elements around a node (Q4: 4, Hex8: 8)
+
+// Everything a kernel needs, as raw device pointers (passed by value).
+struct DevView {
+  int dim, n_node, n_fam, n_feonly, n_eq;
+  int64_t n_bond;
+  int n_corr_bond;
+  // nodes
+  const double* X;          // n_node*3
+  const float4* Xf;         // n_node (x, y, z, 0) FP32 copy
+  const int* eq;            // n_node*dim
+  const double* mass;       // n_node lumped mass of the node's active DOFs
+  const uint8_t* bcflag;    // bit i: DOF i prescribed and varying (VEBC)
+  const double* dtv;        // n_node*3 per-step increment of varying prescribed DOFs
+  // families
+  const int* fam_node;
+  const int* fam_ptr;       // n_fam+1 bond offsets
+  const int* fam_corr;      // offset of the family's bonds in the PDBE-correction arrays, -1 if none
+  int* fam_intact;          // intact bond count
+  const int* feonly_node;   // nodes without family
+  // bonds
+  const int* nbr;
+  uint32_t* state;          // 1 bit per bond, 1 = intact
+  const double* coef64;     // (3|6) * n_bond symmetric block G*dv_k*dv_m
+  const float* coef32;
+  const double* corr64;     // (4|9) * n_corr_bond general PD-boundary block
+  const float* corr32;
+  const double* cvec;       // dim * n_bond strain-operator columns omega*g*dv_m
+  // FE
+  const int* fe_conn;       // n_fe*8
+  const int* fe_cls;        // n_fe
+  const double* ke64;       // n_cls * nd*nd
+  const float* ke32;
+  const int* fe_adj_ptr;    // n_node+1
+  const int* fe_adj;        // (fe_local << 3) | local node
+  // external force (traction BCs): per node list of (nbc id, unit force)
+  const int* ext_ptr;       // n_node+1 or null
+  const int* ext_nbc;
+  const double* ext_f;      // 3 per entry
+  int n_nbc;
+  // material / failure
+  double s0, s0_pert;
+  uint64_t s0_seed;
+  int fail3;
+};
+
+struct StepArgs {
+  DevView v;
+  const double* u_n;        // n_node*dim, stored DOF values after the previous step
+  double* u_next;           // u_{n-1} in, u_{n+1} out (same buffer)
+  const float4* uf_n;       // FP32 shadow of u_n (mixed)
+  float4* uf_next;
+  const double* nbc_val;    // n_nbc values for this step (null without NBCs)
+  double dt;
+  int mode;                 // 0 first step, 1 regular step, 2 failure pass only
+};
+
+struct ForceArgs {
+  DevView v;
+  const double* u;          // n_node*dim DOF values
+  double* f_eq;             // n_eq output
+  const double* nbc_val;    // add external forces when non-null
+  double ext_scale;
+};
+
+struct CoeffArgs {
+  int dim, n_fam;
+  int64_t n_bond;
+  int64_t n_corr;           // bonds of families with a PD-boundary correction
+  const double* X;
+  const double* vol;
+  const int* fam_node;
+  const int* fam_ptr;
+  const int* nbr;
+  const double* fam_delta;
+  const double* fam_cdv;
+  const int* fam_corr;
+  const double* wd;         // per corrected family: dim x nv matrix W*D
+  const int* fam_wd;        // index into wd per family, -1 none
+  double nlf, lambda, mu;
+  double* coef64;
+  float* coef32;
+  double* corr64;
+  float* corr32;
+  double* cvec;
+  double* A_out;            // optional dumps
+  double* g_out;
+  double* d_out;
+  double* G_out;
+  int* err;                 // set to 1 + family on a singular moment matrix
+};
+
+struct StressArgs {
+  DevView v;
+  const double* u;
+  const double* D;          // nv x nv
+  const double* bgp;        // per class: ngp * nv * nd strain-displacement at stress Gauss points
+  const double* L;          // ngp x ngp extrapolation
+  int protype;
+  double nu;
+  double* sigma;            // n_node*6
+  double* phi;              // n_node
+};
+
+struct AsmArgs {
+  DevView v;
+  const int64_t* ia;
+  const int* rel_bond;      // per bond: column offset of node m in row of node k
+  const int* rel_self;      // per family: column offset of node k in its own row
+  const int* rel_fe;        // per FE adjacency entry: 8 column offsets
+  const double* table;      // element matrix table (Ke or Me classes), nd*nd per class
+  double* a;                // nnz values (accumulated)
+  int with_pd;              // add PD bond blocks
+  double pd_diag_rho;       // >0: add rho*cd_v on the diagonal of family rows (consistent mass)
+  const double* fam_cdv;
+};
+
+// kernel launchers (return cudaError_t of the launch)
+cudaError_t launch_coeff(const CoeffArgs& a, cudaStream_t s);
+cudaError_t launch_step(const StepArgs& a, int mixed, int lanes, cudaStream_t s);
+cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
+cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
+cudaError_t launch_assemble(const AsmArgs& a, cudaStream_t s);
+cudaError_t launch_newmark_predict(const DevView& v, const double* u, const double* vel, const double* acc,
+                                   double dt, double beta, double* upred, cudaStream_t s);
+cudaError_t launch_newmark_update(int n, const double* vel0, const double* a0, const double* a1, double dt,
+                                  double beta, double gamma, double* u_eq, double* vel, cudaStream_t s);
+cudaError_t launch_axpby_scale(int64_t n, const double* x, double alpha, double* y, double beta, cudaStream_t s);
+cudaError_t launch_scatter_eq(const DevView& v, const double* u_eq, double* u_all, cudaStream_t s);
+cudaError_t launch_gather_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s);
+cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStream_t s);
+cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, double beta, double dt, cudaStream_t s);
+cudaError_t launch_shadow(const DevView& v, const double* u_all, float4* uf, cudaStream_t s);
+
+// Krylov solvers on a device CSR matrix (k_krylov.cu)
+struct DevCsr {
+  int64_t n = 0, nnz = 0;
+  const int64_t* ia = nullptr;
+  const int* ja = nullptr;
+  const double* a = nullptr;
+};
+struct KrylovResult {
+  int iterations = 0;
+  double rel_residual = 0;
+  int converged = 0;
+};
+cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
+                         int block_dim, cudaStream_t s, KrylovResult* res);
+cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+
+}  // namespace pdx

@@ -1,0 +1,218 @@
+// pdx_run: the solver selected by the command file (pdsolve::pdfemSolver,
+// pdsolve.cpp:5073-5103), on the GPU, writing the reference's result files.
+//   explicit dynamic, lumped mass   pdfemDynamicSolver_CSRformat   :5842-6090
+//   Newmark implicit dynamic        pdfemDynamicNewmarkSolver_CSRformat :6092-6290
+//   static                          pdfemStaticSolver_CSRformat    :5557-5654
+//   quasi-static                    pdfemQuasiStaticSolver_CSRformat :6464-6590
+// The direct sparse solves of the reference become Krylov solves judged by
+// the true FP64 residual (SOLVE keyword; default BiCGStab, tolerance 1e-8).
+#include <cstdio>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "model_impl.h"
+
+namespace pdx {
+
+namespace {
+
+struct HostState {
+  std::vector<double> u, sigma, phi;
+};
+
+pdx_status fetch(pdx_model* m, const double* d_u, HostState& h) {
+  const int N = m->mesh.n_node, D = m->mesh.dim;
+  h.u.resize((size_t)N * D);
+  h.sigma.resize((size_t)N * 6);
+  h.phi.resize(N);
+  cudaMemcpyAsync(h.u.data(), d_u, h.u.size() * 8, cudaMemcpyDeviceToHost, m->stream);
+  cudaMemcpyAsync(h.sigma.data(), m->d_sigma, h.sigma.size() * 8, cudaMemcpyDeviceToHost, m->stream);
+  cudaMemcpyAsync(h.phi.data(), m->d_phi, h.phi.size() * 8, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "state download");
+}
+
+std::string out_name(const pdx_model* m, const std::string& dir, const std::string& tag) {
+  return dir + "/" + m->mesh.title + "_" + tag + ".vtk";
+}
+
+pdx_status solve_device(pdx_model* m, const double* b, double* x, KrylovResult* kr) {
+  DevCsr A;
+  A.n = m->setup.n_eq;
+  A.nnz = (int64_t)m->setup.csr_ja.size();
+  A.ia = m->d_ia;
+  A.ja = m->d_ja;
+  A.a = m->d_Kval;
+  int method = m->cmd.solve_method;
+  cudaError_t e = krylov_solve(A, b, x, method, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
+  pdx_status st = cuda_check(e, "Krylov solve");
+  if (st) return st;
+  if (!kr->converged) {
+    // BiCGStab as the fallback of a stalled CG on the unsymmetric stiffness
+    if (method != 2) {
+      e = krylov_solve(A, b, x, 2, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
+      st = cuda_check(e, "Krylov solve");
+      if (st) return st;
+    }
+    if (!kr->converged)
+      return set_error(PDX_ERR_NOCONV, "Krylov solve stopped at relative residual " + std::to_string(kr->rel_residual));
+  }
+  return PDX_OK;
+}
+
+pdx_status run_explicit(pdx_model* m, const std::string& dir) {
+  if (!m->cmd.lumped) return set_error(PDX_ERR_UNSUPPORTED, "explicit dynamics needs LUMPMASS ON");
+  pdx_status st = pdx_explicit_init(m);
+  if (st) return st;
+  FILE* rf = std::fopen((dir + "/" + m->mesh.title + "RF.out").c_str(), "w");
+  if (rf) { std::fprintf(rf, "Step\tU\tRFx\tRFy\tRFz\n"); std::fclose(rf); }
+  st = pdx_explicit_advance(m, 1);   // step 0: u1 = u0 + dt^2/2 a0
+  if (st) return st;
+  const int nsteps = m->cmd.nsteps, save = std::max(1, m->cmd.save_freq);
+  int n = 0;
+  while (n < nsteps) {
+    int next = std::min(nsteps, (n / save + 1) * save);
+    st = pdx_explicit_advance(m, next - n);
+    if (st) return st;
+    n = next;
+    HostState h;
+    st = pdx_get_state(m, nullptr, nullptr, nullptr, nullptr);
+    if (st) return st;
+    st = fetch(m, m->d_u[m->cur], h);
+    if (st) return st;
+    write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
+  }
+  return PDX_OK;
+}
+
+pdx_status run_static(pdx_model* m, const std::string& dir) {
+  const int N = m->mesh.n_node, D = m->mesh.dim;
+  std::vector<double> v(m->prep.u0);
+  for (size_t i = 0; i < v.size(); i++)
+    if (m->setup.eq[i] >= 0) v[i] = 0.0;
+  cudaMemcpyAsync(m->d_u[0], v.data(), v.size() * 8, cudaMemcpyHostToDevice, m->stream);
+  pdx_status st = assemble_device(m, 1, m->d_u[0], 0);
+  if (st) return st;
+  double* x = m->d_tmp_eq[1];
+  cudaMemsetAsync(x, 0, (size_t)m->setup.n_eq * 8, m->stream);
+  KrylovResult kr;
+  st = solve_device(m, m->d_tmp_eq[0], x, &kr);
+  if (st) return st;
+  launch_scatter_eq(m->view, x, m->d_u[0], m->stream);
+  m->cur = 0;
+  st = model_stress(m, m->d_u[0], true, true);
+  if (st) return st;
+  HostState h;
+  st = fetch(m, m->d_u[0], h);
+  if (st) return st;
+  (void)N; (void)D;
+  std::printf("static solve: %d iterations, relative residual %.3e\n", kr.iterations, kr.rel_residual);
+  write_vtk(m, out_name(m, dir, "static"), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
+  return PDX_OK;
+}
+
+pdx_status run_quasi(pdx_model* m, const std::string& dir) {
+  pdx_status st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
+  if (st) return st;
+  double* u_all = m->d_u[0];
+  m->cur = 0;
+  const int ne = m->setup.n_eq;
+  double* du = m->d_tmp_eq[1];
+  double* ueq = m->d_tmp_eq[2];
+  for (int n = 1; n <= m->cmd.nsteps; n++) {
+    st = assemble_device(m, 2, u_all, n - 1);
+    if (st) return st;
+    cudaMemsetAsync(du, 0, (size_t)ne * 8, m->stream);
+    KrylovResult kr;
+    st = solve_device(m, m->d_tmp_eq[0], du, &kr);
+    if (st) return st;
+    launch_gather_eq(m->view, u_all, ueq, m->stream);
+    launch_axpby_scale(ne, du, 1.0, ueq, 1.0, m->stream);
+    launch_scatter_eq(m->view, ueq, u_all, m->stream);
+    m->steps_done = n;
+    if (m->view.fail3) {
+      st = model_stress(m, u_all, true, false);
+      if (st) return st;
+      if (m->mixed) launch_shadow(m->view, u_all, m->d_uf[0], m->stream);
+      st = explicit_step_launch(m, 2, n);
+      if (st) return st;
+      st = model_stress(m, u_all, false, true);
+    } else {
+      st = model_stress(m, u_all, true, true);
+    }
+    if (st) return st;
+    if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps || n == 1) {
+      HostState h;
+      st = fetch(m, u_all, h);
+      if (st) return st;
+      write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
+    }
+    launch_advance_prescribed(m->view, u_all, m->stream);
+  }
+  return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
+}
+
+pdx_status run_newmark(pdx_model* m, const std::string& dir) {
+  pdx_status st = pdx_explicit_init(m);
+  if (st) return st;
+  double* u_all = m->d_u[0];
+  m->cur = 0;
+  const int ne = m->setup.n_eq;
+  double* vel = m->d_tmp_eq[1];
+  double* acc = m->d_tmp_eq[2];
+  double* acc1 = m->d_tmp_eq[3];
+  double* ueq = m->d_tmp_eq[4];
+  double* upred = m->d_u[1];
+  cudaMemsetAsync(vel, 0, (size_t)ne * 8, m->stream);
+  cudaMemsetAsync(acc, 0, (size_t)ne * 8, m->stream);
+  for (int n = 1; n <= m->cmd.nsteps; n++) {
+    st = cuda_check(launch_newmark_predict(m->view, u_all, vel, acc, m->cmd.dt, m->cmd.beta, upred, m->stream),
+                    "Newmark predictor");
+    if (st) return st;
+    st = assemble_device(m, 3, upred, n - 1);
+    if (st) return st;
+    cudaMemcpyAsync(acc1, acc, (size_t)ne * 8, cudaMemcpyDeviceToDevice, m->stream);
+    KrylovResult kr;
+    st = solve_device(m, m->d_tmp_eq[0], acc1, &kr);
+    if (st) return st;
+    launch_gather_eq(m->view, u_all, ueq, m->stream);
+    launch_newmark_update(ne, vel, acc, acc1, m->cmd.dt, m->cmd.beta, m->cmd.gamma, ueq, vel, m->stream);
+    launch_scatter_eq(m->view, ueq, u_all, m->stream);
+    launch_advance_prescribed(m->view, u_all, m->stream);
+    std::swap(acc, acc1);
+    m->steps_done = n;
+    if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps) {
+      st = model_stress(m, u_all, true, true);
+      if (st) return st;
+      HostState h;
+      st = fetch(m, u_all, h);
+      if (st) return st;
+      write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
+    }
+  }
+  return cuda_check(cudaStreamSynchronize(m->stream), "Newmark");
+}
+
+}  // namespace
+
+}  // namespace pdx
+
+using namespace pdx;
+
+extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
+  if (!m || !results_dir) return set_error(PDX_ERR_INVALID, "null argument");
+  if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
+  cudaSetDevice(m->device);
+  mkdir(results_dir, 0755);
+  const std::string dir(results_dir);
+  if (m->cmd.fail_flag == 1 || m->cmd.fail_flag == 2) {
+    if (m->cmd.solver != 1)
+      return set_error(PDX_ERR_UNSUPPORTED, "failure criteria FC 1 / FC 2 are not implemented (FC 0 and FC 3 are)");
+  }
+  switch (m->cmd.solver) {
+    case 0: return m->cmd.newmark ? run_newmark(m, dir) : run_explicit(m, dir);
+    case 1: return run_static(m, dir);
+    case 2: return run_quasi(m, dir);
+    default: return set_error(PDX_ERR_PARSE, "solver flag is wrong");
+  }
+}

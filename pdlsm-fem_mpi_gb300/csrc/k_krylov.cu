@@ -1,0 +1,441 @@
+// Krylov solves of K x = b on the GPU, standing beside the reference's
+// direct solve (cluster_PARDISO_64Solver, calMatrixOperations.cpp:378-498,
+// real unsymmetric, one right-hand side).
+//
+//   method 0  PCG, Jacobi preconditioner
+//   method 1  PCG, block-Jacobi (the d x d diagonal block of every node)
+//   method 2  BiCGStab, Jacobi (K is unsymmetric: family k's row uses A_k and
+//             delta_k while row m uses A_m and delta_m)
+//   method 3  PCG in FP32 (FP32 matrix copy and vectors) inside FP64 iterative
+//             refinement: r = b - A x in FP64, A d ~= r in FP32, x += d
+//
+// Convergence is always judged on the true FP64 residual ||b - A x|| / ||b||.
+// Scalars stay on the device; iterations are launched in chunks and the host
+// reads the residual once per chunk.  Reductions are two-pass (per-block
+// partials then one block) so results are bitwise reproducible.
+#include <cmath>
+#include <vector>
+
+#include "device.h"
+
+namespace pdx {
+
+namespace {
+
+constexpr int kRedBlocks = 1024;
+constexpr int kThreads = 256;
+
+template <typename T, int L>
+__global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restrict__ ia, const int* __restrict__ ja,
+                                              const T* __restrict__ a, const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = gt / L;
+  const int lane = (int)(gt % L);
+  T s = 0;
+  if (row < n) {
+    const int64_t p0 = ia[row], p1 = ia[row + 1];
+    for (int64_t p = p0 + lane; p < p1; p += L) s += a[p] * x[ja[p]];
+  }
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (row < n && lane == 0) y[row] = s;
+}
+
+template <typename T>
+__global__ void k_dot_partial(int64_t n, const T* x, const T* y, double* part) {
+  __shared__ double sh[kThreads];
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)x[i] * (double)y[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_final(const double* part, int np, double* out) {
+  __shared__ double sh[kThreads];
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// inverse of the diagonal blocks; blocks given by bptr (rows [bptr[i], bptr[i+1]))
+__global__ void k_block_inverse(int64_t nb, const int64_t* bptr, const int64_t* ia, const int* ja, const double* a,
+                                double* binv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int64_t r0 = bptr[i];
+  const int s = (int)(bptr[i + 1] - r0);
+  double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int r = 0; r < s; r++)
+    for (int64_t p = ia[r0 + r]; p < ia[r0 + r + 1]; p++) {
+      const int64_t c = ja[p] - r0;
+      if (c >= 0 && c < s) M[r][c] = a[p];
+    }
+  double I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int k = 0; k < s; k++) {
+    int p = k;
+    for (int r = k + 1; r < s; r++)
+      if (fabs(M[r][k]) > fabs(M[p][k])) p = r;
+    if (p != k)
+      for (int c = 0; c < 3; c++) {
+        double t = M[k][c]; M[k][c] = M[p][c]; M[p][c] = t;
+        t = I[k][c]; I[k][c] = I[p][c]; I[p][c] = t;
+      }
+    const double d = M[k][k] != 0.0 ? M[k][k] : 1.0;
+    for (int c = 0; c < 3; c++) { M[k][c] /= d; I[k][c] /= d; }
+    for (int r = 0; r < s; r++) {
+      if (r == k) continue;
+      const double f = M[r][k];
+      for (int c = 0; c < 3; c++) { M[r][c] -= f * M[k][c]; I[r][c] -= f * I[k][c]; }
+    }
+  }
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) binv[i * 9 + r * 3 + c] = (r < s && c < s) ? I[r][c] : 0.0;
+}
+
+template <typename T>
+__global__ void k_apply_block(int64_t nb, const int64_t* bptr, const double* binv, const T* r, T* z) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int64_t r0 = bptr[i];
+  const int s = (int)(bptr[i + 1] - r0);
+  double v[3] = {0, 0, 0};
+  for (int c = 0; c < s; c++) v[c] = (double)r[r0 + c];
+  for (int rr = 0; rr < s; rr++) {
+    double acc = 0;
+    for (int c = 0; c < s; c++) acc += binv[i * 9 + rr * 3 + c] * v[c];
+    z[r0 + rr] = (T)acc;
+  }
+}
+
+// x += alpha p ; r -= alpha q   with alpha = num/den from device scalars
+template <typename T>
+__global__ void k_cg_update(int64_t n, const double* num, const double* den, const T* p, const T* q, T* x, T* r) {
+  const double alpha = *den != 0.0 ? *num / *den : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    r[i] = (T)((double)r[i] - alpha * (double)q[i]);
+  }
+}
+
+// p = z + (rz_new / rz_old) p ; rz_old = rz_new (last block thread 0 copies after all)
+template <typename T>
+__global__ void k_cg_dir(int64_t n, const double* rz_new, const double* rz_old, const T* z, T* p) {
+  const double beta = *rz_old != 0.0 ? *rz_new / *rz_old : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = (T)((double)z[i] + beta * (double)p[i]);
+}
+
+__global__ void k_copy_scalar(const double* src, double* dst) { *dst = *src; }
+
+template <typename T>
+__global__ void k_jacobi(int64_t n, const double* dinv, const T* r, T* z) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = (T)(dinv[i] * (double)r[i]);
+}
+
+__global__ void k_diag_inv(int64_t n, const int64_t* ia, const int* ja, const double* a, double* dinv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double d = 0;
+  for (int64_t p = ia[i]; p < ia[i + 1]; p++)
+    if (ja[p] == i) d = a[p];
+  dinv[i] = d != 0.0 ? 1.0 / d : 1.0;
+}
+
+__global__ void k_residual(int64_t n, const double* b, const double* ax, double* r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - ax[i];
+}
+
+template <typename S, typename T>
+__global__ void k_convert(int64_t n, const S* a, T* b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (T)a[i];
+}
+
+template <typename T>
+__global__ void k_sub(int64_t n, const T* b, const T* q, T* r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - q[i];
+}
+
+__global__ void k_add_to(int64_t n, const float* d, double* x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += (double)d[i];
+}
+
+// BiCGStab vector updates with device scalars
+__global__ void k_bicg_p(int64_t n, const double* rho, const double* rho_old, const double* alpha,
+                         const double* omega, const double* r, const double* v, double* p) {
+  const double beta = (*rho / *rho_old) * (*alpha / *omega);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = r[i] + beta * (p[i] - *omega * v[i]);
+}
+__global__ void k_bicg_alpha(const double* rho, const double* r0v, double* alpha) {
+  *alpha = *r0v != 0.0 ? *rho / *r0v : 0.0;
+}
+__global__ void k_bicg_s(int64_t n, const double* alpha, const double* r, const double* v, double* s) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s[i] = r[i] - *alpha * v[i];
+}
+__global__ void k_bicg_omega(const double* ts, const double* tt, double* omega) {
+  *omega = *tt != 0.0 ? *ts / *tt : 0.0;
+}
+__global__ void k_bicg_x(int64_t n, const double* alpha, const double* omega, const double* phat,
+                         const double* shat, const double* s, const double* t, double* x, double* r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += *alpha * phat[i] + *omega * shat[i];
+    r[i] = s[i] - *omega * t[i];
+  }
+}
+
+template <typename T>
+struct Work {
+  T* buf = nullptr;
+  size_t n = 0;
+};
+
+int grid_for(int64_t n) { return (int)std::min<int64_t>((n + kThreads - 1) / kThreads, kRedBlocks); }
+
+struct Ctx {
+  cudaStream_t s;
+  double* part;   // kRedBlocks
+  template <typename T>
+  void dot(int64_t n, const T* x, const T* y, double* out) {
+    const int g = grid_for(n);
+    k_dot_partial<T><<<g, kThreads, 0, s>>>(n, x, y, part);
+    k_dot_final<<<1, kThreads, 0, s>>>(part, g, out);
+  }
+};
+
+template <typename T>
+void spmv_t(int64_t n, double avg, const int64_t* ia, const int* ja, const T* a, const T* x, T* y, cudaStream_t s) {
+  if (avg > 48) {
+    k_spmv<T, 32><<<(int)((n * 32 + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, y);
+  } else if (avg > 12) {
+    k_spmv<T, 8><<<(int)((n * 8 + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, y);
+  } else {
+    k_spmv<T, 2><<<(int)((n * 2 + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, y);
+  }
+}
+
+// Preconditioned CG in precision T on (ia, ja, aT); solves for x given b, both in T.
+// Returns iterations; stops when the recursive residual is below rtol*||b|| or max_iter.
+template <typename T>
+int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, const T* aT, const T* b, T* x,
+             const double* dinv, int64_t nb, const int64_t* bptr, const double* binv, double rtol, int max_iter,
+             double* dscal, T* r, T* z, T* p, T* q) {
+  cudaStream_t s = c.s;
+  double* rz = dscal + 0;
+  double* rz_new = dscal + 1;
+  double* pq = dscal + 2;
+  double* bb = dscal + 3;
+  double* rr = dscal + 4;
+  const int g = grid_for(n);
+  spmv_t<T>(n, avg, ia, ja, aT, x, q, s);
+  k_sub<T><<<g, kThreads, 0, s>>>(n, b, q, r);
+  c.dot<T>(n, b, b, bb);
+  auto precond = [&](const T* rin, T* zout) {
+    if (binv) k_apply_block<T><<<(int)((nb + 255) / 256), 256, 0, s>>>(nb, bptr, binv, rin, zout);
+    else k_jacobi<T><<<g, kThreads, 0, s>>>(n, dinv, rin, zout);
+  };
+  precond(r, z);
+  c.dot<T>(n, r, z, rz);
+  cudaMemcpyAsync(p, z, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  double hb = 0;
+  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double bnorm = std::sqrt(hb);
+  if (bnorm == 0.0) {
+    cudaMemsetAsync(x, 0, n * sizeof(T), s);
+    return 0;
+  }
+  int it = 0;
+  const int chunk = 10;
+  while (it < max_iter) {
+    for (int k = 0; k < chunk && it < max_iter; k++, it++) {
+      spmv_t<T>(n, avg, ia, ja, aT, p, q, s);
+      c.dot<T>(n, p, q, pq);
+      k_cg_update<T><<<g, kThreads, 0, s>>>(n, rz, pq, p, q, x, r);
+      precond(r, z);
+      c.dot<T>(n, r, z, rz_new);
+      k_cg_dir<T><<<g, kThreads, 0, s>>>(n, rz_new, rz, z, p);
+      k_copy_scalar<<<1, 1, 0, s>>>(rz_new, rz);
+    }
+    c.dot<T>(n, r, r, rr);
+    double hr = 0;
+    cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    if (!(std::sqrt(hr) > rtol * bnorm)) break;
+  }
+  return it;
+}
+
+}  // namespace
+
+cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s) {
+  const double avg = A.n ? (double)A.nnz / (double)A.n : 0.0;
+  spmv_t<double>(A.n, avg, A.ia, A.ja, A.a, x, y, s);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
+                         int block_dim, cudaStream_t s, KrylovResult* res) {
+  const int64_t n = A.n;
+  const double avg = n ? (double)A.nnz / (double)n : 0.0;
+  Ctx c{s, nullptr};
+  double* dscal = nullptr;
+  cudaMallocAsync(&c.part, kRedBlocks * sizeof(double), s);
+  cudaMallocAsync(&dscal, 16 * sizeof(double), s);
+  double* dinv = nullptr;
+  cudaMallocAsync(&dinv, n * sizeof(double), s);
+  k_diag_inv<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A.ia, A.ja, A.a, dinv);
+  // diagonal blocks for block-Jacobi: consecutive rows in groups of block_dim
+  int64_t nb = 0;
+  int64_t* bptr = nullptr;
+  double* binv = nullptr;
+  if (method == 1) {
+    const int bd = block_dim > 0 ? block_dim : 3;
+    nb = (n + bd - 1) / bd;
+    std::vector<int64_t> hp(nb + 1);
+    for (int64_t i = 0; i <= nb; i++) hp[i] = std::min<int64_t>(i * bd, n);
+    cudaMallocAsync(&bptr, (nb + 1) * sizeof(int64_t), s);
+    cudaMemcpyAsync(bptr, hp.data(), (nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s);
+    cudaMallocAsync(&binv, nb * 9 * sizeof(double), s);
+    k_block_inverse<<<(int)((nb + 255) / 256), 256, 0, s>>>(nb, bptr, A.ia, A.ja, A.a, binv);
+    cudaStreamSynchronize(s);  // hp leaves scope
+  }
+  double *r, *z, *p, *q, *ax;
+  cudaMallocAsync(&r, n * sizeof(double), s);
+  cudaMallocAsync(&z, n * sizeof(double), s);
+  cudaMallocAsync(&p, n * sizeof(double), s);
+  cudaMallocAsync(&q, n * sizeof(double), s);
+  cudaMallocAsync(&ax, n * sizeof(double), s);
+  const int g = grid_for(n);
+  int iters = 0;
+  if (method == 0 || method == 1) {
+    iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, nb, bptr, binv, rtol, max_iter, dscal, r, z,
+                             p, q);
+  } else if (method == 2) {
+    // BiCGStab, right Jacobi preconditioning
+    double *r0, *v, *ss, *t, *ph, *sh;
+    cudaMallocAsync(&r0, n * sizeof(double), s);
+    cudaMallocAsync(&v, n * sizeof(double), s);
+    cudaMallocAsync(&ss, n * sizeof(double), s);
+    cudaMallocAsync(&t, n * sizeof(double), s);
+    cudaMallocAsync(&ph, n * sizeof(double), s);
+    cudaMallocAsync(&sh, n * sizeof(double), s);
+    double* rho = dscal + 0;
+    double* rho_old = dscal + 1;
+    double* alpha = dscal + 2;
+    double* omega = dscal + 3;
+    double* tmp = dscal + 4;
+    double* tmp2 = dscal + 5;
+    double* bb = dscal + 6;
+    double* rr = dscal + 7;
+    spmv(A, x, ax, s);
+    k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
+    cudaMemcpyAsync(r0, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(v, 0, n * sizeof(double), s);
+    cudaMemsetAsync(p, 0, n * sizeof(double), s);
+    const double ones[4] = {1.0, 1.0, 1.0, 1.0};
+    cudaMemcpyAsync(dscal, ones, 4 * sizeof(double), cudaMemcpyHostToDevice, s);
+    c.dot<double>(n, b, b, bb);
+    double hb = 0;
+    cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const double bnorm = std::sqrt(hb);
+    const int chunk = 10;
+    while (bnorm > 0 && iters < max_iter) {
+      for (int k = 0; k < chunk && iters < max_iter; k++, iters++) {
+        c.dot<double>(n, r0, r, rho);
+        k_bicg_p<<<g, kThreads, 0, s>>>(n, rho, rho_old, alpha, omega, r, v, p);
+        k_jacobi<double><<<g, kThreads, 0, s>>>(n, dinv, p, ph);
+        spmv(A, ph, v, s);
+        c.dot<double>(n, r0, v, tmp);
+        k_bicg_alpha<<<1, 1, 0, s>>>(rho, tmp, alpha);
+        k_bicg_s<<<g, kThreads, 0, s>>>(n, alpha, r, v, ss);
+        k_jacobi<double><<<g, kThreads, 0, s>>>(n, dinv, ss, sh);
+        spmv(A, sh, t, s);
+        c.dot<double>(n, t, ss, tmp);
+        c.dot<double>(n, t, t, tmp2);
+        k_bicg_omega<<<1, 1, 0, s>>>(tmp, tmp2, omega);
+        k_bicg_x<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, x, r);
+        k_copy_scalar<<<1, 1, 0, s>>>(rho, rho_old);
+      }
+      c.dot<double>(n, r, r, rr);
+      double hr = 0;
+      cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      if (!(std::sqrt(hr) > rtol * bnorm) || !std::isfinite(hr)) break;
+    }
+    cudaFreeAsync(r0, s); cudaFreeAsync(v, s); cudaFreeAsync(ss, s);
+    cudaFreeAsync(t, s); cudaFreeAsync(ph, s); cudaFreeAsync(sh, s);
+  } else if (method == 3) {
+    // FP32 PCG inside FP64 iterative refinement
+    float *af, *rf, *df, *zf, *pf, *qf, *wf;
+    cudaMallocAsync(&wf, n * sizeof(float), s);
+    cudaMallocAsync(&af, A.nnz * sizeof(float), s);
+    cudaMallocAsync(&rf, n * sizeof(float), s);
+    cudaMallocAsync(&df, n * sizeof(float), s);
+    cudaMallocAsync(&zf, n * sizeof(float), s);
+    cudaMallocAsync(&pf, n * sizeof(float), s);
+    cudaMallocAsync(&qf, n * sizeof(float), s);
+    k_convert<double, float><<<grid_for(A.nnz), kThreads, 0, s>>>(A.nnz, A.a, af);
+    double* bb = dscal + 8;
+    double* rr = dscal + 9;
+    c.dot<double>(n, b, b, bb);
+    double hb = 0;
+    cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const double bnorm = std::sqrt(hb);
+    for (int outer = 0; outer < 60 && bnorm > 0 && iters < max_iter; outer++) {
+      spmv(A, x, ax, s);
+      k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
+      c.dot<double>(n, r, r, rr);
+      double hr = 0;
+      cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      if (!(std::sqrt(hr) > rtol * bnorm)) break;
+      k_convert<double, float><<<g, kThreads, 0, s>>>(n, r, rf);
+      cudaMemsetAsync(df, 0, n * sizeof(float), s);
+      iters += pcg_core<float>(c, n, avg, A.ia, A.ja, af, rf, df, dinv, 0, nullptr, nullptr, 1e-4,
+                               max_iter - iters, dscal, zf, pf, qf, wf);
+      k_add_to<<<g, kThreads, 0, s>>>(n, df, x);
+    }
+    cudaFreeAsync(wf, s);
+    cudaFreeAsync(af, s); cudaFreeAsync(rf, s); cudaFreeAsync(df, s);
+    cudaFreeAsync(zf, s); cudaFreeAsync(pf, s); cudaFreeAsync(qf, s);
+  }
+  // true residual
+  spmv(A, x, ax, s);
+  k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
+  c.dot<double>(n, r, r, dscal + 10);
+  c.dot<double>(n, b, b, dscal + 11);
+  double h[2] = {0, 0};
+  cudaMemcpyAsync(h, dscal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaError_t err = cudaStreamSynchronize(s);
+  res->iterations = iters;
+  res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+  res->converged = res->rel_residual <= rtol;
+  cudaFreeAsync(r, s); cudaFreeAsync(z, s); cudaFreeAsync(p, s); cudaFreeAsync(q, s); cudaFreeAsync(ax, s);
+  cudaFreeAsync(dinv, s); cudaFreeAsync(c.part, s); cudaFreeAsync(dscal, s);
+  if (bptr) cudaFreeAsync(bptr, s);
+  if (binv) cudaFreeAsync(binv, s);
+  if (err == cudaSuccess) err = cudaGetLastError();
+  return err;
+}
+
+}  // namespace pdx

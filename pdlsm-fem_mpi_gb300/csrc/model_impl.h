@@ -1,0 +1,119 @@
+// Internal definition of pdx_model: host setup, host-prepared device inputs,
+// device buffers and run state.  Shared by capi.cpp and drivers.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/pdx.h"
+#include "device.h"
+#include "model.h"
+
+namespace pdx {
+
+// Host arrays derived from Setup that the kernels need.
+struct Prepared {
+  std::vector<double> mass_node;     // lumped mass per node (active DOFs)
+  std::vector<double> mass_eq;       // per equation, as the reference's cdp_MGlo
+  std::vector<uint8_t> bcflag;       // varying prescribed DOF bits
+  std::vector<double> dtv;           // n_node*3
+  std::vector<double> u0;            // n_node*dim initial DOF values
+  std::vector<int> fam_ptr;          // bond offsets (self excluded)
+  std::vector<int> nbr;              // bond neighbours
+  std::vector<uint32_t> state_bits;  // initial bond states
+  std::vector<int> fam_intact;
+  std::vector<int> fam_corr;         // slot offset or -1
+  std::vector<int> fam_wd;           // W*D index or -1
+  std::vector<double> wd;            // dim x nv per corrected family
+  int64_t n_corr = 0;
+  std::vector<int> feonly;           // FE-only nodes
+  // FE elements (order of Setup::fe)
+  std::vector<int> fe_conn;          // 8 per element
+  std::vector<int> fe_cls;
+  std::vector<double> ke, me, bgp;   // per class tables
+  std::vector<double> L;             // extrapolation matrix
+  std::vector<int> fe_adj_ptr, fe_adj;
+  int n_cls = 0;
+  // traction BCs
+  std::vector<int> ext_ptr, ext_nbc;
+  std::vector<double> ext_f;
+  // scatter map into the CSR pattern
+  std::vector<int> rel_bond, rel_self, rel_fe;
+  std::vector<double> D;             // constitutive matrix
+  double lambda = 0, mu = 0;
+};
+
+struct DevBuf {
+  std::vector<void*> ptrs;
+  template <typename T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return (T*)p;
+  }
+  void free_all() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+}  // namespace pdx
+
+struct pdx_model {
+  pdx::Mesh mesh;
+  pdx::Command cmd;
+  pdx::Setup setup;
+  pdx::Prepared prep;
+  std::string base_dir;
+  int device = -1;
+  int mixed = 0;
+  int lanes = 0;
+  bool has_device = false;
+  cudaStream_t stream = nullptr;
+  pdx::DevBuf buf;
+  pdx::DevView view{};
+  // device arrays kept by name for updates
+  double* d_u[2] = {nullptr, nullptr};
+  float4* d_uf[2] = {nullptr, nullptr};
+  uint32_t* d_state = nullptr;
+  int* d_intact = nullptr;
+  double* d_nbcval = nullptr;        // (nsteps + 2) * n_nbc
+  double* d_D = nullptr;
+  double* d_bgp = nullptr;
+  double* d_L = nullptr;
+  double* d_me = nullptr;
+  int64_t* d_ia = nullptr;
+  int* d_ja = nullptr;
+  int* d_rel_bond = nullptr;
+  int* d_rel_self = nullptr;
+  int* d_rel_fe = nullptr;
+  double* d_fam_cdv = nullptr;
+  double* d_Kval = nullptr;
+  double* d_Mval = nullptr;
+  double* d_sigma = nullptr;
+  double* d_phi = nullptr;
+  double* d_tmp_all = nullptr;       // n_node*dim scratch
+  double* d_tmp_eq[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // explicit run state
+  int cur = 0;                       // index of the buffer holding u_n
+  int64_t steps_done = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  int graph_parity = 0;
+};
+
+namespace pdx {
+pdx_status set_error(pdx_status code, const std::string& msg);
+pdx_status cuda_check(cudaError_t e, const char* what);
+void write_vtk(const pdx_model* m, const std::string& path, const std::vector<double>& u_all,
+               const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);
+pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi);
+pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
+extern const int kEqTemps;
+pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);
+}  // namespace pdx

@@ -1,0 +1,306 @@
+// Host preparation of the arrays the kernels consume, from the model setup:
+//   lumped mass (assembleLumpedMass, pdsolve.cpp:4618-4669),
+//   prescribed-DOF increments (setVaryEssentialBC :5263-5312),
+//   bond lists and initial bond states, per family,
+//   PD-boundary traction weights W_k (2D: 1/2 N per segment, assemblePDBEwork_CSRformat
+//   :4049-4252; 3D: area-weighted normal matrix of every face, normMatArea :2917-2967
+//   and assemblePDBEwork3D_CSRformat :2732-2915) folded with D,
+//   FE stiffness/mass classes: elements whose node positions relative to their
+//   first node agree to 1e-12 of the element size share one Ke / Me (FP64),
+//   node -> FE element adjacency, traction-BC unit forces (pdfemEleLine2N.cpp:45-75,
+//   pdfemEleQuad4N.cpp eleEquivNodalForce), and the scatter map of every bond /
+//   element block into the CSR pattern.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+
+#include "model_impl.h"
+
+namespace pdx {
+
+namespace {
+
+struct VecHash {
+  size_t operator()(const std::vector<int64_t>& v) const {
+    uint64_t h = 1469598103934665603ull;
+    for (int64_t x : v) { h ^= (uint64_t)x; h *= 1099511628211ull; }
+    return (size_t)h;
+  }
+};
+
+void norm_mat_area(const double xN[4][3], bool quad, double Nmat[3][6], bool& ok) {
+  double v1[3], v2[3];
+  for (int i = 0; i < 3; i++) { v1[i] = xN[1][i] - xN[0][i]; v2[i] = xN[2][i] - xN[0][i]; }
+  double N1 = v1[1] * v2[2] - v1[2] * v2[1];
+  double N2 = v2[0] * v1[2] - v1[0] * v2[2];
+  double N3 = v1[0] * v2[1] - v2[0] * v1[1];
+  const double A1 = std::sqrt(N1 * N1 + N2 * N2 + N3 * N3);
+  ok = A1 != 0;
+  double A2 = 0, w = 1.0 / 3;
+  if (quad) {
+    for (int i = 0; i < 3; i++) { v1[i] = xN[3][i] - xN[0][i]; v2[i] = xN[2][i] - xN[0][i]; }
+    const double t1 = v1[1] * v2[2] - v1[2] * v2[1];
+    const double t2 = v2[0] * v1[2] - v1[0] * v2[2];
+    const double t3 = v1[0] * v2[1] - v2[0] * v1[1];
+    A2 = std::sqrt(t1 * t1 + t2 * t2 + t3 * t3);
+    w = 0.25;
+  }
+  const double area = (A1 + A2) * 0.5;
+  N1 = N1 / A1 * area * w;
+  N2 = N2 / A1 * area * w;
+  N3 = N3 / A1 * area * w;
+  std::memset(Nmat, 0, sizeof(double) * 18);
+  Nmat[0][0] = N1; Nmat[1][1] = N2; Nmat[2][2] = N3;
+  Nmat[0][3] = N2; Nmat[0][5] = N3;
+  Nmat[1][3] = N1; Nmat[1][4] = N3;
+  Nmat[2][4] = N2; Nmat[2][5] = N1;
+}
+
+}  // namespace
+
+bool prepare_model(pdx_model* m, Error& err) {
+  const Mesh& me = m->mesh;
+  const Setup& s = m->setup;
+  const Command& c = m->cmd;
+  Prepared& p = m->prep;
+  const int D = me.dim, N = me.n_node;
+  const int NV = D == 2 ? 3 : 6;
+  material_D(me, p.D, p.lambda, p.mu);
+  // lumped mass over all elements, in element order
+  p.mass_node.assign(N, 0.0);
+  for (int e = 0; e < me.n_elem; e++) {
+    const int nn = me.elem_nn[e];
+    const double dv = s.vol_elem[e] / nn;
+    for (int i = 0; i < nn; i++) {
+      const int n = me.conn[(size_t)e * 8 + i];
+      p.mass_node[n] = p.mass_node[n] + dv * me.rho;
+    }
+  }
+  p.mass_eq.assign(s.n_eq, 0.0);
+  for (int k = 0; k < N; k++)
+    for (int i = 0; i < D; i++)
+      if (s.eq[(size_t)k * D + i] >= 0) p.mass_eq[s.eq[(size_t)k * D + i]] = p.mass_node[k];
+  // prescribed DOFs
+  p.bcflag.assign(N, 0);
+  p.dtv.assign((size_t)N * 3, 0.0);
+  p.u0.assign((size_t)N * D, 0.0);
+  for (const auto& b : me.ebcs)
+    for (int n : b.nodes) {
+      p.u0[(size_t)n * D + b.dof] = b.value;
+      if (b.varying) {
+        p.bcflag[n] |= (uint8_t)(1u << b.dof);
+        p.dtv[(size_t)n * 3 + b.dof] = c.dt * b.velocity;
+      }
+    }
+  // bonds
+  const int nf = (int)s.fam_node.size();
+  p.fam_ptr.assign(nf + 1, 0);
+  p.nbr.clear();
+  std::vector<uint8_t> st;
+  for (int f = 0; f < nf; f++) {
+    for (int64_t q = s.fam_off[f] + 1; q < s.fam_off[f + 1]; q++) {
+      p.nbr.push_back(s.fam_members[q]);
+      st.push_back(s.bond_state[q]);
+    }
+    p.fam_ptr[f + 1] = (int)p.nbr.size();
+    if (s.fam_off[f + 1] - s.fam_off[f] < 2) { err.code = 6; err.msg = "a PD family has no member"; return false; }
+  }
+  const int64_t nb = (int64_t)p.nbr.size();
+  p.state_bits.assign((size_t)(nb + 31) / 32 + 1, 0u);
+  p.fam_intact.assign(nf, 0);
+  for (int f = 0; f < nf; f++)
+    for (int b = p.fam_ptr[f]; b < p.fam_ptr[f + 1]; b++)
+      if (st[b]) { p.state_bits[b >> 5] |= 1u << (b & 31); p.fam_intact[f]++; }
+  // PD-boundary weights W per node
+  std::vector<std::vector<double>> W(N);
+  auto addW = [&](int n, const double* w) {
+    if (W[n].empty()) W[n].assign((size_t)D * NV, 0.0);
+    for (int i = 0; i < D * NV; i++) W[n][i] += w[i];
+  };
+  for (const auto& b : s.pdbe) {
+    if (D == 2) {
+      const double* x1 = &me.X[(size_t)b[0] * 3];
+      const double* x2 = &me.X[(size_t)b[1] * 3];
+      const double nx = x2[1] - x1[1], ny = x1[0] - x2[0];
+      const double w[6] = {0.5 * nx, 0.0, 0.5 * ny, 0.0, 0.5 * ny, 0.5 * nx};
+      addW(b[0], w);
+      addW(b[1], w);
+    } else {
+      double xN[4][3];
+      for (int i = 0; i < 4; i++)
+        for (int a = 0; a < 3; a++) xN[i][a] = me.X[(size_t)b[i] * 3 + a];
+      const bool quad = b[3] != b[2];
+      double Nm[3][6];
+      bool ok;
+      norm_mat_area(xN, quad, Nm, ok);
+      if (!ok) { err.code = 2; err.msg = "Area is zero!"; return false; }
+      const int nn = quad ? 4 : 3;
+      for (int i = 0; i < nn; i++) addW(b[i], &Nm[0][0]);
+    }
+  }
+  p.fam_corr.assign(nf, -1);
+  p.fam_wd.assign(nf, -1);
+  p.wd.clear();
+  p.n_corr = 0;
+  for (int f = 0; f < nf; f++) {
+    const int k = s.fam_node[f];
+    if (W[k].empty()) continue;
+    p.fam_wd[f] = (int)(p.wd.size() / ((size_t)D * NV));
+    for (int i = 0; i < D; i++)
+      for (int j = 0; j < NV; j++) {
+        double acc = 0;
+        for (int t = 0; t < NV; t++) acc += W[k][(size_t)i * NV + t] * p.D[(size_t)t * NV + j];
+        p.wd.push_back(acc);
+      }
+    p.fam_corr[f] = (int)p.n_corr;
+    p.n_corr += p.fam_ptr[f + 1] - p.fam_ptr[f];
+  }
+  // FE-only nodes
+  p.feonly.clear();
+  for (int k = 0; k < N; k++)
+    if (s.node_type[k] == 0) p.feonly.push_back(k);
+  // FE elements and stiffness classes
+  const int nen = D == 2 ? 4 : 8;
+  const int nd = nen * D;
+  const int ngp = nen;
+  const int nfe = (int)s.fe.size();
+  p.fe_conn.assign((size_t)nfe * 8, 0);
+  p.fe_cls.assign(nfe, 0);
+  p.ke.clear(); p.me.clear(); p.bgp.clear();
+  std::unordered_map<std::vector<int64_t>, int, VecHash> classes;
+  for (int i = 0; i < nfe; i++) {
+    const int e = s.fe[i];
+    double xN[8][3];
+    for (int j = 0; j < nen; j++) {
+      p.fe_conn[(size_t)i * 8 + j] = me.conn[(size_t)e * 8 + j];
+      for (int a = 0; a < 3; a++) xN[j][a] = me.X[(size_t)me.conn[(size_t)e * 8 + j] * 3 + a];
+    }
+    double Le = 0;
+    for (int j = 1; j < nen; j++)
+      for (int a = 0; a < 3; a++) Le = std::max(Le, std::fabs(xN[j][a] - xN[0][a]));
+    const double q = Le > 0 ? 1e-12 * Le : 1.0;
+    std::vector<int64_t> key;
+    key.reserve(nen * 3);
+    for (int j = 1; j < nen; j++)
+      for (int a = 0; a < 3; a++) key.push_back(std::llround((xN[j][a] - xN[0][a]) / q));
+    key.push_back(std::llround(std::log2(q) * 1e6));
+    auto it = classes.find(key);
+    int cls;
+    if (it == classes.end()) {
+      cls = (int)classes.size();
+      classes.emplace(key, cls);
+      std::vector<double> K((size_t)nd * nd), Me((size_t)nd * nd), B((size_t)ngp * NV * nd);
+      if (D == 2) {
+        double x4[4][3];
+        std::memcpy(x4, xN, sizeof(x4));
+        ke_quad4(x4, p.D.data(), K.data());
+        me_quad4(x4, me.rho, Me.data());
+        b_gauss_quad4(x4, B.data());
+      } else {
+        ke_hex8(xN, p.D.data(), K.data());
+        me_hex8(xN, me.rho, Me.data());
+        b_gauss_hex8(xN, B.data());
+      }
+      p.ke.insert(p.ke.end(), K.begin(), K.end());
+      p.me.insert(p.me.end(), Me.begin(), Me.end());
+      p.bgp.insert(p.bgp.end(), B.begin(), B.end());
+    } else {
+      cls = it->second;
+    }
+    p.fe_cls[i] = cls;
+  }
+  p.n_cls = (int)classes.size();
+  p.L.assign((size_t)ngp * ngp, 0.0);
+  extrap_L(D, p.L.data());
+  // node -> FE element adjacency, in FE element order
+  p.fe_adj_ptr.assign(N + 1, 0);
+  for (int i = 0; i < nfe; i++)
+    for (int j = 0; j < nen; j++) p.fe_adj_ptr[p.fe_conn[(size_t)i * 8 + j] + 1]++;
+  for (int k = 0; k < N; k++) p.fe_adj_ptr[k + 1] += p.fe_adj_ptr[k];
+  p.fe_adj.assign(p.fe_adj_ptr[N], 0);
+  {
+    std::vector<int> fill(p.fe_adj_ptr.begin(), p.fe_adj_ptr.end() - 1);
+    for (int i = 0; i < nfe; i++)
+      for (int j = 0; j < nen; j++) {
+        const int n = p.fe_conn[(size_t)i * 8 + j];
+        p.fe_adj[fill[n]++] = (i << 3) | j;
+      }
+  }
+  for (int k = 0; k < N; k++)
+    if (p.fe_adj_ptr[k + 1] - p.fe_adj_ptr[k] > kMaxFeAdj && D == 3) {
+      err.code = 3; err.msg = "more than 8 FE elements around a node"; return false;
+    }
+  // traction BCs: unit forces per node and NBC
+  {
+    std::map<std::pair<int, int>, std::array<double, 3>> acc;
+    for (size_t bi = 0; bi < me.nbcs.size(); bi++)
+      for (const auto& el : me.nbcs[bi].elems) {
+        double xN[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        const int nn = D == 2 ? 2 : 4;
+        for (int j = 0; j < nn; j++)
+          for (int a = 0; a < 3; a++) xN[j][a] = me.X[(size_t)el[j] * 3 + a];
+        double Fe[12];
+        nbc_unit_force(D, xN, Fe);
+        for (int j = 0; j < nn; j++) {
+          auto& v = acc[{el[j], (int)bi}];
+          for (int a = 0; a < D; a++) v[a] += Fe[j * D + a];
+        }
+      }
+    p.ext_ptr.assign(N + 1, 0);
+    p.ext_nbc.clear();
+    p.ext_f.clear();
+    for (const auto& kv : acc) p.ext_ptr[kv.first.first + 1]++;
+    for (int k = 0; k < N; k++) p.ext_ptr[k + 1] += p.ext_ptr[k];
+    p.ext_nbc.assign(acc.size(), 0);
+    p.ext_f.assign(acc.size() * 3, 0.0);
+    std::vector<int> fill(p.ext_ptr.begin(), p.ext_ptr.end() - 1);
+    for (const auto& kv : acc) {
+      const int slot = fill[kv.first.first]++;
+      p.ext_nbc[slot] = kv.first.second;
+      for (int a = 0; a < 3; a++) p.ext_f[(size_t)slot * 3 + a] = kv.second[a];
+    }
+  }
+  // scatter map: offset of every neighbour's first column inside a node's rows
+  {
+    std::vector<std::vector<int>> inter(N);
+    for (int f = 0; f < nf; f++)
+      inter[s.fam_node[f]].assign(s.fam_members.begin() + s.fam_off[f], s.fam_members.begin() + s.fam_off[f + 1]);
+    for (int i = 0; i < nfe; i++)
+      for (int a = 0; a < nen; a++)
+        for (int b = 0; b < nen; b++) inter[p.fe_conn[(size_t)i * 8 + a]].push_back(p.fe_conn[(size_t)i * 8 + b]);
+    std::vector<std::vector<int>> off(N);
+    for (int k = 0; k < N; k++) {
+      auto& v = inter[k];
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      off[k].resize(v.size());
+      int o = 0;
+      for (size_t j = 0; j < v.size(); j++) {
+        off[k][j] = o;
+        for (int d = 0; d < D; d++) o += s.eq[(size_t)v[j] * D + d] >= 0 ? 1 : 0;
+      }
+    }
+    auto lookup = [&](int k, int n) {
+      auto it = std::lower_bound(inter[k].begin(), inter[k].end(), n);
+      return off[k][it - inter[k].begin()];
+    };
+    p.rel_bond.assign(nb, 0);
+    p.rel_self.assign(nf, 0);
+    for (int f = 0; f < nf; f++) {
+      const int k = s.fam_node[f];
+      p.rel_self[f] = lookup(k, k);
+      for (int b = p.fam_ptr[f]; b < p.fam_ptr[f + 1]; b++) p.rel_bond[b] = lookup(k, p.nbr[b]);
+    }
+    p.rel_fe.assign((size_t)p.fe_adj.size() * 8, 0);
+    for (int k = 0; k < N; k++)
+      for (int j = p.fe_adj_ptr[k]; j < p.fe_adj_ptr[k + 1]; j++) {
+        const int i = p.fe_adj[j] >> 3;
+        for (int a = 0; a < nen; a++) p.rel_fe[(size_t)j * 8 + a] = lookup(k, p.fe_conn[(size_t)i * 8 + a]);
+      }
+  }
+  return true;
+}
+
+}  // namespace pdx

@@ -1,0 +1,236 @@
+"""ctypes binding of the C ABI in include/pdx.h (lib/libpdx.so, built in-tree).
+
+This is the reference-facing seam as a Python caller binds it: plain
+pointers and sizes, numpy arrays on the host, status codes turned into
+exceptions.  Loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpdx.so")
+
+STATUS = {0: "OK", 1: "IO", 2: "PARSE", 3: "UNSUPPORTED", 4: "INVALID", 5: "CUDA", 6: "SINGULAR",
+          7: "NOCONV", 8: "NODEVICE", 9: "NUMERIC"}
+
+
+class PdxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pdx status {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Options(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("lanes", C.c_int), ("verbose", C.c_int)]
+
+
+class ModelInfo(C.Structure):
+    _fields_ = [("dim", C.c_int), ("n_node", C.c_int), ("n_elem", C.c_int), ("n_eq", C.c_int),
+                ("n_fam", C.c_int), ("n_pdbe", C.c_int), ("n_fe", C.c_int), ("n_fe_classes", C.c_int),
+                ("n_bond", C.c_int64), ("nnz", C.c_int64), ("solver", C.c_int), ("newmark", C.c_int),
+                ("lumped", C.c_int), ("fail_flag", C.c_int), ("precision", C.c_int), ("nsteps", C.c_int),
+                ("save_freq", C.c_int), ("lanes", C.c_int), ("dt", C.c_double), ("min_delta", C.c_double),
+                ("max_delta", C.c_double), ("s0", C.c_double), ("s0_pert", C.c_double)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", C.c_int), ("rtol", C.c_double), ("max_iter", C.c_int), ("use_x0", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("seconds", C.c_double),
+                ("converged", C.c_int)]
+
+
+EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_model_destroy",
+            "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array", "pdx_bond_coefficients",
+            "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance", "pdx_explicit_advance_timed",
+            "pdx_explicit_step_host", "pdx_explicit_step_count", "pdx_get_state", "pdx_assemble_csr",
+            "pdx_solve_csr", "pdx_run"]
+
+_lib: Optional[C.CDLL] = None
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    L = C.CDLL(LIB_PATH)
+    L.pdx_last_error.restype = C.c_char_p
+    L.pdx_version.restype = C.c_char_p
+    L.pdx_model_create_from_cmd.argtypes = [C.c_char_p, C.POINTER(Options), C.POINTER(_P)]
+    L.pdx_model_destroy.argtypes = [_P]
+    L.pdx_model_destroy.restype = None
+    L.pdx_model_get_info.argtypes = [_P, C.POINTER(ModelInfo)]
+    L.pdx_model_array_len.argtypes = [_P, C.c_char_p, C.POINTER(C.c_int64)]
+    L.pdx_model_array.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.pdx_bond_coefficients.argtypes = [_P, _D, _D, _D, _D]
+    L.pdx_internal_force.argtypes = [_P, _D, _D]
+    L.pdx_explicit_init.argtypes = [_P]
+    L.pdx_explicit_advance.argtypes = [_P, C.c_int]
+    L.pdx_explicit_advance_timed.argtypes = [_P, C.c_int, _D]
+    L.pdx_explicit_step_host.argtypes = [_P, _D, _D, _D]
+    L.pdx_explicit_step_count.argtypes = [_P]
+    L.pdx_explicit_step_count.restype = C.c_int64
+    L.pdx_get_state.argtypes = [_P, _D, _D, _D, C.POINTER(C.c_uint8)]
+    L.pdx_assemble_csr.argtypes = [_P, C.c_int, _D, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _D, _D]
+    L.pdx_solve_csr.argtypes = [C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _D, _D, _D,
+                                C.POINTER(SolveOpts), C.POINTER(SolveInfo)]
+    L.pdx_run.argtypes = [_P, C.c_char_p]
+    for name in ("pdx_model_create_from_cmd", "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array",
+                 "pdx_bond_coefficients", "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance",
+                 "pdx_explicit_advance_timed", "pdx_explicit_step_host", "pdx_get_state", "pdx_assemble_csr",
+                 "pdx_solve_csr", "pdx_run"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        raise PdxError(code, lib().pdx_last_error().decode())
+
+
+def _dptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+_ARRAY_DTYPES = {"eq": np.int32, "vol_node": np.float64, "vol_elem": np.float64, "node_type": np.int32,
+                 "fam_off": np.int64, "fam_members": np.int32, "fam_horizon": np.float64, "fam_cdv": np.float64,
+                 "bond_state0": np.uint8, "pdbe": np.int32, "pde_idx": np.int32, "fe_idx": np.int32,
+                 "csr_ia": np.int64, "csr_ja": np.int64, "mass": np.float64, "u0": np.float64, "geom": np.float64,
+                 "X": np.float64, "conn": np.int32, "elem_nn": np.int32, "bcflag": np.uint8, "dtv": np.float64,
+                 "material": np.float64}
+
+
+class Model:
+    """A PDLSM-FEM model built from a reference command file."""
+
+    def __init__(self, cmd_path: str, device: int = 0, precision: int = -1, lanes: int = 0):
+        L = lib()
+        h = _P()
+        opt = Options(device, precision, lanes, 0)
+        _check(L.pdx_model_create_from_cmd(cmd_path.encode(), C.byref(opt), C.byref(h)))
+        self._h = h
+        inf = ModelInfo()
+        _check(L.pdx_model_get_info(h, C.byref(inf)))
+        self.info = inf
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pdx_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def dim(self) -> int:
+        return self.info.dim
+
+    def array(self, name: str) -> np.ndarray:
+        n = C.c_int64()
+        _check(lib().pdx_model_array_len(self._h, name.encode(), C.byref(n)))
+        out = np.zeros(n.value, dtype=_ARRAY_DTYPES[name])
+        _check(lib().pdx_model_array(self._h, name.encode(), out.ctypes.data_as(_P), n.value))
+        return out
+
+    def bond_coefficients(self):
+        d = self.dim
+        na = 5 if d == 2 else 9
+        nd = 3 if d == 2 else 6
+        A = np.zeros((self.info.n_fam, na, na))
+        g = np.zeros((self.info.n_bond, d))
+        dv = np.zeros((self.info.n_bond, nd))
+        G = np.zeros((self.info.n_bond, d, d))
+        _check(lib().pdx_bond_coefficients(self._h, _dptr(A), _dptr(g), _dptr(dv), _dptr(G)))
+        return A, g, dv, G
+
+    def internal_force(self, u_all: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u_all, dtype=np.float64).reshape(-1)
+        f = np.zeros(self.info.n_eq)
+        _check(lib().pdx_internal_force(self._h, _dptr(u), _dptr(f)))
+        return f
+
+    def explicit_init(self) -> None:
+        _check(lib().pdx_explicit_init(self._h))
+
+    def explicit_advance(self, n: int) -> None:
+        _check(lib().pdx_explicit_advance(self._h, int(n)))
+
+    def explicit_advance_timed(self, n: int) -> float:
+        ms = C.c_double()
+        _check(lib().pdx_explicit_advance_timed(self._h, int(n), C.byref(ms)))
+        return ms.value
+
+    def explicit_step_host(self, u_n: np.ndarray, u_nm1: np.ndarray, out: np.ndarray) -> None:
+        _check(lib().pdx_explicit_step_host(self._h, _dptr(u_n), _dptr(u_nm1), _dptr(out)))
+
+    @property
+    def steps_done(self) -> int:
+        return int(lib().pdx_explicit_step_count(self._h))
+
+    def state(self):
+        N, d = self.info.n_node, self.dim
+        u = np.zeros((N, d))
+        sig = np.zeros((N, 6))
+        phi = np.zeros(N)
+        nm = int(self.array_len("fam_members"))
+        bs = np.zeros(nm, dtype=np.uint8)
+        _check(lib().pdx_get_state(self._h, _dptr(u), _dptr(sig), _dptr(phi), bs.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return u, sig, phi, bs
+
+    def array_len(self, name: str) -> int:
+        n = C.c_int64()
+        _check(lib().pdx_model_array_len(self._h, name.encode(), C.byref(n)))
+        return n.value
+
+    def assemble(self, mode: int, v_all: Optional[np.ndarray] = None):
+        ne, nnz = self.info.n_eq, self.info.nnz
+        ia = np.zeros(ne + 1, dtype=np.int64)
+        ja = np.zeros(nnz, dtype=np.int64)
+        a = np.zeros(nnz)
+        f = np.zeros(ne)
+        v = None if v_all is None else np.ascontiguousarray(v_all, dtype=np.float64).reshape(-1)
+        _check(lib().pdx_assemble_csr(self._h, int(mode), _dptr(v), ia.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      ja.ctypes.data_as(C.POINTER(C.c_int64)), _dptr(a), _dptr(f)))
+        return ia, ja, a, f
+
+    def run(self, results_dir: str) -> None:
+        _check(lib().pdx_run(self._h, results_dir.encode()))
+
+
+def solve_csr(ia: np.ndarray, ja: np.ndarray, a: np.ndarray, b: np.ndarray, method: int = 2,
+              rtol: float = 1e-8, max_iter: int = 20000, x0: Optional[np.ndarray] = None):
+    n = len(ia) - 1
+    ia = np.ascontiguousarray(ia, dtype=np.int64)
+    ja = np.ascontiguousarray(ja, dtype=np.int64)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    opts = SolveOpts(method, rtol, max_iter, 0 if x0 is None else 1)
+    info = SolveInfo()
+    code = lib().pdx_solve_csr(n, ia.ctypes.data_as(C.POINTER(C.c_int64)), ja.ctypes.data_as(C.POINTER(C.c_int64)),
+                               _dptr(a), _dptr(b), _dptr(x), C.byref(opts), C.byref(info))
+    if code not in (0, 7):
+        _check(code)
+    return x, info
