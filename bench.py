@@ -1,0 +1,252 @@
+"""Benchmark: explicit PD bond-updates/s on the 3D box-with-hole workload (C2).
+
+Workload: 121x61x21-node (120x60x20 mm) Hex8 box, 8 mm central hole, 40x40
+element PD zone through the thickness (31,584 families, 3.53 M directed bonds),
+FP32 forces / FP64 integration, critical stretch 2e-3 +-5 % per bond, seeded
+synthetic mesh.  One step = one explicit central-difference step of the whole
+model (failure pass, PD + PD-boundary + FE force, update): one kernel launch.
+
+  value   B * K / t over K device-resident steps (CUDA events on the model stream)
+  e2e     same metric through pdx_explicit_step_host with pinned host buffers
+          (u_n, u_n-1 in, u_n+1 out, copies inside the timed region)
+  roofline  algorithmic bytes per step / mean step-kernel time vs measured HBM copy peak
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle, all host threads) on the same model.  Under torchrun every rank runs an
+independent replica on its own GPU (the path does not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "pdlsm-fem_mpi_gb300"))
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(tmp: str, nsteps: int, precision: str):
+    import meshgen
+    mesh, kw = meshgen.config_c2(nsteps=nsteps, precision=precision)
+    return meshgen.write_case(mesh, tmp, "c2", **kw)
+
+
+def algorithmic_bytes(model) -> dict:
+    """Unique bytes one step must move (the design doc gives the per-unit figures)."""
+    info = model.info
+    mixed = info.precision == 1
+    cs = 4 if mixed else 8
+    d = info.dim
+    nsym = 3 if d == 2 else 6
+    n_bond = info.n_bond
+    fam_off = model.array("fam_off")
+    pdbe_nodes = set(model.array("pdbe").reshape(-1, 4)[:, : (2 if d == 2 else 4)].ravel().tolist())
+    fam_nodes = model.array("fam_members")[fam_off[:-1]]
+    sizes = np.diff(fam_off) - 1
+    corr_bonds = int(sum(int(s) for n, s in zip(fam_nodes, sizes) if n in pdbe_nodes))
+    b_bond = 4 + nsym * cs + 1.0 / 8
+    b_corr = d * d * cs
+    b_node = 2 * d * 8 + 8 + d * 8 + (d * 4 if mixed else 0)
+    b_elem = 4 * (4 if d == 2 else 8)
+    total = n_bond * b_bond + corr_bonds * b_corr + info.n_node * b_node + info.n_fe * b_elem
+    return {"bytes": total, "b_bond": b_bond, "b_corr": b_corr, "corr_bonds": corr_bonds, "b_node": b_node,
+            "b_elem": b_elem}
+
+
+def cpu_sample(cmd: str, target_s: float = 15.0, threads: int = 0):
+    """Oracle (CPU restatement of the reference path) on a bounded number of steps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import orc
+    import pdx
+    host = pdx.Model(cmd, device=-1)
+    o = orc.Oracle(host, nthreads=threads)
+    t = time.perf_counter()
+    o.explicit(nsteps=1)
+    one = (time.perf_counter() - t) / 2.0
+    n = max(2, int(target_s / max(one, 1e-6)))
+    t = time.perf_counter()
+    o.explicit(nsteps=n - 1)
+    el = time.perf_counter() - t
+    cores = o_threads()
+    return host.info.n_bond * n / el, n, el, cores
+
+
+def o_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="MIXED", choices=["MIXED", "FP64"])
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    tmp = tempfile.mkdtemp(prefix="pdx_bench_")
+    cmd = make_workload(tmp, args.steps + args.warmup + 1, args.precision)
+    config = {"workload": "c2: 3D explicit box with hole, 121x61x21 nodes, Hex8 + PDLSM zone 40x40, s0=2e-3+-5%",
+              "precision": args.precision, "inputs_vs_l2": "bond data streamed per step exceeds the 129 MB L2",
+              "step": "one central-difference step (failure + force + update)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        rate, n, el, cores = cpu_sample(cmd, target_s=20.0)
+        line = {"metric": "explicit PD bond-updates/s", "value": rate, "unit": "bond-updates/s", "n_gpus": args.gpus,
+                "steps": n, "warmup": 0, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",
+                                 "sample": f"{n} explicit steps of the full C2 model on {cores} host threads"},
+                "e2e": {"value": rate, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import pdx
+    model = pdx.Model(cmd, device=local, precision=1 if args.precision == "MIXED" else 0, lanes=args.lanes)
+    info = model.info
+    alg = algorithmic_bytes(model)
+    # warm-up steps (step 0 included), then the timed region
+    model.explicit_init()
+    model.explicit_advance(args.warmup)
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = model.explicit_advance_timed(args.steps)
+    clk = clocks.stop()
+    t_s = ms * 1e-3
+    if dist:
+        import torch
+        t = torch.tensor([t_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_s = float(t.item())
+    value = info.n_bond * args.steps * ws / t_s
+    # end to end through the host-buffer entry point
+    eq = model.array("eq")
+    act = eq >= 0
+    u0 = model.array("u0")
+    import ctypes
+    def pinned(n):
+        try:
+            import torch
+            return torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:
+            return np.zeros(n)
+    un, unm1, out = pinned(info.n_eq), pinned(info.n_eq), pinned(info.n_eq)
+    un[eq[act]] = u0[act]
+    unm1[:] = un
+    model.explicit_init()
+    for _ in range(3):
+        model.explicit_step_host(un, unm1, out)
+        unm1[:] = un; un[:] = out
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        model.explicit_step_host(un, unm1, out)
+        unm1[:] = un; un[:] = out
+    t_e2e = time.perf_counter() - t0
+    e2e = info.n_bond * args.e2e_steps / t_e2e
+    peak, kind = measured_peaks()
+    achieved = alg["bytes"] / (t_s / args.steps) / 1e9
+    line = {"metric": "explicit PD bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 forces / f64 state" if args.precision == "MIXED"
+            else "f64", "data": "synthetic (seeded meshgen config_c2)", "config": config,
+            "e2e": {"value": e2e, "unit": "bond-updates/s", "h2d_bytes_per_step": 2 * info.n_eq * 8,
+                    "d2h_bytes_per_step": info.n_eq * 8, "steps": args.e2e_steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": kind,
+                         "algorithmic_bytes_per_step": alg["bytes"], "kernel": "k_step"},
+            "gpu_launches": args.steps, "clocks": clk,
+            "model": {"n_node": info.n_node, "n_fam": info.n_fam, "n_bond": info.n_bond, "n_eq": info.n_eq,
+                      "n_fe": info.n_fe, "lanes": info.lanes}}
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, n, el, cores = cpu_sample(cmd, target_s=15.0)
+        line["cpu_baseline"] = {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",
+                                "sample": f"{n} explicit steps of the full model (FP64 oracle) on {cores} threads"}
+    if rank == 0:
+        print(json.dumps(line))
+    model.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+"""Host setup (parsers + pdsolve::setDatModel restatement) against the
+reference's own setup dumps, and input-format round trips.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import case_cmd, golden
+
+import meshgen
+import pdx
+
+CASES = [("p21", "p21_explicit"), ("b13", "b13_explicit")]
+
+
+@pytest.mark.parametrize("case,cmd", CASES)
+def test_setup_matches_reference(built, case, cmd):
+    g = golden(case + "_setup")
+    m = pdx.Model(case_cmd(case, cmd), device=-1)
+    np.testing.assert_array_equal(m.array("eq"), g["eq"].reshape(-1))
+    np.testing.assert_array_equal(m.array("node_type"), g["node_type"])
+    np.testing.assert_array_equal(m.array("fam_off"), g["fam_off"])
+    np.testing.assert_array_equal(m.array("fam_members") + 1, g["fam_members"])
+    np.testing.assert_array_equal(m.array("bond_state0"), g["bond_state0"])
+    np.testing.assert_array_equal(m.array("pde_idx"), g["pde_idx"])
+    np.testing.assert_array_equal(m.array("fe_idx"), g["fe_idx"])
+    np.testing.assert_array_equal(m.array("csr_ia"), g["csr_ia"])
+    np.testing.assert_array_equal(m.array("csr_ja"), g["csr_ja"])
+    # volumes, horizons and PD volumes are computed in the reference's operation order
+    np.testing.assert_array_equal(m.array("vol_node"), g["vol_node"])
+    np.testing.assert_array_equal(m.array("vol_elem"), g["vol_elem"])
+    np.testing.assert_array_equal(m.array("fam_horizon"), g["fam_horizon"])
+    np.testing.assert_array_equal(m.array("fam_cdv"), g["fam_cdv"])
+    np.testing.assert_array_equal(m.array("geom"), g["geom"])
+    nn = 2 if m.dim == 2 else 4
+    mine = sorted(tuple(r[:nn]) for r in m.array("pdbe").reshape(-1, 4) + 1)
+    ref = sorted(tuple(r[:nn]) for r in g["pdbe"])
+    assert mine == ref
+
+
+def test_lumped_mass_matches_reference(built):
+    for case, cmd in CASES:
+        m = pdx.Model(case_cmd(case, cmd), device=-1)
+        np.testing.assert_array_equal(m.array("mass"), golden(case + "_explicit")["mass"])
+
+
+def test_meshgen_roundtrip(tmp_path, built):
+    mesh = meshgen.plate_strip_crack(n=15, L=0.02)
+    cmd = meshgen.write_case(mesh, str(tmp_path), "rt", solver="DYNAMIC", dt=1e-8, nsteps=3, save=1,
+                             factor=3.015, nlf=1.0, fc="3 1e-3 7 0.05")
+    m = pdx.Model(cmd, device=-1)
+    assert m.info.n_node == mesh.n_node and m.info.n_elem == mesh.n_elem
+    np.testing.assert_array_equal(m.array("X").reshape(-1, 3), mesh.X)
+    conn = m.array("conn").reshape(-1, 8)[:, :4] + 1
+    np.testing.assert_array_equal(conn, mesh.elems)
+    assert m.info.fail_flag == 3 and m.info.s0 == 1e-3 and abs(m.info.s0_pert - 0.05) < 1e-15
+    mat = m.array("material")
+    assert int(mat[11]) == 7
+
+
+def test_hole_mesh_has_no_orphans(built, tmp_path):
+    mesh = meshgen.box_hole(nx=13, ny=9, nz=3, h=1e-3, radius=2e-3, pd_x=8, pd_y=6)
+    used = np.zeros(mesh.n_node, bool)
+    used[mesh.elems.ravel() - 1] = True
+    assert used.all()
+    cmd = meshgen.write_case(mesh, str(tmp_path), "bh", solver="DYNAMIC", dt=1e-8, nsteps=1, save=1,
+                             factor=3.015, nlf=1.0)
+    m = pdx.Model(cmd, device=-1)
+    assert (m.array("vol_node") > 0).all()
+
+
+def _write(path, text):
+    with open(path, "w") as f:
+        f.write(text)
+
+
+def test_errors_are_returned_not_exit(built, tmp_path):
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "missing.in"), device=-1)
+    assert e.value.code == 1
+    _write(tmp_path / "bad.in", "MSHFILE nothere.lis\nSOLVER DYNAMIC\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "bad.in"), device=-1)
+    assert e.value.code == 1
+    mesh = meshgen.plate_strip_crack(n=11, L=0.01)
+    meshgen.write_lis(mesh, str(tmp_path / "m.lis"))
+    _write(tmp_path / "s.in", "MSHFILE m.lis\nSOLVER SIDEWAYS\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "s.in"), device=-1)
+    assert e.value.code == 2
+    _write(tmp_path / "p.in", "MSHFILE m.lis\nSOLVER DYNAMIC\nPRECISION HALF\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "p.in"), device=-1)
+    assert e.value.code == 2
+    _write(tmp_path / "f.in", "MSHFILE m.lis\nSOLVER DYNAMIC\nFC 3\n")
+    with pytest.raises(pdx.PdxError):
+        pdx.Model(str(tmp_path / "f.in"), device=-1)
+
+
+def test_duplicate_dof_and_unsupported_elements(built, tmp_path):
+    mesh = meshgen.plate_strip_crack(n=11, L=0.01)
+    mesh.ebcs.append(meshgen.EBC(0, 0.0, mesh.ebcs[0].nodes[:2]))
+    meshgen.write_lis(mesh, str(tmp_path / "d.lis"))
+    _write(tmp_path / "d.in", "MSHFILE d.lis\nSOLVER DYNAMIC\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "d.in"), device=-1)
+    assert "repeatly" in str(e.value)
+    tri = meshgen.plate_strip_crack(n=11, L=0.01)
+    tri.elems[0, 3] = tri.elems[0, 2]
+    meshgen.write_lis(tri, str(tmp_path / "t.lis"))
+    _write(tmp_path / "t.in", "MSHFILE t.lis\nSOLVER DYNAMIC\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "t.in"), device=-1)
+    assert e.value.code == 3
+
+
+def test_compute_without_device_fails_loudly(built):
+    m = pdx.Model(case_cmd("p21", "p21_explicit"), device=-1)
+    with pytest.raises(pdx.PdxError) as e:
+        m.internal_force(np.zeros((m.info.n_node, 2)))
+    assert e.value.code == 8
+    with pytest.raises(pdx.PdxError):
+        m.explicit_advance(1)
+
+
+def test_command_keywords(built, tmp_path):
+    mesh = meshgen.plate_strip_crack(n=11, L=0.01)
+    meshgen.write_lis(mesh, str(tmp_path / "k.lis"))
+    _write(tmp_path / "k.in", "# comment\nMSHFILE k.lis\nSOLVER QUASI-STATIC\nSETSOLVING 5e-7 12 3 3.5 0.5 2\n"
+           "NEWMARK ON 0.6 0.3\nLUMPMASS ON\nEBC 2 1e-6\nVEBC 2 2e-6\nFC 3 2e-3 9 0.1\nPRECISION MIXED\n"
+           "SOLVE BJPCG 1e-9 500\nFOO bar\nVTKFORMAT ASCII\n")
+    m = pdx.Model(str(tmp_path / "k.in"), device=-1)
+    i = m.info
+    assert i.solver == 2 and i.dt == 1.0 and i.nsteps == 12 and i.save_freq == 3
+    assert i.newmark == 1 and i.lumped == 1 and i.fail_flag == 3 and i.precision == 1
+    u0 = m.array("u0").reshape(-1, 2)
+    top = mesh.ebcs[2].nodes - 1
+    assert np.all(u0[top, 1] == 1e-6)
+    dtv = m.array("dtv").reshape(-1, 3)
+    assert np.all(dtv[top, 1] == 1.0 * 2e-6)

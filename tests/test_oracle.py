@@ -1,0 +1,118 @@
+"""The CPU oracle pinned against FP64 dumps of the reference itself
+(tests/golden, made by tests/golden/make_golden.py from oracle/ref).  CPU only."""
+import numpy as np
+import pytest
+
+from conftest import case_cmd, golden, rel
+
+import orc
+import pdx
+
+CASES = [("p21", "p21_explicit"), ("b13", "b13_explicit")]
+
+
+@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+def oracle_case(request, built):
+    case, cmd = request.param
+    m = pdx.Model(case_cmd(case, cmd), device=-1)
+    return case, m, orc.Oracle(m)
+
+
+def test_moment_matrix_and_coefficients(oracle_case):
+    case, m, o = oracle_case
+    gc = golden(case + "_coeffs")
+    A, g, d, G = o.coeffs()
+    assert rel(A, gc["A"]) < 1e-13
+    assert rel(g, gc["g"]) < 1e-12
+    assert rel(d, gc["d"]) < 1e-12
+    # the reference's G carries the bond state; compare intact bonds
+    st = m.array("bond_state0")
+    off = m.array("fam_off")
+    member_is_bond = np.ones(len(st), bool)
+    member_is_bond[off[:-1]] = False
+    intact = st[member_is_bond] == 1
+    Gr = gc["G"].reshape(G.shape)
+    assert rel(G[intact], Gr[intact]) < 1e-12
+    assert np.all(Gr[~intact] == 0)
+
+
+def test_internal_force(oracle_case):
+    case, m, o = oracle_case
+    gf = golden(case + "_force")
+    f = o.internal_force(gf["u_all"])
+    assert rel(f, gf["F"]) < 1e-13
+
+
+def test_explicit_trajectory_and_broken_bonds(oracle_case):
+    case, m, o = oracle_case
+    ge = golden(case + "_explicit")
+    u, bs, traj, nb = o.explicit(keep_traj=True)
+    for i, s in enumerate(ge["u_traj_steps"]):
+        assert rel(traj[s], ge["u_traj"][i]) < 1e-12, s
+    np.testing.assert_array_equal(bs, ge["bond_state_final"])
+    assert nb > 0
+    sig, phi = o.stress(u, bs)
+    np.testing.assert_allclose(phi, ge["phi_final"], rtol=0, atol=1e-15)
+
+
+def test_lumped_mass(oracle_case):
+    case, m, o = oracle_case
+    np.testing.assert_array_equal(o.lumped_mass(), golden(case + "_explicit")["mass"])
+
+
+@pytest.mark.parametrize("case,cmd", [("p21", "p21s"), ("b13", "b13s")])
+def test_static_assembly(built, case, cmd):
+    gs = golden(case + "_static")
+    m = pdx.Model(case_cmd(case, cmd), device=-1)
+    o = orc.Oracle(m)
+    v = m.array("u0").copy()
+    v[m.array("eq") >= 0] = 0.0
+    ia, ja, a, f = o.assemble(v)
+    np.testing.assert_array_equal(ia, gs["K_ia"])
+    np.testing.assert_array_equal(ja, gs["K_ja"])
+    assert rel(a, gs["K_a"]) < 1e-13
+    assert rel(f, gs["F"]) < 1e-13
+    # stress recovery of the reference's own solution
+    sig, phi = o.stress(gs["u"])
+    assert rel(sig, gs["sigma"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["p21", "b13"])
+def test_newmark_matrix(built, case):
+    gn = golden(case + "_newmark")
+    m = pdx.Model(case_cmd(case, case + "_newmark"), device=-1)
+    o = orc.Oracle(m)
+    info = m.info
+    mat = m.array("material")
+    beta = 0.25
+    up = m.array("u0").reshape(-1).copy()
+    # first step: u = u0, v = a = 0, prescribed advanced by dt*v
+    up += m.array("dtv").reshape(-1, 3)[:, :m.dim].reshape(-1) * (m.array("eq") < 0)
+    ia, ja, K, f = o.assemble(up)
+    M = o.consistent_mass()
+    KN = K * beta * info.dt * info.dt + M
+    assert rel(M, gn["M_a"]) < 1e-13
+    assert rel(KN, gn["KN_a"]) < 1e-12
+    assert rel(f, gn["FN"]) < 1e-12
+    assert mat[0] > 0
+
+
+def test_oracle_force_properties(oracle_case):
+    """Rigid translation gives no force; the force is linear in u."""
+    case, m, o = oracle_case
+    n, d = m.info.n_node, m.dim
+    t = np.tile(np.array([1.3e-5, -0.7e-5, 0.4e-5][:d]), (n, 1))
+    f = o.internal_force(t)
+    f_ref = o.internal_force(np.random.default_rng(1).standard_normal((n, d)) * 1e-5)
+    assert np.linalg.norm(f) < 1e-9 * np.linalg.norm(f_ref)
+    rng = np.random.default_rng(2)
+    a, b = rng.standard_normal((2, n, d)) * 1e-6
+    lhs = o.internal_force(2.0 * a - 3.0 * b)
+    rhs = 2.0 * o.internal_force(a) - 3.0 * o.internal_force(b)
+    assert rel(lhs, rhs) < 1e-12
+
+
+def test_bond_uniform_is_uniform(built):
+    u = np.array([orc.lib().orc_bond_uniform(5, k, m) for k in range(60) for m in range(60)])
+    assert 0 <= u.min() and u.max() < 1
+    assert abs(u.mean() - 0.5) < 0.02
