@@ -481,16 +481,16 @@ void orc_lumped_mass(const orc_ctx* c, double* m_eq) {
       if (m->eq[k * m->dim + i] >= 0) m_eq[m->eq[k * m->dim + i]] = c->mass[k];
 }
 
-static uint64_t splitmix64(uint64_t z) {
-  z += 0x9e3779b97f4a7c15ull;
-  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-  return z ^ (z >> 31);
-}
-
+/* Per-bond uniform draw for FC 3 with a perturbed s0: murmur3's 32-bit
+ * finaliser of (k, m, seed folded to 32 bits), top 24 bits / 2^24. */
 double orc_bond_uniform(uint64_t seed, int k, int m) {
-  uint64_t key = seed * 0x9e3779b97f4a7c15ull + (uint64_t)(uint32_t)k * 0xd1b54a32d192ed03ull + (uint32_t)m;
-  return (double)(splitmix64(key) >> 11) * 0x1.0p-53;
+  uint32_t x = ((uint32_t)k * 0x9e3779b1u) ^ ((uint32_t)m + 0x7f4a7c15u) ^ (uint32_t)(seed ^ (seed >> 32));
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return (double)(x >> 8) * 0x1.0p-24;
 }
 
 static int64_t stretch_pass(const orc_ctx* c, const double* u, double s0, uint64_t seed, double pert, uint8_t* bs) {

@@ -83,6 +83,7 @@ static pdx_status upload_model(pdx_model* m) {
   v.dtv = upload(m, p.dtv);
   v.fam_node = upload(m, s.fam_node);
   v.fam_ptr = upload(m, p.fam_ptr);
+  v.fam_order = upload(m, p.fam_order);
   v.fam_corr = upload(m, p.fam_corr);
   m->d_intact = upload(m, p.fam_intact);
   v.fam_intact = m->d_intact;
@@ -114,6 +115,9 @@ static pdx_status upload_model(pdx_model* m) {
   v.s0 = m->cmd.s0;
   v.s0_pert = m->cmd.s0_pert;
   v.s0_seed = m->cmd.s0_seed;
+  v.s0_seed32 = (uint32_t)(m->cmd.s0_seed ^ (m->cmd.s0_seed >> 32));
+  v.fam_brk = upload(m, p.fam_brk);
+  v.dt2m = upload(m, p.dt2m);
   v.fail3 = m->cmd.fail_flag == 3 ? 1 : 0;
   m->d_D = upload(m, p.D);
   m->d_bgp = upload(m, p.bgp);
@@ -127,7 +131,13 @@ static pdx_status upload_model(pdx_model* m) {
   m->d_rel_fe = upload(m, p.rel_fe);
   for (int i = 0; i < 2; i++) {
     m->d_u[i] = m->buf.alloc<double>((size_t)N * D);
-    m->d_uf[i] = m->buf.alloc<float4>((size_t)N);
+    m->d_uf[i] = m->buf.alloc<float4>((size_t)2 * N);
+  }
+  m->d_brec = m->buf.alloc<float4>((size_t)(D == 3 ? 2 : 1) * std::max<int64_t>(v.n_bond, 1));
+  {
+    const int nd = (D == 2 ? 4 : 8) * D;
+    const size_t floats = (size_t)p.n_cls * nd * nd;
+    m->ke_smem = floats * sizeof(float) <= 48 * 1024 ? (int)floats : 0;
   }
   m->d_sigma = m->buf.alloc<double>((size_t)N * 6);
   m->d_phi = m->buf.alloc<double>((size_t)N);
@@ -197,6 +207,10 @@ static StepArgs step_args(pdx_model* m, int mode, int64_t step_index) {
   a.uf_next = m->d_uf[1 - m->cur];
   a.dt = m->cmd.dt;
   a.mode = mode;
+  a.brec = m->d_brec;
+  a.ke_smem = m->ke_smem;
+  a.s0f = (float)m->cmd.s0;
+  a.pertf = (float)m->cmd.s0_pert;
   if (m->view.n_nbc) {
     int64_t row = std::min<int64_t>(step_index + 1, m->cmd.nsteps + 1);
     a.nbc_val = m->d_nbcval + row * m->view.n_nbc;
@@ -490,6 +504,11 @@ pdx_status pdx_explicit_init(pdx_model* m) {
                   m->stream);
   cudaMemcpyAsync(m->d_intact, m->prep.fam_intact.data(), m->prep.fam_intact.size() * 4, cudaMemcpyHostToDevice,
                   m->stream);
+  if (m->mixed) {
+    pdx_status st = cuda_check(
+        launch_pack_bonds(m->view, (float)m->cmd.s0, (float)m->cmd.s0_pert, m->d_brec, m->stream), "pack bonds");
+    if (st) return st;
+  }
   m->cur = 0;
   m->steps_done = 0;
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit init");

@@ -27,6 +27,7 @@ struct DevView {
   // families
   const int* fam_node;
   const int* fam_ptr;       // n_fam+1 bond offsets
+  const int* fam_order;     // family of each step-kernel work item (spatially tiled order)
   const int* fam_corr;      // offset of the family's bonds in the PDBE-correction arrays, -1 if none
   int* fam_intact;          // intact bond count
   const int* feonly_node;   // nodes without family
@@ -53,18 +54,24 @@ struct DevView {
   // material / failure
   double s0, s0_pert;
   uint64_t s0_seed;
+  uint32_t s0_seed32;       // folded seed of the per-bond draw
   int fail3;
+  const int* fam_brk;       // least intact-bond count at which a family may still break (damage <= 0.42)
+  const double* dt2m;       // dt^2 / lumped mass per node (0 without active DOFs)
 };
 
 struct StepArgs {
   DevView v;
   const double* u_n;        // n_node*dim, stored DOF values after the previous step
   double* u_next;           // u_{n-1} in, u_{n+1} out (same buffer)
-  const float4* uf_n;       // FP32 shadow of u_n (mixed)
+  const float4* uf_n;       // mixed: node records of u_n, [2n] position, [2n+1] displacement + flags
   float4* uf_next;
   const double* nbc_val;    // n_nbc values for this step (null without NBCs)
   double dt;
   int mode;                 // 0 first step, 1 regular step, 2 failure pass only
+  float4* brec;             // mixed: per-bond records (3D: 2 float4, 2D: 1)
+  int ke_smem;              // mixed: floats of FE stiffness classes staged in shared memory (0: global)
+  float s0f, pertf;         // FP32 copies of s0 and its relative perturbation
 };
 
 struct ForceArgs {
@@ -131,6 +138,7 @@ struct AsmArgs {
 cudaError_t launch_coeff(const CoeffArgs& a, cudaStream_t s);
 cudaError_t launch_step(const StepArgs& a, int mixed, int lanes, cudaStream_t s);
 cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
+cudaError_t launch_pack_bonds(const DevView& v, float s0f, float pertf, float4* rec, cudaStream_t s);
 cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
 cudaError_t launch_assemble(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_newmark_predict(const DevView& v, const double* u, const double* vel, const double* acc,

@@ -316,8 +316,9 @@ template <int D>
 __global__ void k_shadow(DevView v, const double* u, float4* uf) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.n_node) return;
-  uf[n] = make_float4((float)u[(int64_t)n * D], (float)u[(int64_t)n * D + 1], D == 3 ? (float)u[(int64_t)n * D + 2] : 0.f,
-                      __uint_as_float((unsigned)v.bcflag[n]));
+  uf[2 * n] = v.Xf[n];
+  uf[2 * n + 1] = make_float4((float)u[(int64_t)n * D], (float)u[(int64_t)n * D + 1],
+                              D == 3 ? (float)u[(int64_t)n * D + 2] : 0.f, __uint_as_float((unsigned)v.bcflag[n]));
 }
 
 __global__ void k_newmark_matrix(int64_t n, double* k, const double* m, double beta, double dt) {

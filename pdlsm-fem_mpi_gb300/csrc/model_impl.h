@@ -25,11 +25,14 @@ struct Prepared {
   std::vector<int> nbr;              // bond neighbours
   std::vector<uint32_t> state_bits;  // initial bond states
   std::vector<int> fam_intact;
+  std::vector<int> fam_brk;          // least intact count with damage <= 0.42
+  std::vector<double> dt2m;          // dt^2 / mass per node
   std::vector<int> fam_corr;         // slot offset or -1
   std::vector<int> fam_wd;           // W*D index or -1
   std::vector<double> wd;            // dim x nv per corrected family
   int64_t n_corr = 0;
-  std::vector<int> feonly;           // FE-only nodes
+  std::vector<int> feonly;           // FE-only nodes (spatially tiled order)
+  std::vector<int> fam_order;        // families in spatially tiled order
   // FE elements (order of Setup::fe)
   std::vector<int> fe_conn;          // 8 per element
   std::vector<int> fe_cls;
@@ -80,6 +83,8 @@ struct pdx_model {
   // device arrays kept by name for updates
   double* d_u[2] = {nullptr, nullptr};
   float4* d_uf[2] = {nullptr, nullptr};
+  float4* d_brec = nullptr;          // mixed-precision bond records
+  int ke_smem = 0;                   // floats of FE classes staged in shared memory
   uint32_t* d_state = nullptr;
   int* d_intact = nullptr;
   double* d_nbcval = nullptr;        // (nsteps + 2) * n_nbc

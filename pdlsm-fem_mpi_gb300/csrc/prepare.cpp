@@ -113,6 +113,19 @@ bool prepare_model(pdx_model* m, Error& err) {
   for (int f = 0; f < nf; f++)
     for (int b = p.fam_ptr[f]; b < p.fam_ptr[f + 1]; b++)
       if (st[b]) { p.state_bits[b >> 5] |= 1u << (b & 31); p.fam_intact[f]++; }
+  // the damage test of failureCriterion_stretch, phi = 1 - intact/(n-1) > 0.42,
+  // evaluated once per possible intact count so the kernel compares integers
+  p.fam_brk.assign(nf, 0);
+  for (int f = 0; f < nf; f++) {
+    const int nbf = p.fam_ptr[f + 1] - p.fam_ptr[f];
+    int t = nbf + 1;
+    for (int i = 0; i <= nbf; i++)
+      if (!(1.0 - (double)i / ((double)(nbf + 1) - 1.0) > 0.42)) { t = i; break; }
+    p.fam_brk[f] = t;
+  }
+  p.dt2m.assign(N, 0.0);
+  for (int k = 0; k < N; k++)
+    if (p.mass_node[k] > 0) p.dt2m[k] = c.dt * c.dt / p.mass_node[k];
   // PD-boundary weights W per node
   std::vector<std::vector<double>> W(N);
   auto addW = [&](int n, const double* w) {
@@ -157,10 +170,37 @@ bool prepare_model(pdx_model* m, Error& err) {
     p.fam_corr[f] = (int)p.n_corr;
     p.n_corr += p.fam_ptr[f + 1] - p.fam_ptr[f];
   }
-  // FE-only nodes
+  // FE-only nodes; families and FE-only nodes are handed to the step kernel in
+  // spatial tiles (4x4x4 in 3D, 8x8 in 2D, tile edge in units of the smallest
+  // element size) so that the neighbours one thread block gathers fit in L1
   p.feonly.clear();
   for (int k = 0; k < N; k++)
     if (s.node_type[k] == 0) p.feonly.push_back(k);
+  {
+    const double tile = (D == 3 ? 4.0 : 8.0) * s.min_delta;
+    auto key = [&](int k) {
+      int64_t t[3], r[3];
+      for (int a = 0; a < 3; a++) {
+        const double x = (me.X[(size_t)k * 3 + a] - s.lbc[a]) / tile;
+        t[a] = (int64_t)std::floor(x);
+        r[a] = (int64_t)std::floor((x - (double)t[a]) * 64.0);
+      }
+      return std::array<int64_t, 7>{t[2], t[1], t[0], r[2], r[1], r[0], (int64_t)k};
+    };
+    std::vector<std::array<int64_t, 7>> kf(nf);
+    for (int f = 0; f < nf; f++) kf[f] = key(s.fam_node[f]);
+    p.fam_order.resize(nf);
+    for (int f = 0; f < nf; f++) p.fam_order[f] = f;
+    std::sort(p.fam_order.begin(), p.fam_order.end(), [&](int a, int b) { return kf[a] < kf[b]; });
+    std::vector<std::array<int64_t, 7>> ke(p.feonly.size());
+    for (size_t i = 0; i < p.feonly.size(); i++) ke[i] = key(p.feonly[i]);
+    std::vector<int> idx(p.feonly.size());
+    for (size_t i = 0; i < idx.size(); i++) idx[i] = (int)i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return ke[a] < ke[b]; });
+    std::vector<int> tmp(p.feonly.size());
+    for (size_t i = 0; i < idx.size(); i++) tmp[i] = p.feonly[idx[i]];
+    p.feonly.swap(tmp);
+  }
   // FE elements and stiffness classes
   const int nen = D == 2 ? 4 : 8;
   const int nd = nen * D;
