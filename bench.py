@@ -154,7 +154,8 @@ def main():
     ap.add_argument("--precision", default="MIXED", choices=["MIXED", "FP64"])
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: autotuned)")
+    ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: autotuned)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = None
@@ -180,7 +181,8 @@ def main():
         print(json.dumps(line))
         return
     import pdx
-    model = pdx.Model(cmd, device=local, precision=1 if args.precision == "MIXED" else 0, lanes=args.lanes)
+    model = pdx.Model(cmd, device=local, precision=1 if args.precision == "MIXED" else 0, lanes=args.lanes,
+                      fe_lanes=args.fe_lanes)
     info = model.info
     alg = algorithmic_bytes(model)
     # warm-up steps (step 0 included), then the timed region
@@ -236,7 +238,7 @@ def main():
                          "algorithmic_bytes_per_step": alg["bytes"], "kernel": "k_step"},
             "gpu_launches": args.steps, "clocks": clk,
             "model": {"n_node": info.n_node, "n_fam": info.n_fam, "n_bond": info.n_bond, "n_eq": info.n_eq,
-                      "n_fe": info.n_fe, "lanes": info.lanes}}
+                      "n_fe": info.n_fe, "lanes": info.lanes, "fe_lanes": info.fe_lanes}}
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, el, cores = cpu_sample(cmd, target_s=15.0)
         line["cpu_baseline"] = {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",

@@ -38,15 +38,16 @@ typedef struct pdx_model pdx_model;
 typedef struct pdx_options {
   int device;      /* CUDA device ordinal; -1 builds the host setup only (no compute) */
   int precision;   /* -1: PRECISION keyword of the command file; 0 FP64; 1 mixed (FP32 forces) */
-  int lanes;       /* lanes per family in the step kernel (4, 8, 16, 32); 0 = autotuned */
+  int lanes;       /* lanes per PD family in the step kernel (4, 8, 16); 0 = autotuned */
   int verbose;
+  int fe_lanes;    /* lanes per FE-only node in the step kernel (1, 2, 4); 0 = autotuned */
 } pdx_options;
 
 typedef struct pdx_model_info {
   int dim, n_node, n_elem, n_eq, n_fam, n_pdbe, n_fe, n_fe_classes;
   int64_t n_bond, nnz;
   int solver;      /* 0 dynamic, 1 static, 2 quasi-static (SOLVER keyword) */
-  int newmark, lumped, fail_flag, precision, nsteps, save_freq, lanes;
+  int newmark, lumped, fail_flag, precision, nsteps, save_freq, lanes, fe_lanes;
   double dt, min_delta, max_delta, s0, s0_pert;
 } pdx_model_info;
 

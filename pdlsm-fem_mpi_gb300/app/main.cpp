@@ -12,7 +12,7 @@
 
 int main(int argc, char** argv) {
   const std::string cmd = argc > 1 ? argv[1] : "PDFEMcmd.in";
-  pdx_options opt{0, -1, 0, 0};
+  pdx_options opt{0, -1, 0, 0, 0};
   pdx_model* m = nullptr;
   pdx_status st = pdx_model_create_from_cmd(cmd.c_str(), &opt, &m);
   if (st != PDX_OK) {

@@ -32,7 +32,7 @@ def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(
             os.path.getmtime(src), *(os.path.getmtime(os.path.join(CSRC, h))
-                                     for h in os.listdir(CSRC) if h.endswith(".h"))):
+                                     for h in os.listdir(CSRC) if h.endswith((".h", ".cuh")))):
         return obj
     flags = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC,-ffp-contract=off", "-c"]
     if src.endswith(".cu"):

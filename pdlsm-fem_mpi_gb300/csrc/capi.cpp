@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -224,7 +225,7 @@ pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index) {
     a.u_next = m->d_u[m->cur];   // not written in mode 2
     a.uf_next = m->d_uf[m->cur];
   }
-  pdx_status st = cuda_check(launch_step(a, m->mixed, m->lanes, m->stream), "explicit step kernel");
+  pdx_status st = cuda_check(launch_step(a, m->mixed, m->lanes, m->fe_lanes, m->stream), "explicit step kernel");
   if (st) return st;
   if (mode != 2) m->cur ^= 1;
   return PDX_OK;
@@ -284,7 +285,7 @@ const char* pdx_version(void) { return "pdlsm-gb300 0.1"; }
 pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* opts, pdx_model** out) {
   if (!cmd_path || !out) return set_error(PDX_ERR_INVALID, "null argument");
   *out = nullptr;
-  pdx_options o{0, -1, 0, 0};
+  pdx_options o{0, -1, 0, 0, 0};
   if (opts) o = *opts;
   pdx_model* m = new pdx_model();
   Error err{0, ""};
@@ -298,10 +299,17 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
     return set_error(code, err.msg);
   }
   m->mixed = o.precision >= 0 ? o.precision : m->cmd.precision;
-  m->lanes = o.lanes > 0 ? o.lanes : (m->mesh.dim == 2 ? 4 : 8);
-  if (m->lanes != 4 && m->lanes != 8 && m->lanes != 16 && m->lanes != 32) {
+  m->verbose = o.verbose;
+  // Lanes per family / per FE-only node: given, or timed on this model by
+  // pdx_explicit_init (autotune_lanes) with these as the starting point.
+  m->tune = o.lanes <= 0 || o.fe_lanes <= 0;
+  m->lanes = o.lanes > 0 ? o.lanes : 4;
+  m->fe_lanes = o.fe_lanes > 0 ? o.fe_lanes : 2;
+  m->tune_lanes = o.lanes <= 0;
+  m->tune_fe_lanes = o.fe_lanes <= 0;
+  if (!step_lanes_valid(m->lanes, m->fe_lanes)) {
     delete m;
-    return set_error(PDX_ERR_INVALID, "lanes must be 4, 8, 16 or 32");
+    return set_error(PDX_ERR_INVALID, "lanes must be 4, 8 or 16 and fe_lanes 1, 2 or 4");
   }
   if (o.device >= 0) {
     m->device = o.device;
@@ -354,6 +362,7 @@ pdx_status pdx_model_get_info(const pdx_model* m, pdx_model_info* info) {
   i.nsteps = m->cmd.nsteps;
   i.save_freq = m->cmd.save_freq;
   i.lanes = m->lanes;
+  i.fe_lanes = m->fe_lanes;
   i.dt = m->cmd.dt;
   i.min_delta = m->setup.min_delta;
   i.max_delta = m->setup.max_delta;
@@ -493,8 +502,11 @@ pdx_status pdx_internal_force(pdx_model* m, const double* u_all, double* f_eq) {
   return cuda_check(cudaStreamSynchronize(m->stream), "internal force");
 }
 
-pdx_status pdx_explicit_init(pdx_model* m) {
-  NEED_DEVICE(m);
+}  // extern "C"
+
+// Initial state of an explicit run: u_0 in both buffers, FP32 node records,
+// initial bond states and, for mixed precision, the packed bond records.
+static pdx_status explicit_reset(pdx_model* m) {
   const size_t nd = (size_t)m->mesh.n_node * m->mesh.dim;
   for (int i = 0; i < 2; i++)
     cudaMemcpyAsync(m->d_u[i], m->prep.u0.data(), nd * 8, cudaMemcpyHostToDevice, m->stream);
@@ -514,6 +526,63 @@ pdx_status pdx_explicit_init(pdx_model* m) {
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit init");
 }
 
+// Times the step kernel on this model for every (lanes per family, lanes per
+// FE-only node) pair left open by the options and keeps the fastest.  The
+// trial steps run on the model's own buffers; the caller resets the state
+// afterwards, so tuning changes no result except the FP32 summation order of
+// the mixed-precision forces.
+static pdx_status autotune_lanes(pdx_model* m) {
+  static const int kLp[3] = {4, 8, 16}, kLf[3] = {1, 2, 4};
+  const int nlp = m->tune_lanes ? 3 : 1, nlf = m->tune_fe_lanes ? 3 : 1;
+  const int lp0 = m->lanes, lf0 = m->fe_lanes;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  pdx_status st = cuda_check(cudaEventCreate(&e0), "event");
+  if (!st) st = cuda_check(cudaEventCreate(&e1), "event");
+  float best = 1e30f;
+  int best_lp = lp0, best_lf = lf0;
+  for (int i = 0; i < nlp && !st; i++) {
+    for (int j = 0; j < nlf && !st; j++) {
+      m->lanes = m->tune_lanes ? kLp[i] : lp0;
+      m->fe_lanes = m->tune_fe_lanes ? kLf[j] : lf0;
+      for (int w = 0; w < 2 && !st; w++) st = explicit_step_launch(m, 1, 0);
+      if (!st) st = cuda_check(cudaEventRecord(e0, m->stream), "event record");
+      for (int w = 0; w < 5 && !st; w++) st = explicit_step_launch(m, 1, 0);
+      if (!st) st = cuda_check(cudaEventRecord(e1, m->stream), "event record");
+      if (!st) st = cuda_check(cudaEventSynchronize(e1), "event sync");
+      float ms = 0.f;
+      if (!st) st = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event time");
+      if (!st && ms < best) {
+        best = ms;
+        best_lp = m->lanes;
+        best_lf = m->fe_lanes;
+      }
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  m->lanes = best_lp;
+  m->fe_lanes = best_lf;
+  if (m->graph) {
+    cudaGraphExecDestroy(m->graph);
+    m->graph = nullptr;
+  }
+  if (m->verbose) fprintf(stderr, "pdx: step lanes %d per family, %d per FE node (%.1f us/step)\n", best_lp, best_lf,
+                          1000.f * best / 5);
+  return st;
+}
+
+extern "C" {
+
+pdx_status pdx_explicit_init(pdx_model* m) {
+  NEED_DEVICE(m);
+  pdx_status st = explicit_reset(m);
+  if (st || !m->tune) return st;
+  m->tune = false;
+  st = autotune_lanes(m);
+  if (st) return st;
+  return explicit_reset(m);
+}
+
 static pdx_status build_graph(pdx_model* m, int gsteps) {
   if (m->graph) { cudaGraphExecDestroy(m->graph); m->graph = nullptr; }
   cudaGraph_t g;
@@ -522,7 +591,7 @@ static pdx_status build_graph(pdx_model* m, int gsteps) {
   if (st) return st;
   for (int i = 0; i < gsteps; i++) {
     StepArgs a = step_args(m, 1, 0);
-    launch_step(a, m->mixed, m->lanes, m->stream);
+    launch_step(a, m->mixed, m->lanes, m->fe_lanes, m->stream);
     m->cur ^= 1;
   }
   st = cuda_check(cudaStreamEndCapture(m->stream, &g), "graph capture end");

@@ -72,6 +72,7 @@ struct StepArgs {
   float4* brec;             // mixed: per-bond records (3D: 2 float4, 2D: 1)
   int ke_smem;              // mixed: floats of FE stiffness classes staged in shared memory (0: global)
   float s0f, pertf;         // FP32 copies of s0 and its relative perturbation
+  int pd_blocks;            // set by the launcher: blocks [0, pd_blocks) take the PD families
 };
 
 struct ForceArgs {
@@ -136,7 +137,10 @@ struct AsmArgs {
 
 // kernel launchers (return cudaError_t of the launch)
 cudaError_t launch_coeff(const CoeffArgs& a, cudaStream_t s);
-cudaError_t launch_step(const StepArgs& a, int mixed, int lanes, cudaStream_t s);
+// lp: lanes per PD family (4, 8, 16); lf: lanes per FE-only node (1, 2, 4)
+bool step_lanes_valid(int lp, int lf);
+cudaError_t launch_step(const StepArgs& a, int mixed, int lp, int lf, cudaStream_t s);
+cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s);
 cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
 cudaError_t launch_pack_bonds(const DevView& v, float s0f, float pertf, float4* rec, cudaStream_t s);
 cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);

@@ -1,0 +1,255 @@
+// Mixed-precision explicit step: forces in FP32, state, mass and update in
+// FP64.  Same work split, failure order and update as the FP64 kernel
+// (k_step.cu, k_step_common.cuh); the data it streams differ:
+//
+// Bond records (one per bond; 3D: 32 B = 6 FP32 coefficients, the neighbour
+// index whose sign carries the bond state, the bond's FP32 threshold; 2D:
+// 16 B = 3 coefficients + neighbour) are the only per-bond stream.  They are
+// prefetched one iteration ahead in registers.  Breaking a bond flips the
+// record's sign and clears the bit of the FP64 state array as well.
+//
+// Node records (2 float4 per node): [2n] = position (x, y, z, 0),
+// [2n+1] = stored displacement (ux, uy, uz, varying-prescribed bits), so one
+// 32-byte sector serves both the stretch test and the force.
+//
+// The stretch test runs in FP32 on the sqrt-free form (see k_step.cu); a bond
+// within a relative band of 2e-4 around its threshold is settled after the
+// bond loop by the reference's FP64 expression.
+#include "k_step_common.cuh"
+
+namespace pdx {
+
+using namespace step;
+
+namespace {
+
+template <int D>
+__device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, const float* du, float* acc) {
+  if (D == 2) {
+    acc[0] += ra.x * du[0] + ra.y * du[1];
+    acc[1] += ra.y * du[0] + ra.z * du[1];
+  } else {
+    acc[0] += ra.x * du[0] + ra.y * du[1] + ra.z * du[2];
+    acc[1] += ra.y * du[0] + ra.w * du[1] + rb.x * du[2];
+    acc[D - 1] += ra.z * du[0] + rb.x * du[1] + rb.y * du[2];
+  }
+}
+
+template <int D, int L>
+__device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float* ke, int64_t t) {
+  constexpr int RS = D == 3 ? 2 : 1;       // float4 per bond record
+  const DevView& v = a.v;
+  const float4* nr = a.uf_n;               // node records of u_n
+  const LoadMixed<D> load_u{nr, v.dtv};
+  const int item = (int)(t / L);
+  const int lane = (int)(t % L);
+  const bool valid = item < v.n_fam;
+  const int f = valid ? v.fam_order[item] : 0;
+  const int node = valid ? v.fam_node[f] : 0;
+  float acc[D];
+#pragma unroll
+  for (int i = 0; i < D; i++) acc[i] = 0.f;
+  int nbroken = 0;
+  if (valid) {
+    const int b0 = v.fam_ptr[f], b1 = v.fam_ptr[f + 1];
+    const bool brk = a.mode >= 1 && v.fail3 && v.fam_intact[f] >= v.fam_brk[f];
+    const bool force = a.mode != 2;
+    const int corr0 = v.fam_corr[f];
+    const float4 xk = nr[2 * node];
+    const float4 qk = nr[2 * node + 1];
+    float uk[D];
+    load_u(node, uk);
+    float4* R = a.brec;
+    bool deferred = false;
+    int b = b0 + lane;
+    float4 ra = make_float4(0, 0, 0, 0), rb = ra;
+    if (b < b1) {
+      ra = __ldcs(R + (int64_t)RS * b);
+      if (D == 3) rb = __ldcs(R + (int64_t)RS * b + 1);
+    }
+    while (b < b1) {
+      const int bn = b + L;
+      float4 na = make_float4(0, 0, 0, 0), nb = na;
+      if (bn < b1) {
+        na = __ldcs(R + (int64_t)RS * bn);
+        if (D == 3) nb = __ldcs(R + (int64_t)RS * bn + 1);
+      }
+      const int m = __float_as_int(D == 3 ? rb.z : ra.w);
+      if (m >= 0) {
+        const float4 um = nr[2 * m + 1];
+        bool cut = false;
+        if (brk) {
+          const float4 xm = nr[2 * m];
+          const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
+          const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
+          const float xx = x0 * x0 + x1 * x1 + x2 * x2;
+          const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
+          const float sc = D == 3 ? rb.w : bond_s0_f32(a.s0f, a.pertf, bond_hash(v.s0_seed32, node, m));
+          const float rhs = sc * (2.f + sc) * xx;
+          if (fabsf(lhs - rhs) <= 2e-4f * rhs) {
+            // Near the threshold: decided in FP64 by the pass after the loop,
+            // which also adds the bond's force if it stays intact.
+            deferred = true;
+            cut = true;
+          } else if (lhs > rhs) {
+            cut = true;
+            int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
+            *mslot = ~m;
+            atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
+            nbroken++;
+          }
+        }
+        if (force && !cut) {
+          float du[D];
+          du[0] = um.x;
+          du[1] = um.y;
+          if (D == 3) du[D - 1] = um.z;
+          const unsigned fl = __float_as_uint(um.w);
+          if (fl) {
+#pragma unroll
+            for (int i = 0; i < D; i++)
+              if ((fl >> i) & 1u) du[i] += (float)v.dtv[3 * m + i];
+          }
+#pragma unroll
+          for (int i = 0; i < D; i++) du[i] -= uk[i];
+          bond_force<D>(ra, rb, du, acc);
+          if (corr0 >= 0) corr_block<D, float>(v.corr32, v.n_corr_bond, (int64_t)corr0 + (b - b0), du, acc);
+        }
+      }
+      b = bn;
+      ra = na;
+      rb = nb;
+    }
+    if (deferred) {
+      // Rare: repeat the FP32 test on this lane's bonds and settle the ones
+      // in the band with the reference's FP64 expression.
+      for (b = b0 + lane; b < b1; b += L) {
+        ra = R[(int64_t)RS * b];
+        if (D == 3) rb = R[(int64_t)RS * b + 1];
+        const int m = __float_as_int(D == 3 ? rb.z : ra.w);
+        if (m < 0) continue;
+        const float4 xm = nr[2 * m], um = nr[2 * m + 1];
+        const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
+        const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
+        const float xx = x0 * x0 + x1 * x1 + x2 * x2;
+        const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
+        const uint32_t h = bond_hash(v.s0_seed32, node, m);
+        const float sc = D == 3 ? rb.w : bond_s0_f32(a.s0f, a.pertf, h);
+        const float rhs = sc * (2.f + sc) * xx;
+        if (!(fabsf(lhs - rhs) <= 2e-4f * rhs)) continue;
+        if (stretch_over_fp64<D>(v, a.u_n, node, m, h)) {
+          int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
+          *mslot = ~m;
+          atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
+          nbroken++;
+        } else if (force) {
+          float du[D];
+          load_u(m, du);
+#pragma unroll
+          for (int i = 0; i < D; i++) du[i] -= uk[i];
+          bond_force<D>(ra, rb, du, acc);
+          if (corr0 >= 0) corr_block<D, float>(v.corr32, v.n_corr_bond, (int64_t)corr0 + (b - b0), du, acc);
+        }
+      }
+    }
+    if (force) {
+      const int j0 = v.fe_adj_ptr[node], j1 = v.fe_adj_ptr[node + 1];
+      for (int j = j0 + lane; j < j1; j += L) {
+        const int ent = v.fe_adj[j];
+        fe_rows<D, float>(v, ke, ent >> 3, ent & 7, load_u, acc);
+      }
+    }
+  }
+  warp_sum<D, L>(acc);
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) nbroken += __shfl_xor_sync(kFull, nbroken, o);
+  if (lane == 0 && valid && nbroken) v.fam_intact[f] -= nbroken;
+  if (a.mode == 2) return;
+  double F[D];
+#pragma unroll
+  for (int i = 0; i < D; i++) F[i] = (double)acc[i];
+  if (lane == 0 && valid) external_force<D>(a, node, F);
+  warp_update<D, L, true>(a, F, valid ? node : -1);
+}
+
+template <int D, int LP, int LF>
+__global__ void __launch_bounds__(256, 4) k_step_mixed(StepArgs a) {
+  extern __shared__ float s_ke[];
+  const float* ke = a.v.ke32;
+  if (a.ke_smem) {
+    for (int i = threadIdx.x; i < a.ke_smem; i += blockDim.x) s_ke[i] = a.v.ke32[i];
+    __syncthreads();
+    ke = s_ke;
+  }
+  if ((int)blockIdx.x < a.pd_blocks) {
+    mixed_family_item<D, LP>(a, ke, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  } else {
+    const int64_t t = (int64_t)(blockIdx.x - a.pd_blocks) * blockDim.x + threadIdx.x;
+    feonly_item<D, LF, float, true>(a, ke, t, LoadMixed<D>{a.uf_n, a.v.dtv});
+  }
+}
+
+// Mixed-precision bond records from the FP32 coefficients, the bond states and
+// the per-bond thresholds.
+template <int D>
+__global__ void k_pack_bonds(DevView v, float s0f, float pertf, float4* rec) {
+  const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (f >= v.n_fam) return;
+  const int k = v.fam_node[f];
+  const int64_t nb = v.n_bond;
+  for (int b = v.fam_ptr[f] + (threadIdx.x & 31); b < v.fam_ptr[f + 1]; b += 32) {
+    const int m = v.nbr[b];
+    const bool intact = (v.state[b >> 5] >> (b & 31)) & 1u;
+    const int mb = intact ? m : ~m;
+    if (D == 2) {
+      rec[b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], __int_as_float(mb));
+    } else {
+      const float s0b = bond_s0_f32(s0f, pertf, bond_hash(v.s0_seed32, k, m));
+      rec[2 * (int64_t)b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], v.coef32[3 * nb + b]);
+      rec[2 * (int64_t)b + 1] = make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(mb), s0b);
+    }
+  }
+}
+
+template <int D, int LP>
+cudaError_t mixed_dispatch_lf(const StepArgs& a, int lf, int blocks, size_t smem, cudaStream_t s) {
+  switch (lf) {
+    case 1: k_step_mixed<D, LP, 1><<<blocks, 256, smem, s>>>(a); break;
+    case 2: k_step_mixed<D, LP, 2><<<blocks, 256, smem, s>>>(a); break;
+    case 4: k_step_mixed<D, LP, 4><<<blocks, 256, smem, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <int D>
+cudaError_t mixed_dispatch(StepArgs a, int lp, int lf, cudaStream_t s) {
+  const int pd_blocks = (int)(((int64_t)a.v.n_fam * lp + 255) / 256);
+  const int fe_blocks = a.mode == 2 ? 0 : (int)(((int64_t)a.v.n_feonly * lf + 255) / 256);
+  a.pd_blocks = pd_blocks;
+  const int blocks = pd_blocks + fe_blocks;
+  if (blocks == 0) return cudaSuccess;
+  const size_t smem = (size_t)a.ke_smem * sizeof(float);
+  switch (lp) {
+    case 4: return mixed_dispatch_lf<D, 4>(a, lf, blocks, smem, s);
+    case 8: return mixed_dispatch_lf<D, 8>(a, lf, blocks, smem, s);
+    case 16: return mixed_dispatch_lf<D, 16>(a, lf, blocks, smem, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s) {
+  return a.v.dim == 2 ? mixed_dispatch<2>(a, lp, lf, s) : mixed_dispatch<3>(a, lp, lf, s);
+}
+
+cudaError_t launch_pack_bonds(const DevView& v, float s0f, float pertf, float4* rec, cudaStream_t s) {
+  if (v.n_fam == 0) return cudaSuccess;
+  const int blocks = (v.n_fam + 7) / 8;
+  if (v.dim == 2) k_pack_bonds<2><<<blocks, 256, 0, s>>>(v, s0f, pertf, rec);
+  else k_pack_bonds<3><<<blocks, 256, 0, s>>>(v, s0f, pertf, rec);
+  return cudaGetLastError();
+}
+
+}  // namespace pdx

@@ -75,7 +75,10 @@ struct pdx_model {
   std::string base_dir;
   int device = -1;
   int mixed = 0;
-  int lanes = 0;
+  int verbose = 0;
+  int lanes = 0;                     // lanes per PD family in the step kernel
+  int fe_lanes = 0;                  // lanes per FE-only node
+  bool tune = false, tune_lanes = false, tune_fe_lanes = false;
   bool has_device = false;
   cudaStream_t stream = nullptr;
   pdx::DevBuf buf;

@@ -26,7 +26,8 @@ class PdxError(RuntimeError):
 
 
 class Options(C.Structure):
-    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("lanes", C.c_int), ("verbose", C.c_int)]
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("lanes", C.c_int), ("verbose", C.c_int),
+                ("fe_lanes", C.c_int)]
 
 
 class ModelInfo(C.Structure):
@@ -34,7 +35,7 @@ class ModelInfo(C.Structure):
                 ("n_fam", C.c_int), ("n_pdbe", C.c_int), ("n_fe", C.c_int), ("n_fe_classes", C.c_int),
                 ("n_bond", C.c_int64), ("nnz", C.c_int64), ("solver", C.c_int), ("newmark", C.c_int),
                 ("lumped", C.c_int), ("fail_flag", C.c_int), ("precision", C.c_int), ("nsteps", C.c_int),
-                ("save_freq", C.c_int), ("lanes", C.c_int), ("dt", C.c_double), ("min_delta", C.c_double),
+                ("save_freq", C.c_int), ("lanes", C.c_int), ("fe_lanes", C.c_int), ("dt", C.c_double), ("min_delta", C.c_double),
                 ("max_delta", C.c_double), ("s0", C.c_double), ("s0_pert", C.c_double)]
 
 
@@ -116,10 +117,10 @@ _ARRAY_DTYPES = {"eq": np.int32, "vol_node": np.float64, "vol_elem": np.float64,
 class Model:
     """A PDLSM-FEM model built from a reference command file."""
 
-    def __init__(self, cmd_path: str, device: int = 0, precision: int = -1, lanes: int = 0):
+    def __init__(self, cmd_path: str, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0):
         L = lib()
         h = _P()
-        opt = Options(device, precision, lanes, 0)
+        opt = Options(device, precision, lanes, 0, fe_lanes)
         _check(L.pdx_model_create_from_cmd(cmd_path.encode(), C.byref(opt), C.byref(h)))
         self._h = h
         inf = ModelInfo()
