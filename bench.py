@@ -216,13 +216,14 @@ def main():
     un[eq[act]] = u0[act]
     unm1[:] = un
     model.explicit_init()
+    # the three pinned buffers rotate roles (u_n+1 of one step is u_n of the next)
     for _ in range(3):
         model.explicit_step_host(un, unm1, out)
-        unm1[:] = un; un[:] = out
+        un, unm1, out = out, un, unm1
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         model.explicit_step_host(un, unm1, out)
-        unm1[:] = un; un[:] = out
+        un, unm1, out = out, un, unm1
     t_e2e = time.perf_counter() - t0
     e2e = info.n_bond * args.e2e_steps / t_e2e
     peak, kind = measured_peaks()
