@@ -141,6 +141,25 @@ pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t
 pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const double* a,
                          const double* rhs, double* x, const pdx_solve_opts* opts, pdx_solve_info* info);
 
+/* Allocation-free Jacobi PCG (no counterpart in the reference).  The same
+ * solve as pdx_solve_csr with opts->method 0, on device-resident arrays of the
+ * current CUDA device (d_ja: int32 column indices), ordered on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  All work space lives in
+ * one fixed device array of the library (12.6 MB), so the call allocates no
+ * device memory: for callers that reserve the GPU's memory up front or must
+ * not let an allocator run inside their time-step loop.
+ *   - n <= 262144 equations; larger n returns PDX_ERR_INVALID;
+ *   - opts->method must be 0 (else PDX_ERR_UNSUPPORTED); use_x0 = 0 zeroes d_x;
+ *   - nothing has to be zeroed beforehand;
+ *   - calls that overlap in time on the same device share the work space and
+ *     race: serialise them;
+ *   - the first call on a device looks up the work space's address; make it
+ *     before any stream capture starts.
+ * info->seconds is not measured (0). */
+pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, const int32_t* d_ja,
+                                 const double* d_a, const double* d_rhs, double* d_x, const pdx_solve_opts* opts,
+                                 void* stream, pdx_solve_info* info);
+
 /* Runs the solver the command file selects (pdsolve::pdfemSolver,
  * pdsolve.cpp:5073-5103) and writes the reference's outputs under
  * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM). */

@@ -787,4 +787,37 @@ pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const 
   return PDX_OK;
 }
 
+// Jacobi PCG on a device-resident CSR system with the work space in a fixed
+// device array: allocates no device memory (k_krylov.cu, krylov_pcg_noalloc).
+pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, const int32_t* d_ja,
+                                 const double* d_a, const double* d_rhs, double* d_x, const pdx_solve_opts* opts,
+                                 void* stream, pdx_solve_info* info) {
+  if (n <= 0 || nnz <= 0 || !d_ia || !d_ja || !d_a || !d_rhs || !d_x) return set_error(PDX_ERR_INVALID, "bad argument");
+  if (n > noalloc_max_n())
+    return set_error(PDX_ERR_INVALID, "pdx_pcg_solve_noalloc: n = " + std::to_string(n) + " exceeds the fixed work space (" +
+                                          std::to_string(noalloc_max_n()) + " equations)");
+  pdx_solve_opts o{0, 1e-8, 20000, 0};
+  if (opts) o = *opts;
+  if (o.method != 0) return set_error(PDX_ERR_UNSUPPORTED, "pdx_pcg_solve_noalloc runs Jacobi PCG only (method 0)");
+  DevCsr A;
+  A.n = n;
+  A.nnz = nnz;
+  A.ia = d_ia;
+  A.ja = d_ja;
+  A.a = d_a;
+  KrylovResult kr;
+  cudaError_t ce =
+      krylov_pcg_noalloc(A, d_rhs, d_x, o.rtol, o.max_iter, o.use_x0, static_cast<cudaStream_t>(stream), &kr);
+  if (ce != cudaSuccess) return set_error(PDX_ERR_CUDA, std::string("Krylov solve: ") + cudaGetErrorString(ce));
+  if (info) {
+    info->iterations = kr.iterations;
+    info->rel_residual = kr.rel_residual;
+    info->seconds = 0.0;
+    info->converged = kr.converged;
+  }
+  if (!kr.converged)
+    return set_error(PDX_ERR_NOCONV, "Krylov solve stopped at relative residual " + std::to_string(kr.rel_residual));
+  return PDX_OK;
+}
+
 }  // extern "C"

@@ -171,5 +171,10 @@ struct KrylovResult {
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
                          int block_dim, cudaStream_t s, KrylovResult* res);
 cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+// Jacobi PCG with its work space in a fixed device array (no allocation);
+// n <= noalloc_max_n(), one solve at a time per device.
+cudaError_t krylov_pcg_noalloc(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int use_x0,
+                               cudaStream_t s, KrylovResult* res);
+int64_t noalloc_max_n();
 
 }  // namespace pdx

@@ -14,6 +14,7 @@
 // reads the residual once per chunk.  Reductions are two-pass (per-block
 // partials then one block) so results are bitwise reproducible.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "device.h"
@@ -434,6 +435,94 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   cudaFreeAsync(dinv, s); cudaFreeAsync(c.part, s); cudaFreeAsync(dscal, s);
   if (bptr) cudaFreeAsync(bptr, s);
   if (binv) cudaFreeAsync(binv, s);
+  if (err == cudaSuccess) err = cudaGetLastError();
+  return err;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Jacobi PCG.
+//
+// Some callers cannot let a library allocate device memory during a solve: a
+// host code that reserves the whole memory budget of the GPU up front for its
+// own pools, or a time-stepping loop that must not be stalled by the
+// allocator between two steps.  For them the Jacobi PCG above also runs with
+// all of its work space (dot-product partials, scalars, 1/diag, r, z, p, q
+// and the residual vector) carved out of one fixed device array,
+// g_noalloc_scratch, so the solve itself issues no cudaMalloc, cudaMallocAsync
+// or cudaFree and calls no allocating library routine.
+//
+// Limits and rules of use:
+//  - n <= kNoAllocMaxN equations (the array holds 6 * kNoAllocMaxN + 1040
+//    doubles, 12.6 MB per device); larger systems are rejected with
+//    cudaErrorInvalidValue before anything is launched;
+//  - the array is global to the device: two solves that overlap in time on
+//    the same device (different streams or host threads) race on it and must
+//    be serialised by the caller;
+//  - no part of the scratch has to start at zero: every word is written
+//    before it is read in each call;
+//  - the first call on a device looks the array's address up with
+//    cudaGetSymbolAddress (once per device, cached); make that first call
+//    before any stream capture begins.
+constexpr int64_t kNoAllocMaxN = 262144;
+constexpr size_t kNoAllocWords = 6 * (size_t)kNoAllocMaxN + kRedBlocks + 16;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocWords];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+}  // namespace
+
+cudaError_t noalloc_scratch_setup(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+int64_t noalloc_max_n() { return kNoAllocMaxN; }
+
+cudaError_t krylov_pcg_noalloc(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int use_x0,
+                               cudaStream_t s, KrylovResult* res) {
+  const int64_t n = A.n;
+  if (n <= 0 || n > kNoAllocMaxN) return cudaErrorInvalidValue;
+  double* w = nullptr;
+  cudaError_t err = noalloc_scratch_setup(&w);
+  if (err != cudaSuccess) return err;
+  const double avg = (double)A.nnz / (double)n;
+  Ctx c{s, w};
+  double* dscal = w + kRedBlocks;
+  double* dinv = dscal + 16;
+  double* r = dinv + n;
+  double* z = r + n;
+  double* p = z + n;
+  double* q = p + n;
+  double* ax = q + n;
+  if (!use_x0) cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  k_diag_inv<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A.ia, A.ja, A.a, dinv);
+  const int iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, 0, nullptr, nullptr, rtol, max_iter,
+                                     dscal, r, z, p, q);
+  // true residual
+  const int g = grid_for(n);
+  spmv_t<double>(n, avg, A.ia, A.ja, A.a, x, ax, s);
+  k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
+  c.dot<double>(n, r, r, dscal + 10);
+  c.dot<double>(n, b, b, dscal + 11);
+  double h[2] = {0, 0};
+  cudaMemcpyAsync(h, dscal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  err = cudaStreamSynchronize(s);
+  res->iterations = iters;
+  res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+  res->converged = res->rel_residual <= rtol;
   if (err == cudaSuccess) err = cudaGetLastError();
   return err;
 }

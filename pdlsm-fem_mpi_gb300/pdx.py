@@ -52,7 +52,7 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array", "pdx_bond_coefficients",
             "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance", "pdx_explicit_advance_timed",
             "pdx_explicit_step_host", "pdx_explicit_step_count", "pdx_get_state", "pdx_assemble_csr",
-            "pdx_solve_csr", "pdx_run"]
+            "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -88,10 +88,12 @@ def lib() -> C.CDLL:
     L.pdx_solve_csr.argtypes = [C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _D, _D, _D,
                                 C.POINTER(SolveOpts), C.POINTER(SolveInfo)]
     L.pdx_run.argtypes = [_P, C.c_char_p]
+    L.pdx_pcg_solve_noalloc.argtypes = [C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts), _P,
+                                        C.POINTER(SolveInfo)]
     for name in ("pdx_model_create_from_cmd", "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array",
                  "pdx_bond_coefficients", "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance",
                  "pdx_explicit_advance_timed", "pdx_explicit_step_host", "pdx_get_state", "pdx_assemble_csr",
-                 "pdx_solve_csr", "pdx_run"):
+                 "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -235,3 +237,16 @@ def solve_csr(ia: np.ndarray, ja: np.ndarray, a: np.ndarray, b: np.ndarray, meth
     if code not in (0, 7):
         _check(code)
     return x, info
+
+
+def pcg_solve_noalloc(n: int, nnz: int, d_ia: int, d_ja: int, d_a: int, d_b: int, d_x: int, rtol: float = 1e-8,
+                      max_iter: int = 20000, use_x0: bool = False, stream: int = 0):
+    """Jacobi PCG on device arrays (raw device addresses: ia int64, ja int32,
+    a, b, x float64) with the library's fixed work space; allocates nothing."""
+    opts = SolveOpts(0, rtol, max_iter, 1 if use_x0 else 0)
+    info = SolveInfo()
+    code = lib().pdx_pcg_solve_noalloc(n, nnz, d_ia, d_ja, d_a, d_b, d_x, C.byref(opts), stream or None,
+                                       C.byref(info))
+    if code not in (0, 7):
+        _check(code)
+    return info, code
