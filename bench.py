@@ -154,8 +154,8 @@ def main():
     ap.add_argument("--precision", default="MIXED", choices=["MIXED", "FP64"])
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: autotuned)")
-    ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: autotuned)")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: default, -1: timed on the model)")
+    ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: default, -1: timed)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = None

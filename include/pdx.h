@@ -38,9 +38,13 @@ typedef struct pdx_model pdx_model;
 typedef struct pdx_options {
   int device;      /* CUDA device ordinal; -1 builds the host setup only (no compute) */
   int precision;   /* -1: PRECISION keyword of the command file; 0 FP64; 1 mixed (FP32 forces) */
-  int lanes;       /* lanes per PD family in the step kernel (4, 8, 16); 0 = autotuned */
+  int lanes;       /* lanes per PD family in the step kernel (4, 8, 16); 0 = default (3D 8, 2D 4);
+                      < 0 = timed on the model at pdx_explicit_init.  The lane counts
+                      fix the order of the force sums: a tuned choice may change
+                      results in the last bits from run to run. */
   int verbose;
-  int fe_lanes;    /* lanes per FE-only node in the step kernel (1, 2, 4); 0 = autotuned */
+  int fe_lanes;    /* lanes per FE-only node in the step kernel (2, 4, 8); 0 = default (4);
+                      < 0 = timed on the model */
 } pdx_options;
 
 typedef struct pdx_model_info {

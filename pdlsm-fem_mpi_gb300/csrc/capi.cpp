@@ -106,6 +106,16 @@ static pdx_status upload_model(pdx_model* m) {
   m->d_me = upload(m, p.me);
   v.fe_adj_ptr = upload(m, p.fe_adj_ptr);
   v.fe_adj = upload(m, p.fe_adj);
+  if (p.n_st_cls > 0) {
+    v.st_cls = upload(m, p.st_cls);
+    v.st_nbr = upload(m, p.st_nbr);
+    v.st_blk64 = upload(m, p.st_blk);
+    const int dd = me.dim * me.dim, w = me.dim == 3 ? 12 : 4;
+    std::vector<float> b32(p.st_blk.size() / dd * w, 0.f);
+    for (size_t i = 0; i < p.st_blk.size() / dd; i++)
+      for (int e = 0; e < dd; e++) b32[i * w + e] = (float)p.st_blk[i * dd + e];
+    v.st_blk32 = upload(m, b32);
+  }
   v.n_nbc = (int)me.nbcs.size();
   if (v.n_nbc) {
     v.ext_ptr = upload(m, p.ext_ptr);
@@ -300,16 +310,18 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
   }
   m->mixed = o.precision >= 0 ? o.precision : m->cmd.precision;
   m->verbose = o.verbose;
-  // Lanes per family / per FE-only node: given, or timed on this model by
-  // pdx_explicit_init (autotune_lanes) with these as the starting point.
-  m->tune = o.lanes <= 0 || o.fe_lanes <= 0;
-  m->lanes = o.lanes > 0 ? o.lanes : 4;
-  m->fe_lanes = o.fe_lanes > 0 ? o.fe_lanes : 2;
-  m->tune_lanes = o.lanes <= 0;
-  m->tune_fe_lanes = o.fe_lanes <= 0;
+  // Lanes per family / per FE-only node: given (> 0), the fixed default (0),
+  // or timed on this model by pdx_explicit_init (< 0, autotune_lanes).  The
+  // lane counts set the order of the force sums, so a fixed choice gives
+  // bitwise reproducible runs and a tuned one may differ in the last bits.
+  m->tune = o.lanes < 0 || o.fe_lanes < 0;
+  m->lanes = o.lanes > 0 ? o.lanes : (m->mesh.dim == 3 ? 8 : 4);
+  m->fe_lanes = o.fe_lanes > 0 ? o.fe_lanes : 4;
+  m->tune_lanes = o.lanes < 0;
+  m->tune_fe_lanes = o.fe_lanes < 0;
   if (!step_lanes_valid(m->lanes, m->fe_lanes)) {
     delete m;
-    return set_error(PDX_ERR_INVALID, "lanes must be 4, 8 or 16 and fe_lanes 1, 2 or 4");
+    return set_error(PDX_ERR_INVALID, "lanes must be 4, 8 or 16 and fe_lanes 2, 4 or 8");
   }
   if (o.device >= 0) {
     m->device = o.device;
@@ -400,6 +412,10 @@ static bool array_ref(const pdx_model* m, const std::string& n, const void** ptr
   if (n == "X") return set(m->mesh.X.data(), m->mesh.X.size(), 8);
   if (n == "conn") return set(m->mesh.conn.data(), m->mesh.conn.size(), 4);
   if (n == "elem_nn") return set(m->mesh.elem_nn.data(), m->mesh.elem_nn.size(), 4);
+  if (n == "feonly") return set(p.feonly.data(), p.feonly.size(), 4);
+  if (n == "st_cls") return set(p.st_cls.data(), p.st_cls.size(), 4);
+  if (n == "st_nbr") return set(p.st_nbr.data(), p.st_nbr.size(), 4);
+  if (n == "st_blk") return set(p.st_blk.data(), p.st_blk.size(), 8);
   if (n == "bcflag") return set(p.bcflag.data(), p.bcflag.size(), 1);
   if (n == "dtv") return set(p.dtv.data(), p.dtv.size(), 8);
   if (n == "material") {
@@ -532,7 +548,7 @@ static pdx_status explicit_reset(pdx_model* m) {
 // afterwards, so tuning changes no result except the FP32 summation order of
 // the mixed-precision forces.
 static pdx_status autotune_lanes(pdx_model* m) {
-  static const int kLp[3] = {4, 8, 16}, kLf[3] = {1, 2, 4};
+  static const int kLp[3] = {4, 8, 16}, kLf[3] = {2, 4, 8};
   const int nlp = m->tune_lanes ? 3 : 1, nlf = m->tune_fe_lanes ? 3 : 1;
   const int lp0 = m->lanes, lf0 = m->fe_lanes;
   cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -11,6 +11,8 @@
 namespace pdx {
 
 constexpr int kMaxFeAdj = 8;      // FE elements around a node (Q4: 4, Hex8: 8)
+constexpr int kStencil2 = 9;      // neighbour slots of an FE-only node's stencil (Q4)
+constexpr int kStencil3 = 27;     // (Hex8)
 
 // Everything a kernel needs, as raw device pointers (passed by value).
 struct DevView {
@@ -46,6 +48,11 @@ struct DevView {
   const float* ke32;
   const int* fe_adj_ptr;    // n_node+1
   const int* fe_adj;        // (fe_local << 3) | local node
+  // node stencils of FE-only nodes (indexed like feonly_node)
+  const int* st_cls;        // stencil class, -1 = element path; null = none
+  const int* st_nbr;        // kStencil2|3 neighbour nodes per FE-only node, -1 padded
+  const float* st_blk32;    // per class and slot: 3D 12 floats (3x3 row-major + pad), 2D 4 floats
+  const double* st_blk64;   // per class and slot: D*D doubles
   // external force (traction BCs): per node list of (nbc id, unit force)
   const int* ext_ptr;       // n_node+1 or null
   const int* ext_nbc;
@@ -137,7 +144,7 @@ struct AsmArgs {
 
 // kernel launchers (return cudaError_t of the launch)
 cudaError_t launch_coeff(const CoeffArgs& a, cudaStream_t s);
-// lp: lanes per PD family (4, 8, 16); lf: lanes per FE-only node (1, 2, 4)
+// lp: lanes per PD family (4, 8, 16); lf: lanes per FE-only node (2, 4, 8)
 bool step_lanes_valid(int lp, int lf);
 cudaError_t launch_step(const StepArgs& a, int mixed, int lp, int lf, cudaStream_t s);
 cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s);

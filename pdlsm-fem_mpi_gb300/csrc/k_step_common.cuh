@@ -16,6 +16,8 @@
 // are gathered by shuffles), so the narrow FP64 pipe sees full warps.
 #pragma once
 
+#include <type_traits>
+
 #include "device.h"
 
 namespace pdx {
@@ -133,47 +135,90 @@ __device__ __forceinline__ void corr_block(const T* corr, int64_t ncorr, int64_t
 // Lane 0 of every item holds F (internal + external force) and its node; the
 // warp's lanes then take one (item, DOF) pair each for the FP64 update, in
 // rounds of 32 / D items.
-template <int D, int L, bool MIXED>
-__device__ __forceinline__ void warp_update(const StepArgs& a, const double* F, int node_or_neg) {
-  constexpr int IPW = 32 / L;                 // items per warp
-  constexpr int IPR = 32 / D;                 // items per round
-  constexpr int ROUNDS = (IPW + IPR - 1) / IPR;
+template <int D, int L>
+struct UpdateOperands {
+  static constexpr int IPW = 32 / L;          // items per warp
+  static constexpr int IPR = 32 / D;          // items per round
+  static constexpr int ROUNDS = (IPW + IPR - 1) / IPR;
+  int n[ROUNDS];                              // node of this lane's (item, DOF) pair, -1 none
+  int eq[ROUNDS];
+  unsigned flag[ROUNDS];
+  double un[ROUNDS], prev[ROUNDS], dt2m[ROUNDS], dtv[ROUNDS];
+};
+
+// Loads what the update of this lane's (item, DOF) pairs needs; it depends
+// only on the items' nodes, so it can be issued before the force is known.
+template <int D, int L>
+__device__ __forceinline__ void update_prefetch(const StepArgs& a, int node_or_neg, UpdateOperands<D, L>& o) {
+  using O = UpdateOperands<D, L>;
   const DevView& v = a.v;
   const int t = threadIdx.x & 31;
   const int jr = t / D, i = t % D;
 #pragma unroll
-  for (int r = 0; r < ROUNDS; r++) {
-    const int j = r * IPR + jr;
-    const bool act = jr < IPR && j < IPW;
-    const int src = (act ? j : 0) * L;
+  for (int r = 0; r < O::ROUNDS; r++) {
+    const int j = r * O::IPR + jr;
+    const bool act = jr < O::IPR && j < O::IPW;
+    const int n = __shfl_sync(kFull, node_or_neg, (act ? j : 0) * L);
+    o.n[r] = act ? n : -1;
+    o.eq[r] = -1;
+    o.flag[r] = 0;
+    o.un[r] = o.prev[r] = o.dt2m[r] = o.dtv[r] = 0.0;
+    if (o.n[r] >= 0) {
+      const int64_t idx = (int64_t)n * D + i;
+      o.un[r] = a.u_n[idx];
+      o.prev[r] = a.u_next[idx];
+      o.eq[r] = v.eq[idx];
+      o.dt2m[r] = v.dt2m[n];
+      o.flag[r] = v.bcflag[n];
+      o.dtv[r] = v.dtv[3 * n + i];
+    }
+  }
+}
+
+// Central-difference update of the active DOFs and the next value of the
+// varying prescribed ones; the mixed kernel also writes the node record.
+template <int D, int L, bool MIXED>
+__device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOperands<D, L>& o, const double* F) {
+  using O = UpdateOperands<D, L>;
+  const int t = threadIdx.x & 31;
+  const int jr = t / D, i = t % D;
+#pragma unroll
+  for (int r = 0; r < O::ROUNDS; r++) {
+    const int j = r * O::IPR + jr;
+    const int src = (jr < O::IPR && j < O::IPW ? j : 0) * L;
     double Fi = 0.0;
 #pragma unroll
     for (int c = 0; c < D; c++) {
       const double x = __shfl_sync(kFull, F[c], src);
       if (c == i) Fi = x;
     }
-    const int n = __shfl_sync(kFull, node_or_neg, src);
+    const int n = o.n[r];
     float uf = 0.f;
-    if (act && n >= 0) {
-      const int64_t idx = (int64_t)n * D + i;
-      const double un = a.u_n[idx];
+    if (n >= 0) {
       double unew;
-      if (v.eq[idx] >= 0) {
-        const double tempA = Fi * v.dt2m[n];
-        unew = a.mode == 0 ? un + 0.5 * tempA : fma(2.0, un, tempA) - a.u_next[idx];
+      if (o.eq[r] >= 0) {
+        const double tempA = Fi * o.dt2m[r];
+        unew = a.mode == 0 ? o.un[r] + 0.5 * tempA : fma(2.0, o.un[r], tempA) - o.prev[r];
       } else {
-        unew = (v.bcflag[n] >> i) & 1u ? un + v.dtv[3 * n + i] : un;
+        unew = (o.flag[r] >> i) & 1u ? o.un[r] + o.dtv[r] : o.un[r];
       }
-      a.u_next[idx] = unew;
+      a.u_next[(int64_t)n * D + i] = unew;
       uf = (float)unew;
     }
     if (MIXED) {
       const float c1 = __shfl_down_sync(kFull, uf, 1);
       const float c2 = __shfl_down_sync(kFull, uf, 2);
-      if (act && n >= 0 && i == 0)
-        a.uf_next[2 * n + 1] = make_float4(uf, c1, D == 3 ? c2 : 0.f, __uint_as_float((unsigned)v.bcflag[n]));
+      if (n >= 0 && i == 0)
+        a.uf_next[2 * n + 1] = make_float4(uf, c1, D == 3 ? c2 : 0.f, __uint_as_float(o.flag[r]));
     }
   }
+}
+
+template <int D, int L, bool MIXED>
+__device__ __forceinline__ void warp_update(const StepArgs& a, const double* F, int node_or_neg) {
+  UpdateOperands<D, L> o;
+  update_prefetch<D, L>(a, node_or_neg, o);
+  update_apply<D, L, MIXED>(a, o, F);
 }
 
 template <int D>
@@ -188,8 +233,53 @@ __device__ __forceinline__ void external_force(const StepArgs& a, int node, doub
   }
 }
 
-// FE-only node item: element rows, then the update.  t = thread index within
-// the FE part of the grid.
+// Stencil rows of an FE-only node: -sum_s K_s u_{nbr_s} over the node's
+// neighbour slots; K_s are the assembled D x D blocks of the node's stencil
+// class (st_blk32: 12 floats per 3D block, 4 per 2D block; st_blk64: D*D
+// doubles).  All of a lane's slots are issued before any is used.
+template <int D, int L, typename T, typename ULoad>
+__device__ __forceinline__ void stencil_rows(const DevView& v, int item, int cls, int lane, const ULoad& uload,
+                                             T* acc) {
+  constexpr int S = D == 2 ? kStencil2 : kStencil3;
+  constexpr int NS = (S + L - 1) / L;
+  const int* nb = v.st_nbr + (int64_t)item * S;
+  int j[NS];
+#pragma unroll
+  for (int q = 0; q < NS; q++) {
+    const int s = q * L + lane;
+    j[q] = s < S ? nb[s] : -1;
+  }
+#pragma unroll
+  for (int q = 0; q < NS; q++) {
+    if (j[q] < 0) continue;
+    const int s = q * L + lane;
+    T un[D];
+    uload(j[q], un);
+    if constexpr (std::is_same<T, float>::value) {
+      if (D == 3) {
+        const float4* B = reinterpret_cast<const float4*>(v.st_blk32) + ((int64_t)cls * S + s) * 3;
+        const float4 b0 = __ldg(B), b1 = __ldg(B + 1), b2 = __ldg(B + 2);
+        acc[0] -= b0.x * un[0] + b0.y * un[1] + b0.z * un[D - 1];
+        acc[1] -= b0.w * un[0] + b1.x * un[1] + b1.y * un[D - 1];
+        acc[D - 1] -= b1.z * un[0] + b1.w * un[1] + b2.x * un[D - 1];
+      } else {
+        const float4 b0 = __ldg(reinterpret_cast<const float4*>(v.st_blk32) + ((int64_t)cls * S + s));
+        acc[0] -= b0.x * un[0] + b0.y * un[1];
+        acc[1] -= b0.z * un[0] + b0.w * un[1];
+      }
+    } else {
+      const double* B = v.st_blk64 + ((int64_t)cls * S + s) * D * D;
+#pragma unroll
+      for (int i = 0; i < D; i++)
+#pragma unroll
+        for (int c = 0; c < D; c++) acc[i] -= __ldg(B + i * D + c) * un[c];
+    }
+  }
+}
+
+// FE-only node item: stencil (or element) rows, then the update, whose
+// operands are requested before the force.  t = thread index within the FE
+// part of the grid.
 template <int D, int L, typename T, bool MIXED, typename ULoad>
 __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int64_t t, const ULoad& uload) {
   const DevView& v = a.v;
@@ -197,14 +287,21 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
   const int lane = (int)(t % L);
   const bool valid = item < v.n_feonly;
   const int node = valid ? v.feonly_node[item] : 0;
+  const int cls = valid && v.st_cls ? v.st_cls[item] : -1;
+  UpdateOperands<D, L> o;
+  update_prefetch<D, L>(a, valid ? node : -1, o);
   T acc[D];
 #pragma unroll
   for (int i = 0; i < D; i++) acc[i] = T(0);
   if (valid) {
-    const int j0 = v.fe_adj_ptr[node], j1 = v.fe_adj_ptr[node + 1];
-    for (int j = j0 + lane; j < j1; j += L) {
-      const int ent = v.fe_adj[j];
-      fe_rows<D, T>(v, ke, ent >> 3, ent & 7, uload, acc);
+    if (cls >= 0) {
+      stencil_rows<D, L, T>(v, item, cls, lane, uload, acc);
+    } else {
+      const int j0 = v.fe_adj_ptr[node], j1 = v.fe_adj_ptr[node + 1];
+      for (int j = j0 + lane; j < j1; j += L) {
+        const int ent = v.fe_adj[j];
+        fe_rows<D, T>(v, ke, ent >> 3, ent & 7, uload, acc);
+      }
     }
   }
   warp_sum<D, L>(acc);
@@ -212,7 +309,7 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
 #pragma unroll
   for (int i = 0; i < D; i++) F[i] = (double)acc[i];
   if (lane == 0 && valid) external_force<D>(a, node, F);
-  warp_update<D, L, MIXED>(a, F, valid ? node : -1);
+  update_apply<D, L, MIXED>(a, o, F);
 }
 
 }  // namespace step

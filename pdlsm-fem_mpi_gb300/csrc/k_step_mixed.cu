@@ -23,6 +23,10 @@ using namespace step;
 
 namespace {
 
+// Bond records in flight per thread: 0 = one record prefetched in registers;
+// K > 0 = a ring of K records per thread in shared memory filled by cp.async.
+constexpr int kRecRing = 0;
+
 template <int D>
 __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, const float* du, float* acc) {
   if (D == 2) {
@@ -36,7 +40,7 @@ __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, c
 }
 
 template <int D, int L>
-__device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float* ke, int64_t t) {
+__device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float* ke, float4* ring, int64_t t) {
   constexpr int RS = D == 3 ? 2 : 1;       // float4 per bond record
   const DevView& v = a.v;
   const float4* nr = a.uf_n;               // node records of u_n
@@ -63,14 +67,37 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
     bool deferred = false;
     int b = b0 + lane;
     float4 ra = make_float4(0, 0, 0, 0), rb = ra;
-    if (b < b1) {
+    // ring slot (s, r) of this thread: ring[(s * RS + r) * blockDim.x + threadIdx.x]
+    auto ring_issue = [&](int bb, int slot) {
+      if (bb < b1) {
+#pragma unroll
+        for (int r = 0; r < RS; r++) {
+          const unsigned dst =
+              (unsigned)__cvta_generic_to_shared(ring + (slot * RS + r) * blockDim.x + threadIdx.x);
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(R + (int64_t)RS * bb + r)
+                       : "memory");
+        }
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if constexpr (kRecRing > 0) {
+#pragma unroll
+      for (int q = 0; q < kRecRing - 1; q++) ring_issue(b + q * L, q);
+    } else if (b < b1) {
       ra = __ldcs(R + (int64_t)RS * b);
       if (D == 3) rb = __ldcs(R + (int64_t)RS * b + 1);
     }
+    int it = 0;
     while (b < b1) {
       const int bn = b + L;
       float4 na = make_float4(0, 0, 0, 0), nb = na;
-      if (bn < b1) {
+      if constexpr (kRecRing > 0) {
+        const int slot = it % kRecRing;
+        ring_issue(b + (kRecRing - 1) * L, (it + kRecRing - 1) % kRecRing);
+        asm volatile("cp.async.wait_group %0;" ::"n"(kRecRing - 1) : "memory");
+        ra = ring[(slot * RS) * blockDim.x + threadIdx.x];
+        if (D == 3) rb = ring[(slot * RS + 1) * blockDim.x + threadIdx.x];
+      } else if (bn < b1) {
         na = __ldcs(R + (int64_t)RS * bn);
         if (D == 3) nb = __ldcs(R + (int64_t)RS * bn + 1);
       }
@@ -119,6 +146,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
       b = bn;
       ra = na;
       rb = nb;
+      it++;
     }
     if (deferred) {
       // Rare: repeat the FP32 test on this lane's bonds and settle the ones
@@ -174,15 +202,17 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
 
 template <int D, int LP, int LF>
 __global__ void __launch_bounds__(256, 4) k_step_mixed(StepArgs a) {
-  extern __shared__ float s_ke[];
+  extern __shared__ __align__(16) float s_ke[];
   const float* ke = a.v.ke32;
   if (a.ke_smem) {
     for (int i = threadIdx.x; i < a.ke_smem; i += blockDim.x) s_ke[i] = a.v.ke32[i];
     __syncthreads();
     ke = s_ke;
   }
+  // bond-record ring (kRecRing slots per thread) after the stiffness classes
+  float4* ring = reinterpret_cast<float4*>(s_ke + ((a.ke_smem + 3) & ~3));
   if ((int)blockIdx.x < a.pd_blocks) {
-    mixed_family_item<D, LP>(a, ke, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    mixed_family_item<D, LP>(a, ke, ring, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   } else {
     const int64_t t = (int64_t)(blockIdx.x - a.pd_blocks) * blockDim.x + threadIdx.x;
     feonly_item<D, LF, float, true>(a, ke, t, LoadMixed<D>{a.uf_n, a.v.dtv});
@@ -214,9 +244,9 @@ __global__ void k_pack_bonds(DevView v, float s0f, float pertf, float4* rec) {
 template <int D, int LP>
 cudaError_t mixed_dispatch_lf(const StepArgs& a, int lf, int blocks, size_t smem, cudaStream_t s) {
   switch (lf) {
-    case 1: k_step_mixed<D, LP, 1><<<blocks, 256, smem, s>>>(a); break;
     case 2: k_step_mixed<D, LP, 2><<<blocks, 256, smem, s>>>(a); break;
     case 4: k_step_mixed<D, LP, 4><<<blocks, 256, smem, s>>>(a); break;
+    case 8: k_step_mixed<D, LP, 8><<<blocks, 256, smem, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -229,7 +259,8 @@ cudaError_t mixed_dispatch(StepArgs a, int lp, int lf, cudaStream_t s) {
   a.pd_blocks = pd_blocks;
   const int blocks = pd_blocks + fe_blocks;
   if (blocks == 0) return cudaSuccess;
-  const size_t smem = (size_t)a.ke_smem * sizeof(float);
+  const size_t smem = (size_t)((a.ke_smem + 3) & ~3) * sizeof(float) +
+                      (size_t)kRecRing * (D == 3 ? 2 : 1) * 256 * sizeof(float4);
   switch (lp) {
     case 4: return mixed_dispatch_lf<D, 4>(a, lf, blocks, smem, s);
     case 8: return mixed_dispatch_lf<D, 8>(a, lf, blocks, smem, s);

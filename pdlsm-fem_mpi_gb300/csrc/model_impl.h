@@ -40,6 +40,11 @@ struct Prepared {
   std::vector<double> L;             // extrapolation matrix
   std::vector<int> fe_adj_ptr, fe_adj;
   int n_cls = 0;
+  // node stencils of FE-only nodes (per FE-only node in feonly order)
+  std::vector<int> st_cls;           // class, -1: element path
+  std::vector<int> st_nbr;           // kStencil2|3 neighbour slots per node, -1 padded
+  std::vector<double> st_blk;        // per class: slots x D x D blocks
+  int n_st_cls = 0;
   // traction BCs
   std::vector<int> ext_ptr, ext_nbc;
   std::vector<double> ext_f;

@@ -11,6 +11,7 @@
 //   pdfemEleQuad4N.cpp eleEquivNodalForce), and the scatter map of every bond /
 //   element block into the CSR pattern.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -56,6 +57,103 @@ void norm_mat_area(const double xN[4][3], bool quad, double Nmat[3][6], bool& ok
   Nmat[0][3] = N2; Nmat[0][5] = N3;
   Nmat[1][3] = N1; Nmat[1][4] = N3;
   Nmat[2][4] = N2; Nmat[2][5] = N1;
+}
+
+// Node stencils of the FE-only nodes.  The FE rows of such a node are
+// -sum_j K_kj u_j with K_kj = sum over the elements around k of the element
+// matrix block (k, j); nodes whose surroundings are the same up to a
+// translation share one table of blocks (a stencil class).  The element
+// entries of a node are taken in the order of their centroids relative to
+// the node and the neighbours in the order of their relative positions, both
+// quantised to 1e-6 of the surrounding element size, so equal surroundings
+// give equal keys and bitwise equal blocks.  Nodes with more than
+// kStencil2/kStencil3 neighbours, or meshes whose classes would not be
+// shared, keep the element path (st_cls = -1).
+void build_stencils(const Mesh& me, Prepared& p) {
+  const int D = me.dim;
+  const int nen = D == 2 ? 4 : 8;
+  const int nd = nen * D;
+  const int S = D == 2 ? kStencil2 : kStencil3;
+  const int nfo = (int)p.feonly.size();
+  p.st_cls.assign(nfo, -1);
+  p.st_nbr.assign((size_t)nfo * S, -1);
+  p.st_blk.clear();
+  p.n_st_cls = 0;
+  std::unordered_map<std::vector<int64_t>, int, VecHash> classes;
+  struct Ent { std::array<int64_t, 3> c; int fe, al; };
+  for (int it = 0; it < nfo; it++) {
+    const int k = p.feonly[it];
+    const double* xk = &me.X[(size_t)k * 3];
+    std::vector<Ent> ent;
+    double Le = 0;
+    for (int j = p.fe_adj_ptr[k]; j < p.fe_adj_ptr[k + 1]; j++) {
+      const int i = p.fe_adj[j] >> 3;
+      for (int a = 0; a < nen; a++)
+        for (int c = 0; c < 3; c++)
+          Le = std::max(Le, std::fabs(me.X[(size_t)p.fe_conn[(size_t)i * 8 + a] * 3 + c] - xk[c]));
+    }
+    if (Le <= 0) continue;
+    const double q = 1e-6 * Le;
+    auto qpos = [&](const double* x) {
+      return std::array<int64_t, 3>{std::llround((x[0] - xk[0]) / q), std::llround((x[1] - xk[1]) / q),
+                                    std::llround((x[2] - xk[2]) / q)};
+    };
+    for (int j = p.fe_adj_ptr[k]; j < p.fe_adj_ptr[k + 1]; j++) {
+      const int i = p.fe_adj[j] >> 3;
+      double c[3] = {0, 0, 0};
+      for (int a = 0; a < nen; a++)
+        for (int d = 0; d < 3; d++) c[d] += me.X[(size_t)p.fe_conn[(size_t)i * 8 + a] * 3 + d] / nen;
+      ent.push_back({qpos(c), i, p.fe_adj[j] & 7});
+    }
+    std::sort(ent.begin(), ent.end(), [](const Ent& x, const Ent& y) {
+      return x.c != y.c ? x.c < y.c : x.fe < y.fe;
+    });
+    std::vector<std::pair<std::array<int64_t, 3>, int>> nb;
+    for (const Ent& e : ent)
+      for (int a = 0; a < nen; a++) {
+        const int n = p.fe_conn[(size_t)e.fe * 8 + a];
+        nb.push_back({qpos(&me.X[(size_t)n * 3]), n});
+      }
+    std::sort(nb.begin(), nb.end());
+    nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+    if ((int)nb.size() > S) continue;
+    std::map<int, int> slot;
+    for (size_t i = 0; i < nb.size(); i++) slot[nb[i].second] = (int)i;
+    std::vector<int64_t> key;
+    key.push_back((int64_t)nb.size());
+    for (const Ent& e : ent) {
+      key.push_back(p.fe_cls[e.fe]);
+      key.push_back(e.al);
+      for (int a = 0; a < nen; a++) key.push_back(slot[p.fe_conn[(size_t)e.fe * 8 + a]]);
+    }
+    auto f = classes.find(key);
+    int cls;
+    if (f == classes.end()) {
+      cls = (int)classes.size();
+      classes.emplace(key, cls);
+      std::vector<double> blk((size_t)S * D * D, 0.0);
+      for (const Ent& e : ent) {
+        const double* K = &p.ke[(size_t)p.fe_cls[e.fe] * nd * nd];
+        for (int a = 0; a < nen; a++) {
+          const int sl = slot[p.fe_conn[(size_t)e.fe * 8 + a]];
+          for (int r = 0; r < D; r++)
+            for (int c = 0; c < D; c++) blk[(size_t)sl * D * D + r * D + c] += K[(e.al * D + r) * nd + a * D + c];
+        }
+      }
+      p.st_blk.insert(p.st_blk.end(), blk.begin(), blk.end());
+    } else {
+      cls = f->second;
+    }
+    p.st_cls[it] = cls;
+    for (size_t i = 0; i < nb.size(); i++) p.st_nbr[(size_t)it * S + i] = nb[i].second;
+  }
+  p.n_st_cls = (int)classes.size();
+  // worth it only when classes are shared
+  if (p.n_st_cls == 0 || (int64_t)p.n_st_cls * 8 > nfo || p.n_st_cls > 4096) {
+    std::fill(p.st_cls.begin(), p.st_cls.end(), -1);
+    p.st_blk.clear();
+    p.n_st_cls = 0;
+  }
 }
 
 }  // namespace
@@ -272,6 +370,7 @@ bool prepare_model(pdx_model* m, Error& err) {
     if (p.fe_adj_ptr[k + 1] - p.fe_adj_ptr[k] > kMaxFeAdj && D == 3) {
       err.code = 3; err.msg = "more than 8 FE elements around a node"; return false;
     }
+  build_stencils(me, p);
   // traction BCs: unit forces per node and NBC
   {
     std::map<std::pair<int, int>, std::array<double, 3>> acc;

@@ -217,3 +217,31 @@ def test_c1_full_size_fp64_parity(built):
         u, sig, phi, bs = m.state()
     assert rel(u, u_o) < FP64_TOL
     assert np.array_equal(bs, bs_o)
+
+
+@pytest.mark.parametrize("lanes,fe_lanes", [(4, 2), (8, 4), (16, 8)])
+def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
+    """A jittered Hex8 box (no shared node stencils: FE-only nodes take the
+    element path) against the oracle, FP64 and mixed, at several lane counts."""
+    d = tempfile.mkdtemp()
+    mesh = meshgen.box_hole(nx=13, ny=9, nz=5, h=1e-3, radius=2e-3, pd_x=8, pd_y=6)
+    rng = np.random.default_rng(5)
+    mesh.X[:, :3] += rng.uniform(-1e-4, 1e-4, mesh.X[:, :3].shape)
+    cmd = meshgen.write_case(mesh, d, "jit", solver="DYNAMIC", dt=2e-8, nsteps=60, save=60, factor=3.015,
+                             nlf=1.0, fc="3 2e-5 3 0.05")
+    host = pdx.Model(cmd, device=-1)
+    assert np.all(host.array("st_cls") == -1)
+    o = orc.Oracle(host)
+    u_o, bs_o, _, nb = o.explicit(nsteps=59)
+    with pdx.Model(cmd, device=0, precision=0, lanes=lanes, fe_lanes=fe_lanes) as m:
+        m.explicit_init()
+        m.explicit_advance(60)
+        u, _, _, bs = m.state()
+    assert rel(u, u_o) < FP64_TOL
+    assert np.array_equal(bs, bs_o)
+    with pdx.Model(cmd, device=0, precision=1, lanes=lanes, fe_lanes=fe_lanes) as m:
+        m.explicit_init()
+        m.explicit_advance(60)
+        u32, _, _, bs32 = m.state()
+    assert rel(u32, u_o) < 1e-4
+    assert int((bs32 != bs_o).sum()) <= max(2, int(0.01 * (bs_o == 0).sum()))
