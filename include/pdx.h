@@ -164,6 +164,25 @@ pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, co
                                  const double* d_a, const double* d_rhs, double* d_x, const pdx_solve_opts* opts,
                                  void* stream, pdx_solve_info* info);
 
+/* Batched explicit runs (no counterpart in the reference, which runs one
+ * model per process): n independent specimens, one command file each, merged
+ * into one model whose explicit step is a single launch over every
+ * specimen's families and nodes.  The result is a pdx_model: pdx_explicit_*,
+ * pdx_get_state (concatenated nodes and family members) and
+ * pdx_model_get_info work on it; pdx_run does not.  Specimens must share the
+ * dimension, precision, failure criterion and per-bond draw (seed,
+ * perturbation), and be explicit dynamic runs without traction BCs;
+ * materials, time steps, critical stretch, sizes and BCs may differ.  Each
+ * specimen's set-up is built exactly as for a single model, so its fields
+ * and broken bonds equal a single-model run's. */
+pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_options* opts, pdx_model** out);
+/* Number of specimens of a batched model (0 for a single model). */
+int pdx_batch_size(const pdx_model* m);
+/* Where specimen i starts in the batch's arrays (n+1 entries each, NULL
+ * skips): nodes (u_all rows, sigma, phi), family members (bond_state of
+ * pdx_get_state), equations. */
+pdx_status pdx_batch_offsets(const pdx_model* m, int64_t* node_off, int64_t* member_off, int64_t* eq_off);
+
 /* Runs the solver the command file selects (pdsolve::pdfemSolver,
  * pdsolve.cpp:5073-5103) and writes the reference's outputs under
  * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM). */

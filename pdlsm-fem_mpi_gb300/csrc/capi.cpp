@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "model_impl.h"
@@ -108,7 +109,12 @@ static pdx_status upload_model(pdx_model* m) {
   v.fe_adj = upload(m, p.fe_adj);
   if (p.n_st_cls > 0) {
     v.st_cls = upload(m, p.st_cls);
-    v.st_nbr = upload(m, p.st_nbr);
+    if (p.st_use_delta) {
+      v.st_dcls = upload(m, p.st_dcls);
+      v.st_delta = upload(m, p.st_delta);
+    } else {
+      v.st_nbr = upload(m, p.st_nbr);
+    }
     v.st_blk64 = upload(m, p.st_blk);
     const int dd = me.dim * me.dim, w = me.dim == 3 ? 12 : 4;
     std::vector<float> b32(p.st_blk.size() / dd * w, 0.f);
@@ -128,9 +134,18 @@ static pdx_status upload_model(pdx_model* m) {
   v.s0_seed = m->cmd.s0_seed;
   v.s0_seed32 = (uint32_t)(m->cmd.s0_seed ^ (m->cmd.s0_seed >> 32));
   v.fam_brk = upload(m, p.fam_brk);
+  v.fam_s0 = upload(m, p.fam_s0);
+  v.fam_s0f = upload(m, to_f32(p.fam_s0));
   v.dt2m = upload(m, p.dt2m);
   v.fail3 = m->cmd.fail_flag == 3 ? 1 : 0;
-  m->d_D = upload(m, p.D);
+  if (m->batch.empty()) {
+    m->d_D = upload(m, p.D);
+    m->d_mat_nu = upload(m, std::vector<double>{me.nu});
+  } else {
+    m->d_D = upload(m, m->mat_D);
+    m->d_mat_nu = upload(m, m->mat_nu);
+    m->d_node_mat = upload(m, m->node_mat);
+  }
   m->d_bgp = upload(m, p.bgp);
   m->d_L = upload(m, p.L);
   m->d_fam_cdv = upload(m, s.fam_cdv);
@@ -181,8 +196,27 @@ static pdx_status upload_model(pdx_model* m) {
   v.n_corr_bond = (int)ca.n_corr;
   for (void* pp : m->buf.ptrs)
     if (!pp) return set_error(PDX_ERR_CUDA, "device allocation failed");
-  pdx_status st = cuda_check(launch_coeff(ca, m->stream), "coefficient kernel launch");
-  if (st) return st;
+  // one launch per coefficient segment (a batch: one per specimen, with its
+  // own Lame constants); all indices inside are global
+  std::vector<CoeffSeg> segs = m->coeff_segs;
+  if (segs.empty()) segs.push_back({0, v.n_fam, m->cmd.nlf, p.lambda, p.mu});
+  pdx_status st = PDX_OK;
+  for (const CoeffSeg& sg : segs) {
+    if (sg.n_fam == 0) continue;
+    CoeffArgs c = ca;
+    c.n_fam = sg.n_fam;
+    c.fam_node = ca.fam_node + sg.fam0;
+    c.fam_ptr = ca.fam_ptr + sg.fam0;
+    c.fam_delta = ca.fam_delta + sg.fam0;
+    c.fam_cdv = ca.fam_cdv + sg.fam0;
+    c.fam_corr = ca.fam_corr + sg.fam0;
+    c.fam_wd = ca.fam_wd + sg.fam0;
+    c.nlf = sg.nlf;
+    c.lambda = sg.lambda;
+    c.mu = sg.mu;
+    st = cuda_check(launch_coeff(c, m->stream), "coefficient kernel launch");
+    if (st) return st;
+  }
   int herr = 0;
   cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
   st = cuda_check(cudaStreamSynchronize(m->stream), "coefficient kernel");
@@ -200,10 +234,11 @@ pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool ph
   a.v = m->view;
   a.u = d_u_all;
   a.D = m->d_D;
+  a.node_mat = m->d_node_mat;
   a.bgp = m->d_bgp;
   a.L = m->d_L;
   a.protype = m->mesh.protype;
-  a.nu = m->mesh.nu;
+  a.nu = m->d_mat_nu;
   a.sigma = sigma ? m->d_sigma : nullptr;
   a.phi = phi ? m->d_phi : nullptr;
   return cuda_check(launch_stress(a, m->stream), "stress kernel");
@@ -287,6 +322,8 @@ pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nb
 
 using namespace pdx;
 
+static pdx_status finish_create(pdx_model* m, const pdx_options& o, pdx_model** out);
+
 extern "C" {
 
 const char* pdx_last_error(void) { return g_err.c_str(); }
@@ -308,6 +345,14 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
                                       : PDX_ERR_PARSE;
     return set_error(code, err.msg);
   }
+  return finish_create(m, o, out);
+}
+
+}  // extern "C"
+
+// Options, device upload and initial explicit state of a model whose host
+// set-up is complete; deletes the model on failure.
+static pdx_status finish_create(pdx_model* m, const pdx_options& o, pdx_model** out) {
   m->mixed = o.precision >= 0 ? o.precision : m->cmd.precision;
   m->verbose = o.verbose;
   // Lanes per family / per FE-only node: given (> 0), the fixed default (0),
@@ -340,6 +385,81 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
   *out = m;
   return PDX_OK;
 }
+
+static pdx_status create_error(const Error& err) {
+  const pdx_status code = err.code == 1   ? PDX_ERR_IO
+                          : err.code == 3 ? PDX_ERR_UNSUPPORTED
+                          : err.code == 4 ? PDX_ERR_INVALID
+                          : err.code == 6 ? PDX_ERR_SINGULAR
+                                          : PDX_ERR_PARSE;
+  return set_error(code, err.msg);
+}
+
+extern "C" {
+
+pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_options* opts, pdx_model** out) {
+  if (!cmd_paths || n <= 0 || !out) return set_error(PDX_ERR_INVALID, "bad argument");
+  *out = nullptr;
+  pdx_options o{0, -1, 0, 0, 0};
+  if (opts) o = *opts;
+  // host set-up of every specimen, in parallel (independent models)
+  std::vector<pdx_model*> parts(n, nullptr);
+  std::vector<Error> errs(n, Error{0, ""});
+  {
+    const int nt = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, t]() {
+        for (int i = t; i < n; i += nt) {
+          if (!cmd_paths[i]) { errs[i] = {4, "null command path"}; continue; }
+          pdx_model* q = new pdx_model();
+          if (!read_command(cmd_paths[i], q->cmd, q->mesh, q->base_dir, errs[i]) ||
+              !build_setup(q->mesh, q->cmd, q->setup, errs[i]) || !prepare_model(q, errs[i])) {
+            delete q;
+            continue;
+          }
+          parts[i] = q;
+        }
+      });
+    for (auto& x : th) x.join();
+  }
+  auto drop = [&]() {
+    for (pdx_model* q : parts) delete q;
+  };
+  for (int i = 0; i < n; i++)
+    if (!parts[i]) {
+      Error e = errs[i];
+      e.msg = "batch specimen " + std::to_string(i) + " (" + cmd_paths[i] + "): " + e.msg;
+      drop();
+      return create_error(e);
+    }
+  pdx_model* m = new pdx_model();
+  Error err{0, ""};
+  if (!merge_batch(parts, m, err)) {
+    drop();
+    delete m;
+    return create_error(err);
+  }
+  m->base_dir = parts[0]->base_dir;
+  drop();
+  return finish_create(m, o, out);
+}
+
+pdx_status pdx_batch_offsets(const pdx_model* m, int64_t* node_off, int64_t* member_off, int64_t* eq_off) {
+  if (!m) return set_error(PDX_ERR_INVALID, "null argument");
+  const size_t n = m->batch.size();
+  if (n == 0) return set_error(PDX_ERR_INVALID, "not a batched model");
+  for (size_t i = 0; i <= n; i++) {
+    const bool end = i == n;
+    const BatchPart& b = m->batch[end ? n - 1 : i];
+    if (node_off) node_off[i] = end ? b.node_off + b.n_node : b.node_off;
+    if (member_off) member_off[i] = end ? b.member_off + b.n_member : b.member_off;
+    if (eq_off) eq_off[i] = end ? b.eq_off + b.n_eq : b.eq_off;
+  }
+  return PDX_OK;
+}
+
+int pdx_batch_size(const pdx_model* m) { return m ? (int)m->batch.size() : 0; }
 
 void pdx_model_destroy(pdx_model* m) {
   if (!m) return;
@@ -534,7 +654,7 @@ static pdx_status explicit_reset(pdx_model* m) {
                   m->stream);
   if (m->mixed) {
     pdx_status st = cuda_check(
-        launch_pack_bonds(m->view, (float)m->cmd.s0, (float)m->cmd.s0_pert, m->d_brec, m->stream), "pack bonds");
+        launch_pack_bonds(m->view, (float)m->cmd.s0_pert, m->d_brec, m->stream), "pack bonds");
     if (st) return st;
   }
   m->cur = 0;

@@ -50,7 +50,9 @@ struct DevView {
   const int* fe_adj;        // (fe_local << 3) | local node
   // node stencils of FE-only nodes (indexed like feonly_node)
   const int* st_cls;        // stencil class, -1 = element path; null = none
-  const int* st_nbr;        // kStencil2|3 neighbour nodes per FE-only node, -1 padded
+  const int* st_nbr;        // kStencil2|3 neighbour nodes per FE-only node, -1 padded (when st_delta is null)
+  const int* st_dcls;       // delta class per FE-only node
+  const int* st_delta;      // per delta class: kStencil2|3 offsets neighbour - node, INT32_MIN empty; or null
   const float* st_blk32;    // per class and slot: 3D 12 floats (3x3 row-major + pad), 2D 4 floats
   const double* st_blk64;   // per class and slot: D*D doubles
   // external force (traction BCs): per node list of (nbc id, unit force)
@@ -64,6 +66,8 @@ struct DevView {
   uint32_t s0_seed32;       // folded seed of the per-bond draw
   int fail3;
   const int* fam_brk;       // least intact-bond count at which a family may still break (damage <= 0.42)
+  const double* fam_s0;     // critical stretch of each family (before the per-bond draw)
+  const float* fam_s0f;
   const double* dt2m;       // dt^2 / lumped mass per node (0 without active DOFs)
 };
 
@@ -120,11 +124,12 @@ struct CoeffArgs {
 struct StressArgs {
   DevView v;
   const double* u;
-  const double* D;          // nv x nv
+  const double* D;          // nv x nv per material
+  const int* node_mat;      // material of each node (null: material 0)
   const double* bgp;        // per class: ngp * nv * nd strain-displacement at stress Gauss points
   const double* L;          // ngp x ngp extrapolation
   int protype;
-  double nu;
+  const double* nu;         // Poisson ratio per material
   double* sigma;            // n_node*6
   double* phi;              // n_node
 };
@@ -149,7 +154,7 @@ bool step_lanes_valid(int lp, int lf);
 cudaError_t launch_step(const StepArgs& a, int mixed, int lp, int lf, cudaStream_t s);
 cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s);
 cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
-cudaError_t launch_pack_bonds(const DevView& v, float s0f, float pertf, float4* rec, cudaStream_t s);
+cudaError_t launch_pack_bonds(const DevView& v, float pertf, float4* rec, cudaStream_t s);
 cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
 cudaError_t launch_assemble(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_newmark_predict(const DevView& v, const double* u, const double* vel, const double* acc,

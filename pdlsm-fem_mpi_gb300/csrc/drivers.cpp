@@ -202,6 +202,8 @@ using namespace pdx;
 extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
   if (!m || !results_dir) return set_error(PDX_ERR_INVALID, "null argument");
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
+  if (!m->batch.empty())
+    return set_error(PDX_ERR_UNSUPPORTED, "a batched model is stepped with pdx_explicit_advance, not pdx_run");
   cudaSetDevice(m->device);
   mkdir(results_dir, 0755);
   const std::string dir(results_dir);

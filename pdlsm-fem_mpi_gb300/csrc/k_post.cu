@@ -42,6 +42,8 @@ __global__ void __launch_bounds__(256) k_stress(StressArgs a) {
   const bool is_fam = valid && item < v.n_fam;
   int node = 0;
   if (valid) node = is_fam ? v.fam_node[item] : v.feonly_node[item - v.n_fam];
+  const int mat = valid && a.node_mat ? a.node_mat[node] : 0;
+  const double* Dm = a.D + (int64_t)mat * NV * NV;
   double eps[NV], sfe[NV];
 #pragma unroll
   for (int i = 0; i < NV; i++) { eps[i] = 0; sfe[i] = 0; }
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(256) k_stress(StressArgs a) {
         for (int r = 0; r < NV; r++) {
           double s = 0;
 #pragma unroll
-          for (int c = 0; c < NV; c++) s += a.D[r * NV + c] * eg[c];
+          for (int c = 0; c < NV; c++) s += Dm[r * NV + c] * eg[c];
           sfe[r] += w * s;
         }
       }
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(256) k_stress(StressArgs a) {
     double s = 0;
     if (is_fam)
 #pragma unroll
-      for (int c = 0; c < NV; c++) s += a.D[r * NV + c] * eps[c];
+      for (int c = 0; c < NV; c++) s += Dm[r * NV + c] * eps[c];
     sig[r] = s + sfe[r];
   }
   const double cnt = (double)((is_fam ? 1 : 0) + nadj);
@@ -135,7 +137,7 @@ __global__ void __launch_bounds__(256) k_stress(StressArgs a) {
     out[3] = sig[2] / cnt;
     out[4] = 0.0;
     out[5] = 0.0;
-    if (a.protype == 2) out[2] = a.nu * (out[0] + out[1]);
+    if (a.protype == 2) out[2] = a.nu[mat] * (out[0] + out[1]);
   } else {
 #pragma unroll
     for (int r = 0; r < 6; r++) out[r] = sig[r] / cnt;

@@ -57,6 +57,7 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
   if (valid) {
     const int b0 = v.fam_ptr[f], b1 = v.fam_ptr[f + 1];
     const bool brk = a.mode >= 1 && v.fail3 && v.fam_intact[f] >= v.fam_brk[f];
+    const double s0fam = v.fam_s0[f];
     const int corr0 = v.fam_corr[f];
     double uk[D], xk[3], ukst[D];
     load_u(node, uk);
@@ -78,9 +79,9 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
         const double xx = xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2];
         const double lhs = 2.0 * (xi[0] * eta[0] + xi[1] * eta[1] + xi[2] * eta[2]) +
                            (eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
-        const double sc = bond_s0(v, h);
+        const double sc = bond_s0(s0fam, v.s0_pert, h);
         const double rhs = sc * (2.0 + sc) * xx;
-        const bool cut = fabs(lhs - rhs) <= 1e-9 * rhs ? stretch_over_fp64<D>(v, a.u_n, node, m, h) : lhs > rhs;
+        const bool cut = fabs(lhs - rhs) <= 1e-9 * rhs ? stretch_over_fp64<D>(v, a.u_n, node, m, sc) : lhs > rhs;
         if (cut) {
           atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
           nbroken++;

@@ -37,9 +37,9 @@ __device__ __forceinline__ uint32_t bond_hash(uint32_t seed, int k, int m) {
   return x;
 }
 
-__device__ __forceinline__ double bond_s0(const DevView& v, uint32_t h) {
-  if (v.s0_pert == 0.0) return v.s0;
-  return v.s0 * (1.0 + v.s0_pert * (2.0 * ((double)(h >> 8) * 0x1.0p-24) - 1.0));
+__device__ __forceinline__ double bond_s0(double s0, double pert, uint32_t h) {
+  if (pert == 0.0) return s0;
+  return s0 * (1.0 + pert * (2.0 * ((double)(h >> 8) * 0x1.0p-24) - 1.0));
 }
 
 __device__ __forceinline__ float bond_s0_f32(float s0, float pert, uint32_t h) {
@@ -47,9 +47,9 @@ __device__ __forceinline__ float bond_s0_f32(float s0, float pert, uint32_t h) {
   return s0 * (1.f + pert * (2.f * ((float)(h >> 8) * 0x1.0p-24f) - 1.f));
 }
 
-// The reference's stretch expression, s = |xi + eta| / |xi| - 1 > s0 (failureCriterion_stretch).
+// The reference's stretch expression, s = |xi + eta| / |xi| - 1 > s_c (failureCriterion_stretch).
 template <int D>
-__device__ __forceinline__ bool stretch_over_fp64(const DevView& v, const double* u, int k, int m, uint32_t h) {
+__device__ __forceinline__ bool stretch_over_fp64(const DevView& v, const double* u, int k, int m, double sc) {
   double xi[3] = {0, 0, 0}, eta[3] = {0, 0, 0};
 #pragma unroll
   for (int i = 0; i < 3; i++) xi[i] = v.X[3 * m + i] - v.X[3 * k + i];
@@ -59,7 +59,7 @@ __device__ __forceinline__ bool stretch_over_fp64(const DevView& v, const double
   const double mag = sqrt((xi[0] + eta[0]) * (xi[0] + eta[0]) + (xi[1] + eta[1]) * (xi[1] + eta[1]) +
                           (xi[2] + eta[2]) * (xi[2] + eta[2]));
   const double s = mag / mag_ref - 1.0;
-  return s > bond_s0(v, h);
+  return s > sc;
 }
 
 template <int D, int L, typename T>
@@ -141,9 +141,8 @@ struct UpdateOperands {
   static constexpr int IPR = 32 / D;          // items per round
   static constexpr int ROUNDS = (IPW + IPR - 1) / IPR;
   int n[ROUNDS];                              // node of this lane's (item, DOF) pair, -1 none
-  int eq[ROUNDS];
-  unsigned flag[ROUNDS];
-  double un[ROUNDS], prev[ROUNDS], dt2m[ROUNDS], dtv[ROUNDS];
+  unsigned flag[ROUNDS];                      // bcflag: bit i varying prescribed, bit 4 + i prescribed
+  double un[ROUNDS], prev[ROUNDS], dt2m[ROUNDS];
 };
 
 // Loads what the update of this lane's (item, DOF) pairs needs; it depends
@@ -160,17 +159,14 @@ __device__ __forceinline__ void update_prefetch(const StepArgs& a, int node_or_n
     const bool act = jr < O::IPR && j < O::IPW;
     const int n = __shfl_sync(kFull, node_or_neg, (act ? j : 0) * L);
     o.n[r] = act ? n : -1;
-    o.eq[r] = -1;
     o.flag[r] = 0;
-    o.un[r] = o.prev[r] = o.dt2m[r] = o.dtv[r] = 0.0;
+    o.un[r] = o.prev[r] = o.dt2m[r] = 0.0;
     if (o.n[r] >= 0) {
       const int64_t idx = (int64_t)n * D + i;
       o.un[r] = a.u_n[idx];
       o.prev[r] = a.u_next[idx];
-      o.eq[r] = v.eq[idx];
       o.dt2m[r] = v.dt2m[n];
       o.flag[r] = v.bcflag[n];
-      o.dtv[r] = v.dtv[3 * n + i];
     }
   }
 }
@@ -196,11 +192,11 @@ __device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOper
     float uf = 0.f;
     if (n >= 0) {
       double unew;
-      if (o.eq[r] >= 0) {
+      if (!((o.flag[r] >> (4 + i)) & 1u)) {
         const double tempA = Fi * o.dt2m[r];
         unew = a.mode == 0 ? o.un[r] + 0.5 * tempA : fma(2.0, o.un[r], tempA) - o.prev[r];
       } else {
-        unew = (o.flag[r] >> i) & 1u ? o.un[r] + o.dtv[r] : o.un[r];
+        unew = (o.flag[r] >> i) & 1u ? o.un[r] + a.v.dtv[3 * n + i] : o.un[r];
       }
       a.u_next[(int64_t)n * D + i] = unew;
       uf = (float)unew;
@@ -238,16 +234,26 @@ __device__ __forceinline__ void external_force(const StepArgs& a, int node, doub
 // class (st_blk32: 12 floats per 3D block, 4 per 2D block; st_blk64: D*D
 // doubles).  All of a lane's slots are issued before any is used.
 template <int D, int L, typename T, typename ULoad>
-__device__ __forceinline__ void stencil_rows(const DevView& v, int item, int cls, int lane, const ULoad& uload,
-                                             T* acc) {
+__device__ __forceinline__ void stencil_rows(const DevView& v, int item, int node, int cls, int dcls, int lane,
+                                             const ULoad& uload, T* acc) {
   constexpr int S = D == 2 ? kStencil2 : kStencil3;
   constexpr int NS = (S + L - 1) / L;
-  const int* nb = v.st_nbr + (int64_t)item * S;
   int j[NS];
+  if (v.st_delta) {
+    const int* dl = v.st_delta + (int64_t)dcls * S;
 #pragma unroll
-  for (int q = 0; q < NS; q++) {
-    const int s = q * L + lane;
-    j[q] = s < S ? nb[s] : -1;
+    for (int q = 0; q < NS; q++) {
+      const int s = q * L + lane;
+      const int d = s < S ? __ldg(dl + s) : INT32_MIN;
+      j[q] = d == INT32_MIN ? -1 : node + d;
+    }
+  } else {
+    const int* nb = v.st_nbr + (int64_t)item * S;
+#pragma unroll
+    for (int q = 0; q < NS; q++) {
+      const int s = q * L + lane;
+      j[q] = s < S ? nb[s] : -1;
+    }
   }
 #pragma unroll
   for (int q = 0; q < NS; q++) {
@@ -288,6 +294,7 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
   const bool valid = item < v.n_feonly;
   const int node = valid ? v.feonly_node[item] : 0;
   const int cls = valid && v.st_cls ? v.st_cls[item] : -1;
+  const int dcls = valid && v.st_delta ? v.st_dcls[item] : 0;
   UpdateOperands<D, L> o;
   update_prefetch<D, L>(a, valid ? node : -1, o);
   T acc[D];
@@ -295,7 +302,7 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
   for (int i = 0; i < D; i++) acc[i] = T(0);
   if (valid) {
     if (cls >= 0) {
-      stencil_rows<D, L, T>(v, item, cls, lane, uload, acc);
+      stencil_rows<D, L, T>(v, item, node, cls, dcls, lane, uload, acc);
     } else {
       const int j0 = v.fe_adj_ptr[node], j1 = v.fe_adj_ptr[node + 1];
       for (int j = j0 + lane; j < j1; j += L) {

@@ -23,9 +23,50 @@ using namespace step;
 
 namespace {
 
-// Bond records in flight per thread: 0 = one record prefetched in registers;
-// K > 0 = a ring of K records per thread in shared memory filled by cp.async.
-constexpr int kRecRing = 0;
+// 32-byte loads (one instruction per bond record or node record).  Bond
+// records are read once per step: they bypass L1 and leave L2 first, so the
+// node records the bonds gather stay cached.
+struct Rec32 {
+  float4 a, b;
+};
+
+__device__ __forceinline__ Rec32 ld_stream32(const float4* p) {
+  Rec32 r;
+  asm("ld.global.L1::no_allocate.L2::evict_first.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z),
+                 "=f"(r.b.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ Rec32 ld_keep32(const float4* p) {
+  Rec32 r;
+  asm("ld.global.L2::evict_last.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(r.a.x), "=f"(r.a.y), "=f"(r.a.z), "=f"(r.a.w), "=f"(r.b.x), "=f"(r.b.y), "=f"(r.b.z),
+                 "=f"(r.b.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ float4 ld_stream16(const float4* p) {
+  float4 r;
+  asm("ld.global.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p));
+  return r;
+}
+
+// record of bond b (3D: 2 float4, 2D: 1)
+template <int D>
+__device__ __forceinline__ void load_record(const float4* R, int64_t b, float4& ra, float4& rb) {
+  if (D == 3) {
+    const Rec32 r = ld_stream32(R + 2 * b);
+    ra = r.a;
+    rb = r.b;
+  } else {
+    ra = ld_stream16(R + b);
+  }
+}
 
 template <int D>
 __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, const float* du, float* acc) {
@@ -40,7 +81,7 @@ __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, c
 }
 
 template <int D, int L>
-__device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float* ke, float4* ring, int64_t t) {
+__device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float* ke, int64_t t) {
   constexpr int RS = D == 3 ? 2 : 1;       // float4 per bond record
   const DevView& v = a.v;
   const float4* nr = a.uf_n;               // node records of u_n
@@ -57,6 +98,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
   if (valid) {
     const int b0 = v.fam_ptr[f], b1 = v.fam_ptr[f + 1];
     const bool brk = a.mode >= 1 && v.fail3 && v.fam_intact[f] >= v.fam_brk[f];
+    const float s0fam = D == 2 ? v.fam_s0f[f] : 0.f;     // 3D records carry their threshold
     const bool force = a.mode != 2;
     const int corr0 = v.fam_corr[f];
     const float4 xk = nr[2 * node];
@@ -67,51 +109,23 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
     bool deferred = false;
     int b = b0 + lane;
     float4 ra = make_float4(0, 0, 0, 0), rb = ra;
-    // ring slot (s, r) of this thread: ring[(s * RS + r) * blockDim.x + threadIdx.x]
-    auto ring_issue = [&](int bb, int slot) {
-      if (bb < b1) {
-#pragma unroll
-        for (int r = 0; r < RS; r++) {
-          const unsigned dst =
-              (unsigned)__cvta_generic_to_shared(ring + (slot * RS + r) * blockDim.x + threadIdx.x);
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(R + (int64_t)RS * bb + r)
-                       : "memory");
-        }
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    if constexpr (kRecRing > 0) {
-#pragma unroll
-      for (int q = 0; q < kRecRing - 1; q++) ring_issue(b + q * L, q);
-    } else if (b < b1) {
-      ra = __ldcs(R + (int64_t)RS * b);
-      if (D == 3) rb = __ldcs(R + (int64_t)RS * b + 1);
-    }
-    int it = 0;
+    if (b < b1) load_record<D>(R, b, ra, rb);
     while (b < b1) {
       const int bn = b + L;
       float4 na = make_float4(0, 0, 0, 0), nb = na;
-      if constexpr (kRecRing > 0) {
-        const int slot = it % kRecRing;
-        ring_issue(b + (kRecRing - 1) * L, (it + kRecRing - 1) % kRecRing);
-        asm volatile("cp.async.wait_group %0;" ::"n"(kRecRing - 1) : "memory");
-        ra = ring[(slot * RS) * blockDim.x + threadIdx.x];
-        if (D == 3) rb = ring[(slot * RS + 1) * blockDim.x + threadIdx.x];
-      } else if (bn < b1) {
-        na = __ldcs(R + (int64_t)RS * bn);
-        if (D == 3) nb = __ldcs(R + (int64_t)RS * bn + 1);
-      }
+      if (bn < b1) load_record<D>(R, bn, na, nb);
       const int m = __float_as_int(D == 3 ? rb.z : ra.w);
       if (m >= 0) {
-        const float4 um = nr[2 * m + 1];
+        const Rec32 nm = ld_keep32(nr + 2 * m);   // position, displacement + flags
+        const float4 um = nm.b;
         bool cut = false;
         if (brk) {
-          const float4 xm = nr[2 * m];
+          const float4 xm = nm.a;
           const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
           const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
           const float xx = x0 * x0 + x1 * x1 + x2 * x2;
           const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
-          const float sc = D == 3 ? rb.w : bond_s0_f32(a.s0f, a.pertf, bond_hash(v.s0_seed32, node, m));
+          const float sc = D == 3 ? rb.w : bond_s0_f32(s0fam, a.pertf, bond_hash(v.s0_seed32, node, m));
           const float rhs = sc * (2.f + sc) * xx;
           if (fabsf(lhs - rhs) <= 2e-4f * rhs) {
             // Near the threshold: decided in FP64 by the pass after the loop,
@@ -146,7 +160,6 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
       b = bn;
       ra = na;
       rb = nb;
-      it++;
     }
     if (deferred) {
       // Rare: repeat the FP32 test on this lane's bonds and settle the ones
@@ -162,10 +175,10 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
         const float xx = x0 * x0 + x1 * x1 + x2 * x2;
         const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
         const uint32_t h = bond_hash(v.s0_seed32, node, m);
-        const float sc = D == 3 ? rb.w : bond_s0_f32(a.s0f, a.pertf, h);
+        const float sc = D == 3 ? rb.w : bond_s0_f32(s0fam, a.pertf, h);
         const float rhs = sc * (2.f + sc) * xx;
         if (!(fabsf(lhs - rhs) <= 2e-4f * rhs)) continue;
-        if (stretch_over_fp64<D>(v, a.u_n, node, m, h)) {
+        if (stretch_over_fp64<D>(v, a.u_n, node, m, bond_s0(v.fam_s0[f], v.s0_pert, h))) {
           int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
           *mslot = ~m;
           atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
@@ -209,10 +222,8 @@ __global__ void __launch_bounds__(256, 4) k_step_mixed(StepArgs a) {
     __syncthreads();
     ke = s_ke;
   }
-  // bond-record ring (kRecRing slots per thread) after the stiffness classes
-  float4* ring = reinterpret_cast<float4*>(s_ke + ((a.ke_smem + 3) & ~3));
   if ((int)blockIdx.x < a.pd_blocks) {
-    mixed_family_item<D, LP>(a, ke, ring, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    mixed_family_item<D, LP>(a, ke, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   } else {
     const int64_t t = (int64_t)(blockIdx.x - a.pd_blocks) * blockDim.x + threadIdx.x;
     feonly_item<D, LF, float, true>(a, ke, t, LoadMixed<D>{a.uf_n, a.v.dtv});
@@ -222,7 +233,7 @@ __global__ void __launch_bounds__(256, 4) k_step_mixed(StepArgs a) {
 // Mixed-precision bond records from the FP32 coefficients, the bond states and
 // the per-bond thresholds.
 template <int D>
-__global__ void k_pack_bonds(DevView v, float s0f, float pertf, float4* rec) {
+__global__ void k_pack_bonds(DevView v, float pertf, float4* rec) {
   const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (f >= v.n_fam) return;
   const int k = v.fam_node[f];
@@ -234,7 +245,7 @@ __global__ void k_pack_bonds(DevView v, float s0f, float pertf, float4* rec) {
     if (D == 2) {
       rec[b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], __int_as_float(mb));
     } else {
-      const float s0b = bond_s0_f32(s0f, pertf, bond_hash(v.s0_seed32, k, m));
+      const float s0b = bond_s0_f32(v.fam_s0f[f], pertf, bond_hash(v.s0_seed32, k, m));
       rec[2 * (int64_t)b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], v.coef32[3 * nb + b]);
       rec[2 * (int64_t)b + 1] = make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(mb), s0b);
     }
@@ -259,8 +270,7 @@ cudaError_t mixed_dispatch(StepArgs a, int lp, int lf, cudaStream_t s) {
   a.pd_blocks = pd_blocks;
   const int blocks = pd_blocks + fe_blocks;
   if (blocks == 0) return cudaSuccess;
-  const size_t smem = (size_t)((a.ke_smem + 3) & ~3) * sizeof(float) +
-                      (size_t)kRecRing * (D == 3 ? 2 : 1) * 256 * sizeof(float4);
+  const size_t smem = (size_t)a.ke_smem * sizeof(float);
   switch (lp) {
     case 4: return mixed_dispatch_lf<D, 4>(a, lf, blocks, smem, s);
     case 8: return mixed_dispatch_lf<D, 8>(a, lf, blocks, smem, s);
@@ -275,11 +285,11 @@ cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s)
   return a.v.dim == 2 ? mixed_dispatch<2>(a, lp, lf, s) : mixed_dispatch<3>(a, lp, lf, s);
 }
 
-cudaError_t launch_pack_bonds(const DevView& v, float s0f, float pertf, float4* rec, cudaStream_t s) {
+cudaError_t launch_pack_bonds(const DevView& v, float pertf, float4* rec, cudaStream_t s) {
   if (v.n_fam == 0) return cudaSuccess;
   const int blocks = (v.n_fam + 7) / 8;
-  if (v.dim == 2) k_pack_bonds<2><<<blocks, 256, 0, s>>>(v, s0f, pertf, rec);
-  else k_pack_bonds<3><<<blocks, 256, 0, s>>>(v, s0f, pertf, rec);
+  if (v.dim == 2) k_pack_bonds<2><<<blocks, 256, 0, s>>>(v, pertf, rec);
+  else k_pack_bonds<3><<<blocks, 256, 0, s>>>(v, pertf, rec);
   return cudaGetLastError();
 }
 

@@ -26,6 +26,7 @@ struct Prepared {
   std::vector<uint32_t> state_bits;  // initial bond states
   std::vector<int> fam_intact;
   std::vector<int> fam_brk;          // least intact count with damage <= 0.42
+  std::vector<double> fam_s0;        // critical stretch per family
   std::vector<double> dt2m;          // dt^2 / mass per node
   std::vector<int> fam_corr;         // slot offset or -1
   std::vector<int> fam_wd;           // W*D index or -1
@@ -45,6 +46,10 @@ struct Prepared {
   std::vector<int> st_nbr;           // kStencil2|3 neighbour slots per node, -1 padded
   std::vector<double> st_blk;        // per class: slots x D x D blocks
   int n_st_cls = 0;
+  std::vector<int> st_dcls;          // delta class per FE-only node, -1 none
+  std::vector<int> st_delta;         // per delta class: slots of (neighbour - node), INT32_MIN empty
+  int n_st_dcls = 0;
+  bool st_use_delta = false;         // kernels read delta classes instead of st_nbr
   // traction BCs
   std::vector<int> ext_ptr, ext_nbc;
   std::vector<double> ext_f;
@@ -52,6 +57,22 @@ struct Prepared {
   std::vector<int> rel_bond, rel_self, rel_fe;
   std::vector<double> D;             // constitutive matrix
   double lambda = 0, mu = 0;
+};
+
+// A specimen of a batched model: where its nodes, family members, equations,
+// families and bonds start in the merged arrays.
+struct BatchPart {
+  int64_t node_off = 0, member_off = 0, eq_off = 0, fam_off = 0, bond_off = 0;
+  int64_t n_node = 0, n_member = 0, n_eq = 0;
+  int n_fam = 0;
+  double dt = 0;
+  std::string title;
+};
+
+// Families [fam0, fam0 + n_fam) get their PDLSM coefficients with these constants.
+struct CoeffSeg {
+  int fam0 = 0, n_fam = 0;
+  double nlf = 0, lambda = 0, mu = 0;
 };
 
 struct DevBuf {
@@ -113,6 +134,13 @@ struct pdx_model {
   double* d_tmp_all = nullptr;       // n_node*dim scratch
   double* d_tmp_eq[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // explicit run state
+  // batched models (empty for a single specimen)
+  std::vector<pdx::BatchPart> batch;
+  std::vector<pdx::CoeffSeg> coeff_segs;
+  std::vector<double> mat_D, mat_nu; // per specimen: constitutive matrix, Poisson ratio
+  std::vector<int> node_mat;         // specimen of each node
+  int* d_node_mat = nullptr;
+  double* d_mat_nu = nullptr;
   int cur = 0;                       // index of the buffer holding u_n
   int64_t steps_done = 0;
   cudaGraphExec_t graph = nullptr;
@@ -129,4 +157,5 @@ pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool ph
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);
+bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& err);
 }  // namespace pdx

@@ -154,6 +154,32 @@ void build_stencils(const Mesh& me, Prepared& p) {
     p.st_blk.clear();
     p.n_st_cls = 0;
   }
+  // Neighbour lists as offsets from the node (node numbering that repeats,
+  // as on structured meshes): nodes with equal offset lists share one delta
+  // class, and the kernel reads a class index instead of S node ids.
+  p.st_dcls.assign(nfo, -1);
+  p.st_delta.clear();
+  p.n_st_dcls = 0;
+  if (p.n_st_cls > 0) {
+    std::unordered_map<std::vector<int64_t>, int, VecHash> dcl;
+    std::vector<int64_t> key(S);
+    for (int it = 0; it < nfo; it++) {
+      if (p.st_cls[it] < 0) continue;
+      const int k = p.feonly[it];
+      for (int i = 0; i < S; i++) {
+        const int j = p.st_nbr[(size_t)it * S + i];
+        key[i] = j < 0 ? INT32_MIN : (int64_t)j - k;
+      }
+      auto f = dcl.find(key);
+      if (f == dcl.end()) {
+        f = dcl.emplace(key, (int)dcl.size()).first;
+        for (int i = 0; i < S; i++) p.st_delta.push_back((int)key[i]);
+      }
+      p.st_dcls[it] = f->second;
+    }
+    p.n_st_dcls = (int)dcl.size();
+  }
+  p.st_use_delta = p.n_st_cls > 0 && (int64_t)p.n_st_dcls * 8 <= nfo && p.n_st_dcls <= 65536;
 }
 
 }  // namespace
@@ -192,6 +218,10 @@ bool prepare_model(pdx_model* m, Error& err) {
         p.dtv[(size_t)n * 3 + b.dof] = c.dt * b.velocity;
       }
     }
+  // bit 4 + i: DOF i has no equation (prescribed), so the update needs no eq
+  for (int k = 0; k < N; k++)
+    for (int i = 0; i < D; i++)
+      if (s.eq[(size_t)k * D + i] < 0) p.bcflag[k] |= (uint8_t)(1u << (4 + i));
   // bonds
   const int nf = (int)s.fam_node.size();
   p.fam_ptr.assign(nf + 1, 0);
@@ -221,6 +251,7 @@ bool prepare_model(pdx_model* m, Error& err) {
       if (!(1.0 - (double)i / ((double)(nbf + 1) - 1.0) > 0.42)) { t = i; break; }
     p.fam_brk[f] = t;
   }
+  p.fam_s0.assign(nf, c.s0);
   p.dt2m.assign(N, 0.0);
   for (int k = 0; k < N; k++)
     if (p.mass_node[k] > 0) p.dt2m[k] = c.dt * c.dt / p.mass_node[k];

@@ -318,6 +318,62 @@ def config_c2(nx: int = 121, ny: int = 61, nz: int = 21, nsteps: int = 5000, pre
                       nlf=1.0, fc="3 2e-3 0 0.05", precision=precision)
 
 
+def _segment_distance(p: np.ndarray, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    ab = b - a
+    t = np.clip(((p - a) @ ab) / (ab @ ab), 0.0, 1.0)
+    return np.linalg.norm(p - (a + t[:, None] * ab), axis=1)
+
+
+def config_c4(n_spec: int = 256, seed: int = 0, nsteps: int = 2000, precision: str = "MIXED",
+              size_range: Tuple[int, int] = (60, 300), h: float = 5e-4, rho: float = 7850.0, nu: float = 0.25):
+    """Batched 2D explicit: n_spec plates of uneven size, each with a hole or an edge pre-crack.
+
+    Per specimen, from one seeded generator: node count uniform in
+    [size_range[0]^2, size_range[1]^2] (square plate, side rounded), a central
+    hole of radius 5-20 % of the width or an edge pre-crack at mid-height of
+    length 5-40 % of the width (half an element above a node row), a PD zone
+    of the elements within 10 h of the defect, E uniform in 50-210 GPa and s0
+    uniform in 5e-4-3e-3.  Bottom edge fixed, top edge pulled at 0.05 m/s,
+    dt = 0.8 x the stable step (the C1 estimate scaled by h and wave speed).
+    Returns a list of (mesh, command keywords)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = size_range
+    c_ref = np.sqrt(72e9 / 2440.0)
+    out = []
+    for i in range(n_spec):
+        count = int(rng.integers(lo * lo, hi * hi + 1))
+        n = int(np.clip(round(np.sqrt(count)), lo, hi))
+        W = (n - 1) * h
+        E = float(rng.uniform(50e9, 210e9))
+        s0 = float(rng.uniform(5e-4, 3e-3))
+        use_hole = bool(rng.random() < 0.5)
+        frac = float(rng.uniform(0.05, 0.20) if use_hole else rng.uniform(0.05, 0.40))
+        cx = cy = W / 2.0
+        cracks = []
+        hole = None
+        if use_hole:
+            r = frac * W
+            hole = (cx, cy, r)
+
+            def pd_mask(cent, r=r):
+                d = np.hypot(cent[:, 0] - cx, cent[:, 1] - cy)
+                return d < r + 10.0 * h
+        else:
+            a = frac * W
+            yc = (n - 1) // 2 * h + 0.5 * h
+            p0 = np.array([0.25 * h, yc]); p1 = np.array([0.25 * h + a, yc])
+            cracks = [np.array([[p0[0], p0[1], 0.0], [p1[0], p1[1], 0.0]])]
+
+            def pd_mask(cent, p0=p0, p1=p1):
+                return _segment_distance(cent[:, :2], p0, p1) < 10.0 * h
+        mesh = plate2d(n, n, h, pd_mask=pd_mask, hole=hole, cracks=cracks, title=f"c4_{i:03d}",
+                       material=(E, nu, rho, 1.0e6, 1.0e8), top_velocity=0.05)
+        dt = 0.8 * 8.99e-8 * (h / 5e-4) * c_ref / np.sqrt(E / rho)
+        out.append((mesh, dict(solver="DYNAMIC", dt=dt, nsteps=nsteps, save=max(1, nsteps), factor=3.015, nlf=1.0,
+                               fc=f"3 {s0:.6e}", precision=precision)))
+    return out
+
+
 CONFIGS = {"c1": config_c1, "c2": config_c2}
 
 

@@ -52,7 +52,8 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array", "pdx_bond_coefficients",
             "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance", "pdx_explicit_advance_timed",
             "pdx_explicit_step_host", "pdx_explicit_step_count", "pdx_get_state", "pdx_assemble_csr",
-            "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc"]
+            "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc", "pdx_batch_create", "pdx_batch_size",
+            "pdx_batch_offsets"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -90,6 +91,12 @@ def lib() -> C.CDLL:
     L.pdx_run.argtypes = [_P, C.c_char_p]
     L.pdx_pcg_solve_noalloc.argtypes = [C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts), _P,
                                         C.POINTER(SolveInfo)]
+    L.pdx_batch_create.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(_P)]
+    L.pdx_batch_create.restype = C.c_int
+    L.pdx_batch_size.argtypes = [_P]
+    L.pdx_batch_size.restype = C.c_int
+    L.pdx_batch_offsets.argtypes = [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.pdx_batch_offsets.restype = C.c_int
     for name in ("pdx_model_create_from_cmd", "pdx_model_get_info", "pdx_model_array_len", "pdx_model_array",
                  "pdx_bond_coefficients", "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance",
                  "pdx_explicit_advance_timed", "pdx_explicit_step_host", "pdx_get_state", "pdx_assemble_csr",
@@ -129,6 +136,28 @@ class Model:
         inf = ModelInfo()
         _check(L.pdx_model_get_info(h, C.byref(inf)))
         self.info = inf
+
+    @classmethod
+    def batch(cls, cmd_paths, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0) -> "Model":
+        """Many specimens (one command file each) merged into one model (pdx_batch_create)."""
+        L = lib()
+        h = _P()
+        opt = Options(device, precision, lanes, 0, fe_lanes)
+        arr = (C.c_char_p * len(cmd_paths))(*[p.encode() for p in cmd_paths])
+        _check(L.pdx_batch_create(arr, len(cmd_paths), C.byref(opt), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        inf = ModelInfo()
+        _check(L.pdx_model_get_info(h, C.byref(inf)))
+        self.info = inf
+        return self
+
+    def batch_offsets(self):
+        """(node_off, member_off, eq_off), n+1 entries each, of a batched model."""
+        n = lib().pdx_batch_size(self._h)
+        outs = [np.zeros(n + 1, dtype=np.int64) for _ in range(3)]
+        _check(lib().pdx_batch_offsets(self._h, *[o.ctypes.data_as(C.POINTER(C.c_int64)) for o in outs]))
+        return tuple(outs)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
