@@ -85,6 +85,43 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def profile_traffic():
+    """DRAM bytes (read + write) per step-kernel launch from the committed ncu summary of this workload."""
+    try:
+        with open(os.path.join(REPO, "profiles", "k_step_mixed_c2.md")) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def make_batch_workload(tmp: str, n_spec: int, nsteps: int, precision: str):
+    import meshgen
+    specs = meshgen.config_c4(n_spec=n_spec, nsteps=nsteps, precision=precision)
+    return [meshgen.write_case(m, tmp, f"c4_{i:03d}", **kw) for i, (m, kw) in enumerate(specs)]
+
+
+def cpu_sample_batch(cmds, target_s: float = 15.0, threads: int = 0):
+    """Oracle on the first specimens of a batch, each from its initial state, until target_s of CPU work."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import orc
+    import pdx
+    bonds_steps, el, used = 0, 0.0, 0
+    for c in cmds:
+        host = pdx.Model(c, device=-1)
+        o = orc.Oracle(host, nthreads=threads)
+        t = time.perf_counter()
+        o.explicit(nsteps=3)
+        el += time.perf_counter() - t
+        bonds_steps += host.info.n_bond * 4
+        used += 1
+        if el > target_s:
+            break
+    return bonds_steps / el, used, el, o_threads()
+
+
 def make_workload(tmp: str, nsteps: int, precision: str):
     import meshgen
     mesh, kw = meshgen.config_c2(nsteps=nsteps, precision=precision)
@@ -156,6 +193,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: default, -1: timed on the model)")
     ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: default, -1: timed)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+                    help="c2: 3D box with hole (default); c4: batch of uneven 2D plates in one launch")
+    ap.add_argument("--specimens", type=int, default=256, help="c4: number of specimens")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     dist = None
@@ -164,25 +204,41 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     tmp = tempfile.mkdtemp(prefix="pdx_bench_")
-    cmd = make_workload(tmp, args.steps + args.warmup + 1, args.precision)
-    config = {"workload": "c2: 3D explicit box with hole, 121x61x21 nodes, Hex8 + PDLSM zone 40x40, s0=2e-3+-5%",
-              "precision": args.precision, "inputs_vs_l2": "bond data streamed per step exceeds the 129 MB L2",
-              "step": "one central-difference step (failure + force + update)"}
+    nsteps_cmd = args.steps + args.warmup + 1
+    if args.workload == "c2":
+        cmd = make_workload(tmp, nsteps_cmd, args.precision)
+        config = {"workload": "c2: 3D explicit box with hole, 121x61x21 nodes, Hex8 + PDLSM zone 40x40, "
+                              "s0=2e-3+-5%",
+                  "precision": args.precision, "inputs_vs_l2": "bond data streamed per step exceeds the 129 MB L2",
+                  "step": "one central-difference step (failure + force + update)"}
+    else:
+        cmd = make_batch_workload(tmp, args.specimens, nsteps_cmd, args.precision)
+        config = {"workload": f"c4: {args.specimens} 2D plates of 60x60..300x300 nodes (seeded), hole or edge "
+                              "crack, PD band 10h, E 50-210 GPa, s0 5e-4..3e-3, one launch per step",
+                  "precision": args.precision, "inputs_vs_l2": "per-step node and bond data exceed the 129 MB L2",
+                  "step": "one central-difference step of every specimen (failure + force + update)"}
     if args.impl == "reference":
         if rank != 0:
             return
-        rate, n, el, cores = cpu_sample(cmd, target_s=20.0)
+        rate, n, el, cores = cpu_sample(cmd, target_s=20.0) if args.workload == "c2" else \
+            cpu_sample_batch(cmd, target_s=20.0)
         line = {"metric": "explicit PD bond-updates/s", "value": rate, "unit": "bond-updates/s", "n_gpus": args.gpus,
                 "steps": n, "warmup": 0, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",
-                                 "sample": f"{n} explicit steps of the full C2 model on {cores} host threads"},
+                                 "sample": (f"{n} explicit steps of the full C2 model on {cores} host threads"
+                                            if args.workload == "c2" else
+                                            f"4 explicit steps of each of the first {n} specimens on {cores} "
+                                            "host threads")},
                 "e2e": {"value": rate, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
     import pdx
-    model = pdx.Model(cmd, device=local, precision=1 if args.precision == "MIXED" else 0, lanes=args.lanes,
-                      fe_lanes=args.fe_lanes)
+    prec = 1 if args.precision == "MIXED" else 0
+    if args.workload == "c2":
+        model = pdx.Model(cmd, device=local, precision=prec, lanes=args.lanes, fe_lanes=args.fe_lanes)
+    else:
+        model = pdx.Model.batch(cmd, device=local, precision=prec, lanes=args.lanes, fe_lanes=args.fe_lanes)
     info = model.info
     alg = algorithmic_bytes(model)
     # warm-up steps (step 0 included), then the timed region
@@ -231,19 +287,26 @@ def main():
     line = {"metric": "explicit PD bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 forces / f64 state" if args.precision == "MIXED"
-            else "f64", "data": "synthetic (seeded meshgen config_c2)", "config": config,
+            else "f64", "data": f"synthetic (seeded meshgen config_{args.workload})", "config": config,
             "e2e": {"value": e2e, "unit": "bond-updates/s", "h2d_bytes_per_step": 2 * info.n_eq * 8,
                     "d2h_bytes_per_step": info.n_eq * 8, "steps": args.e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": kind,
+                         "frac": achieved / peak,
+                         "traffic": profile_traffic() if args.precision == "MIXED" else None,
+                         "traffic_unit": "bytes per launch (ncu, profiles/k_step_mixed_c2.md)", "peak_kind": kind,
                          "algorithmic_bytes_per_step": alg["bytes"], "kernel": "k_step"},
             "gpu_launches": args.steps, "clocks": clk,
             "model": {"n_node": info.n_node, "n_fam": info.n_fam, "n_bond": info.n_bond, "n_eq": info.n_eq,
                       "n_fe": info.n_fe, "lanes": info.lanes, "fe_lanes": info.fe_lanes}}
     if rank == 0 and not args.no_cpu_baseline:
-        rate, n, el, cores = cpu_sample(cmd, target_s=15.0)
+        if args.workload == "c2":
+            rate, n, el, cores = cpu_sample(cmd, target_s=15.0)
+            sample = f"{n} explicit steps of the full model (FP64 oracle) on {cores} threads"
+        else:
+            rate, n, el, cores = cpu_sample_batch(cmd, target_s=15.0)
+            sample = f"4 explicit steps of each of the first {n} specimens (FP64 oracle) on {cores} threads"
         line["cpu_baseline"] = {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",
-                                "sample": f"{n} explicit steps of the full model (FP64 oracle) on {cores} threads"}
+                                "sample": sample}
     if rank == 0:
         print(json.dumps(line))
     model.close()
