@@ -97,9 +97,11 @@ static pdx_status upload_model(pdx_model* m) {
   double* coef64 = m->buf.alloc<double>((size_t)NC * v.n_bond);
   float* coef32 = m->buf.alloc<float>((size_t)NC * v.n_bond);
   double* corr64 = m->buf.alloc<double>((size_t)D * D * std::max<int64_t>(p.n_corr, 1));
-  float* corr32 = m->buf.alloc<float>((size_t)D * D * std::max<int64_t>(p.n_corr, 1));
+  float* corr32 = m->buf.alloc<float>((size_t)(D == 2 ? 4 : 8) * std::max<int64_t>(p.n_corr, 1));
+  float* corr32_last = m->buf.alloc<float>((size_t)std::max<int64_t>(p.n_corr, 1));
   double* cvec = m->buf.alloc<double>((size_t)D * v.n_bond);
   v.coef64 = coef64; v.coef32 = coef32; v.corr64 = corr64; v.corr32 = corr32; v.cvec = cvec;
+  v.corr32_last = corr32_last;
   v.fe_conn = upload(m, p.fe_conn);
   v.fe_cls = upload(m, p.fe_cls);
   v.ke64 = upload(m, p.ke);
@@ -190,6 +192,7 @@ static pdx_status upload_model(pdx_model* m) {
   ca.lambda = p.lambda;
   ca.mu = p.mu;
   ca.coef64 = coef64; ca.coef32 = coef32; ca.corr64 = corr64; ca.corr32 = corr32; ca.cvec = cvec;
+  ca.corr32_last = corr32_last;
   int* derr = m->buf.alloc<int>(1);
   cudaMemsetAsync(derr, 0, sizeof(int), m->stream);
   ca.err = derr;

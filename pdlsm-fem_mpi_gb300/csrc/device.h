@@ -39,7 +39,8 @@ struct DevView {
   const double* coef64;     // (3|6) * n_bond symmetric block G*dv_k*dv_m
   const float* coef32;
   const double* corr64;     // (4|9) * n_corr_bond general PD-boundary block
-  const float* corr32;
+  const float* corr32;      // FP32 per bond record: 2D 4 floats, 3D 8 floats (+ corr32_last)
+  const float* corr32_last; // 3D: the ninth entry of each block
   const double* cvec;       // dim * n_bond strain-operator columns omega*g*dv_m
   // FE
   const int* fe_conn;       // n_fe*8
@@ -112,7 +113,8 @@ struct CoeffArgs {
   double* coef64;
   float* coef32;
   double* corr64;
-  float* corr32;
+  float* corr32;            // per bond record (see DevView)
+  float* corr32_last;
   double* cvec;
   double* A_out;            // optional dumps
   double* g_out;

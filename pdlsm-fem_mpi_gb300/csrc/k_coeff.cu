@@ -231,7 +231,13 @@ __global__ void __launch_bounds__(kWarps * 32) k_coeff(CoeffArgs a) {
 #pragma unroll
         for (int j = 0; j < D; j++) {
           a.corr64[(int64_t)(i * D + j) * a.n_corr + slot] = P[i][j];
-          if (a.corr32) a.corr32[(int64_t)(i * D + j) * a.n_corr + slot] = (float)P[i][j];
+          // FP32 copy, one record per bond: 2D 4 floats; 3D 8 floats + the last in corr32_last
+          const int idx = i * D + j;
+          if (a.corr32) {
+            if (D == 2) a.corr32[slot * 4 + idx] = (float)P[i][j];
+            else if (idx < 8) a.corr32[slot * 8 + idx] = (float)P[i][j];
+            else a.corr32_last[slot] = (float)P[i][j];
+          }
         }
     }
     if (a.g_out)

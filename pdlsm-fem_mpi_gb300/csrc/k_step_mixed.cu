@@ -56,6 +56,23 @@ __device__ __forceinline__ float4 ld_stream16(const float4* p) {
   return r;
 }
 
+// PD-boundary correction of a bond, P du, from its FP32 record (2D: one
+// float4 = 2x2 block; 3D: 8 floats in one 32-byte load + the ninth entry).
+template <int D>
+__device__ __forceinline__ void corr_apply(const DevView& v, int64_t slot, const float* du, float* acc) {
+  if (D == 2) {
+    const float4 c = ld_stream16(reinterpret_cast<const float4*>(v.corr32) + slot);
+    acc[0] += c.x * du[0] + c.y * du[1];
+    acc[1] += c.z * du[0] + c.w * du[1];
+  } else {
+    const Rec32 c = ld_stream32(reinterpret_cast<const float4*>(v.corr32) + 2 * slot);
+    const float c8 = v.corr32_last[slot];
+    acc[0] += c.a.x * du[0] + c.a.y * du[1] + c.a.z * du[D - 1];
+    acc[1] += c.a.w * du[0] + c.b.x * du[1] + c.b.y * du[D - 1];
+    acc[D - 1] += c.b.z * du[0] + c.b.w * du[1] + c8 * du[D - 1];
+  }
+}
+
 // record of bond b (3D: 2 float4, 2D: 1)
 template <int D>
 __device__ __forceinline__ void load_record(const float4* R, int64_t b, float4& ra, float4& rb) {
@@ -123,10 +140,14 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
           const float4 xm = nm.a;
           const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
           const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
-          const float xx = x0 * x0 + x1 * x1 + x2 * x2;
           const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
-          const float sc = D == 3 ? rb.w : bond_s0_f32(s0fam, a.pertf, bond_hash(v.s0_seed32, node, m));
-          const float rhs = sc * (2.f + sc) * xx;
+          float rhs;
+          if (D == 3) {
+            rhs = rb.w;     // s0b (2 + s0b) |xi|^2, from the record
+          } else {
+            const float sc = bond_s0_f32(s0fam, a.pertf, bond_hash(v.s0_seed32, node, m));
+            rhs = sc * (2.f + sc) * (x0 * x0 + x1 * x1 + x2 * x2);
+          }
           if (fabsf(lhs - rhs) <= 2e-4f * rhs) {
             // Near the threshold: decided in FP64 by the pass after the loop,
             // which also adds the bond's force if it stays intact.
@@ -154,7 +175,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
 #pragma unroll
           for (int i = 0; i < D; i++) du[i] -= uk[i];
           bond_force<D>(ra, rb, du, acc);
-          if (corr0 >= 0) corr_block<D, float>(v.corr32, v.n_corr_bond, (int64_t)corr0 + (b - b0), du, acc);
+          if (corr0 >= 0) corr_apply<D>(v, (int64_t)corr0 + (b - b0), du, acc);
         }
       }
       b = bn;
@@ -172,11 +193,15 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
         const float4 xm = nr[2 * m], um = nr[2 * m + 1];
         const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
         const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
-        const float xx = x0 * x0 + x1 * x1 + x2 * x2;
         const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
         const uint32_t h = bond_hash(v.s0_seed32, node, m);
-        const float sc = D == 3 ? rb.w : bond_s0_f32(s0fam, a.pertf, h);
-        const float rhs = sc * (2.f + sc) * xx;
+        float rhs;
+        if (D == 3) {
+          rhs = rb.w;
+        } else {
+          const float sc = bond_s0_f32(s0fam, a.pertf, h);
+          rhs = sc * (2.f + sc) * (x0 * x0 + x1 * x1 + x2 * x2);
+        }
         if (!(fabsf(lhs - rhs) <= 2e-4f * rhs)) continue;
         if (stretch_over_fp64<D>(v, a.u_n, node, m, bond_s0(v.fam_s0[f], v.s0_pert, h))) {
           int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
@@ -189,7 +214,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
 #pragma unroll
           for (int i = 0; i < D; i++) du[i] -= uk[i];
           bond_force<D>(ra, rb, du, acc);
-          if (corr0 >= 0) corr_block<D, float>(v.corr32, v.n_corr_bond, (int64_t)corr0 + (b - b0), du, acc);
+          if (corr0 >= 0) corr_apply<D>(v, (int64_t)corr0 + (b - b0), du, acc);
         }
       }
     }
@@ -245,9 +270,13 @@ __global__ void k_pack_bonds(DevView v, float pertf, float4* rec) {
     if (D == 2) {
       rec[b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], __int_as_float(mb));
     } else {
+      // threshold of the sqrt-free stretch test, s0b (2 + s0b) |xi|^2, from the FP32 positions
       const float s0b = bond_s0_f32(v.fam_s0f[f], pertf, bond_hash(v.s0_seed32, k, m));
+      const float4 xk = v.Xf[k], xm = v.Xf[m];
+      const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
+      const float thr = s0b * (2.f + s0b) * (x0 * x0 + x1 * x1 + x2 * x2);
       rec[2 * (int64_t)b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], v.coef32[3 * nb + b]);
-      rec[2 * (int64_t)b + 1] = make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(mb), s0b);
+      rec[2 * (int64_t)b + 1] = make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(mb), thr);
     }
   }
 }
