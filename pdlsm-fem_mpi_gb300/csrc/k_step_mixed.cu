@@ -239,7 +239,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
 }
 
 template <int D, int LP, int LF>
-__global__ void __launch_bounds__(256, 4) k_step_mixed(StepArgs a) {
+__global__ void __launch_bounds__(256, D == 3 ? 5 : 4) k_step_mixed(StepArgs a) {
   extern __shared__ __align__(16) float s_ke[];
   const float* ke = a.v.ke32;
   if (a.ke_smem) {
