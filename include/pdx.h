@@ -164,6 +164,41 @@ pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, co
                                  const double* d_a, const double* d_rhs, double* d_x, const pdx_solve_opts* opts,
                                  void* stream, pdx_solve_info* info);
 
+/* Implicit Newmark dynamics one step at a time (pdfemDynamicNewmarkSolver_CSRformat,
+ * pdsolve.cpp:6092-6290, beta and gamma from the NEWMARK keyword): predictor,
+ * K_N = beta dt^2 K + M assembled on the GPU (pdfemAssembleKNFR_CSRformat
+ * :6327-6397), K_N a = F solved by `method`, update (updateDispVelo
+ * :6399-6422).  The reference factorises K_N with PARDISO at every step.
+ * method: 0-3 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
+ * method); 5 flexible CG with block-Jacobi plus the learned coarse correction,
+ * falling back to 4 and then BiCGStab when it stalls.  collect = 1 (method 4)
+ * stores one training pair per iteration of the solve.  info: iterations,
+ * true FP64 residual, device time of the solve. */
+pdx_status pdx_newmark_init(pdx_model* m);
+pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_info* info);
+
+/* Learned two-level preconditioner (no counterpart in the reference, which
+ * solves directly).  A regular coarse grid of cx x cy (x cz) cells over the
+ * model's bounding box, trilinear prolongation P and restriction P^T, and a
+ * 3-layer MLP (hidden width `hidden`, Xavier-uniform weights from `seed`)
+ * that maps the normalised restricted residual to the coarse error; trained
+ * with BF16 operands and FP32 accumulation on the pairs that
+ * pdx_newmark_step(m, 4, 1, ...) collects (at most max_samples). */
+pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, uint64_t seed, int max_samples);
+int64_t pdx_learned_samples(const pdx_model* m);
+/* Adam over all collected pairs for `epochs` epochs (batches of 64, order
+ * shuffled from `seed`); final_loss = mean relative squared error of the
+ * last epoch. */
+pdx_status pdx_learned_train(pdx_model* m, int epochs, float lr, uint64_t seed, float* final_loss);
+/* Network parameters (FP32: W1 b1 W2 b2 W3 b3, row-major): count, read (get)
+ * and/or replace (set); NULL skips. */
+pdx_status pdx_mlp_params(pdx_model* m, float* get, const float* set, int64_t* count);
+/* Loss sum_b w_b |N(x_b) - t_b|^2 and its gradient with respect to the
+ * parameters for a batch (<= 64) of inputs x (batch x n_coarse, rounded to
+ * BF16 as in training) and targets t; for gradient checks. */
+pdx_status pdx_mlp_loss_grad(pdx_model* m, int batch, const float* x, const float* t, const float* w, float* loss,
+                             float* grad);
+
 /* Batched explicit runs (no counterpart in the reference, which runs one
  * model per process): n independent specimens, one command file each, merged
  * into one model whose explicit step is a single launch over every

@@ -470,6 +470,7 @@ void pdx_model_destroy(pdx_model* m) {
     cudaSetDevice(m->device);
     if (m->graph) cudaGraphExecDestroy(m->graph);
     if (m->stream) cudaStreamSynchronize(m->stream);
+    learned_destroy(m);
     m->buf.free_all();
     if (m->stream) cudaStreamDestroy(m->stream);
   }

@@ -185,6 +185,28 @@ struct KrylovResult {
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
                          int block_dim, cudaStream_t s, KrylovResult* res);
 cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
+
+// Additive second level of a preconditioner: z += C(r) (learned.cpp, k_learned.cu).
+struct CoarseCorrection {
+  virtual ~CoarseCorrection() = default;
+  virtual cudaError_t add(const double* r, double* z, cudaStream_t s) = 0;
+};
+// Called with the current iterate, residual and preconditioned residual every
+// `every` iterations of a flexible CG solve (training-data collection).
+struct IterHook {
+  virtual ~IterHook() = default;
+  int every = 1;
+  virtual cudaError_t on_iter(int it, const double* x, const double* r, const double* z, cudaStream_t s) = 0;
+};
+// Flexible CG with block-Jacobi (d x d blocks of consecutive rows) plus an
+// optional additive coarse correction; each direction is A-orthogonalised
+// against the last `trunc` directions (trunc = 1 with a fixed preconditioner
+// is PCG); stops on the true FP64 residual.  A solve whose residual has not
+// dropped 10x over `stall_window` iterations (0: never) stops early with
+// res->converged = 0, so that the caller can fall back.
+cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int block_dim,
+                       CoarseCorrection* coarse, IterHook* hook, int stall_window, int trunc, cudaStream_t s,
+                       KrylovResult* res);
 // Jacobi PCG with its work space in a fixed device array (no allocation);
 // n <= noalloc_max_n(), one solve at a time per device.
 cudaError_t krylov_pcg_noalloc(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int use_x0,

@@ -440,6 +440,143 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
 }
 
 // ---------------------------------------------------------------------------
+// Flexible CG with block-Jacobi and an optional additive coarse correction.
+// Each new direction p = z - sum_j (z . q_j / p_j . q_j) p_j is A-orthogonal
+// to the last `trunc` directions (q_j = A p_j): with a fixed SPD
+// preconditioner and trunc = 1 this is PCG; with the learned (nonlinear)
+// coarse correction the longer memory keeps the iteration from stalling.
+
+namespace {
+// p -= (zq / pq) pj
+__global__ void k_fcg_orth(int64_t n, const double* zq, const double* pq, const double* pj, double* p) {
+  const double c = *pq != 0.0 ? *zq / *pq : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] -= c * pj[i];
+}
+}  // namespace
+
+cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int block_dim,
+                       CoarseCorrection* coarse, IterHook* hook, int stall_window, int trunc, cudaStream_t s,
+                       KrylovResult* res) {
+  const int64_t n = A.n;
+  const double avg = n ? (double)A.nnz / (double)n : 0.0;
+  const int g = grid_for(n);
+  Ctx c{s, nullptr};
+  double* dscal = nullptr;
+  cudaMallocAsync(&c.part, kRedBlocks * sizeof(double), s);
+  cudaMallocAsync(&dscal, 16 * sizeof(double), s);
+  double* rp = dscal + 0;
+  double* zq = dscal + 1;
+  double* rr = dscal + 2;
+  double* bb = dscal + 3;
+  // block-Jacobi: inverses of the d x d diagonal blocks of consecutive rows
+  const int bd = block_dim > 0 ? block_dim : 3;
+  const int64_t nb = (n + bd - 1) / bd;
+  std::vector<int64_t> hp(nb + 1);
+  for (int64_t i = 0; i <= nb; i++) hp[i] = std::min<int64_t>(i * bd, n);
+  int64_t* bptr = nullptr;
+  double* binv = nullptr;
+  cudaMallocAsync(&bptr, (nb + 1) * sizeof(int64_t), s);
+  cudaMallocAsync(&binv, nb * 9 * sizeof(double), s);
+  cudaMemcpyAsync(bptr, hp.data(), (nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s);
+  k_block_inverse<<<(int)((nb + 255) / 256), 256, 0, s>>>(nb, bptr, A.ia, A.ja, A.a, binv);
+  // ring of the last `trunc` directions p_j, q_j = A p_j (and the new one)
+  const int mt = std::max(1, trunc) + 1;
+  std::vector<double*> P(mt, nullptr), Q(mt, nullptr);
+  double *r, *z, *pqs;
+  cudaMallocAsync(&r, n * sizeof(double), s);
+  cudaMallocAsync(&z, n * sizeof(double), s);
+  cudaMallocAsync(&pqs, mt * sizeof(double), s);
+  for (int j = 0; j < mt; j++) {
+    cudaMallocAsync(&P[j], n * sizeof(double), s);
+    cudaMallocAsync(&Q[j], n * sizeof(double), s);
+  }
+  cudaError_t err = cudaSuccess;
+  auto precond = [&](const double* rin, double* zout) {
+    k_apply_block<double><<<(int)((nb + 255) / 256), 256, 0, s>>>(nb, bptr, binv, rin, zout);
+    if (coarse && err == cudaSuccess) err = coarse->add(rin, zout, s);
+  };
+  spmv_t<double>(n, avg, A.ia, A.ja, A.a, x, Q[0], s);
+  k_sub<double><<<g, kThreads, 0, s>>>(n, b, Q[0], r);
+  c.dot<double>(n, b, b, bb);
+  precond(r, z);
+  double hb = 0;
+  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double bnorm = std::sqrt(hb);
+  int it = 0;
+  bool stalled = false;
+  if (bnorm == 0.0) {
+    cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  } else {
+    const int chunk = 10;
+    double win_start = -1.0;
+    int win_it = 0;
+    while (it < max_iter && err == cudaSuccess) {
+      for (int k = 0; k < chunk && it < max_iter; k++, it++) {
+        const int slot = it % mt;
+        double* p = P[slot];
+        double* q = Q[slot];
+        cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        for (int j = 1; j <= std::min(it, mt - 1); j++) {
+          const int js = (it - j) % mt;
+          c.dot<double>(n, z, Q[js], zq);
+          k_fcg_orth<<<g, kThreads, 0, s>>>(n, zq, pqs + js, P[js], p);
+        }
+        spmv_t<double>(n, avg, A.ia, A.ja, A.a, p, q, s);
+        c.dot<double>(n, p, q, pqs + slot);
+        c.dot<double>(n, r, p, rp);
+        k_cg_update<double><<<g, kThreads, 0, s>>>(n, rp, pqs + slot, p, q, x, r);
+        precond(r, z);
+        if (hook && (it + 1) % hook->every == 0 && err == cudaSuccess) err = hook->on_iter(it + 1, x, r, z, s);
+      }
+      c.dot<double>(n, r, r, rr);
+      double hr = 0;
+      cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      const double rn = std::sqrt(hr);
+      if (!(rn > rtol * bnorm)) break;
+      if (!(rn == rn)) { stalled = true; break; }
+      if (stall_window > 0) {
+        if (win_start < 0) {
+          win_start = rn;
+          win_it = it;
+        } else if (it - win_it >= stall_window) {
+          if (rn > 0.1 * win_start) { stalled = true; break; }
+          win_start = rn;
+          win_it = it;
+        }
+      }
+    }
+  }
+  // true residual
+  spmv_t<double>(n, avg, A.ia, A.ja, A.a, x, Q[0], s);
+  k_residual<<<g, kThreads, 0, s>>>(n, b, Q[0], r);
+  c.dot<double>(n, r, r, dscal + 10);
+  c.dot<double>(n, b, b, dscal + 11);
+  double h[2] = {0, 0};
+  cudaMemcpyAsync(h, dscal + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (err == cudaSuccess) err = e2;
+  res->iterations = it;
+  res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+  res->converged = !stalled && res->rel_residual <= rtol;
+  cudaFreeAsync(r, s);
+  cudaFreeAsync(z, s);
+  cudaFreeAsync(pqs, s);
+  for (int j = 0; j < mt; j++) {
+    cudaFreeAsync(P[j], s);
+    cudaFreeAsync(Q[j], s);
+  }
+  cudaFreeAsync(bptr, s);
+  cudaFreeAsync(binv, s);
+  cudaFreeAsync(c.part, s);
+  cudaFreeAsync(dscal, s);
+  if (err == cudaSuccess) err = cudaGetLastError();
+  return err;
+}
+
+// ---------------------------------------------------------------------------
 // Allocation-free Jacobi PCG.
 //
 // Some callers cannot let a library allocate device memory during a solve: a

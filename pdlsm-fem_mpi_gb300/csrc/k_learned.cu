@@ -1,0 +1,416 @@
+// Learned two-level preconditioner: kernels.
+//
+// Coarse space: a regular grid over the model's bounding box; fine equation
+// e (node k, DOF i) interpolates DOF i of the 8 (3D) / 4 (2D) corners of the
+// coarse cell around node k with trilinear weights (prolongation P).
+// Residuals are restricted by R = P^T; a fine field is averaged onto the
+// grid by R~ = diag(1 / row sums of P^T) P^T (the training target of an
+// error).
+//
+// Network: y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 with x = R r / |R r|;
+// the coarse correction added to the preconditioned residual is
+// P (|R r| sigma y), sigma a fixed target scale.  Training (forward, backward,
+// Adam) runs with BF16 GEMM operands and FP32 accumulation in the tiled
+// kernels below; inference is one GEMV chain per Krylov iteration.
+// Reductions have a fixed order and there are no atomics, so results are
+// reproducible.
+#include <cuda_bf16.h>
+
+#include <cmath>
+
+#include "learned.h"
+
+namespace pdx {
+
+namespace {
+
+constexpr int kT = 256;
+using bf16 = __nv_bfloat16;
+
+// C[M x N] = alpha op(A)[M x K] op(B)[K x N] + beta C, A and B in BF16, C in FP32:
+// op(A)(m, k) = TA ? A[k lda + m] : A[m lda + k]; op(B)(k, n) = TB ? B[n ldb + k] : B[k ldb + n].
+// 64 x 64 tiles, 16-deep K slices in shared memory, 4 x 4 outputs per thread.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const bf16* __restrict__ A, int lda,
+                                              const bf16* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
+                                              float alpha, float beta) {
+  __shared__ float As[16][65];
+  __shared__ float Bs[16][65];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int e = threadIdx.x; e < 1024; e += 256) {
+      const int mm = TA ? e % 64 : e / 16, kk = TA ? e / 64 : e % 16;
+      const int m = m0 + mm, k = k0 + kk;
+      float val = 0.f;
+      if (m < M && k < K) val = __bfloat162float(TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k]);
+      As[kk][mm] = val;
+    }
+    for (int e = threadIdx.x; e < 1024; e += 256) {
+      const int nn = TB ? e / 16 : e % 64, kk = TB ? e % 16 : e / 64;
+      const int nI = n0 + nn, k = k0 + kk;
+      float val = 0.f;
+      if (nI < N && k < K) val = __bfloat162float(TB ? B[(int64_t)nI * ldb + k] : B[(int64_t)k * ldb + nI]);
+      Bs[kk][nn] = val;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; kk++) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) av[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) bv[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int m = m0 + ty * 4 + i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int nI = n0 + tx * 4 + j;
+      if (nI >= N) continue;
+      float* cp = C + (int64_t)m * ldc + nI;
+      *cp = beta == 0.f ? alpha * acc[i][j] : alpha * acc[i][j] + beta * *cp;
+    }
+  }
+}
+
+template <bool TA, bool TB>
+void gemm(int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, float alpha,
+          float beta, cudaStream_t s) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta);
+}
+
+// Z[m][n] += bias[n]; H = BF16(relu(Z)) (or Z without relu)
+__global__ void k_bias_act(int M, int N, float* Z, const float* bias, bf16* H, int relu) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)M * N) return;
+  const float z = Z[i] + bias[i % N];
+  Z[i] = z;
+  if (H) H[i] = __float2bfloat16(relu ? fmaxf(z, 0.f) : z);
+}
+
+// dY = 2 w_m (Y - T); loss_row[m] = w_m |Y_m - T_m|^2 (one block per row)
+__global__ void k_loss_grad(int M, int N, const float* Y, const float* T, const float* w, float* dY, bf16* dY16,
+                            float* loss_row) {
+  const int m = blockIdx.x;
+  __shared__ float sh[kT];
+  float acc = 0.f;
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    const int64_t i = (int64_t)m * N + n;
+    const float d = Y[i] - T[i];
+    acc += d * d;
+    const float g = 2.f * w[m] * d;
+    dY[i] = g;
+    dY16[i] = __float2bfloat16(g);
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_row[m] = w[m] * sh[0];
+}
+
+// dZ = dH (Z > 0)
+__global__ void k_relu_back(int64_t n, const float* dH, const float* Z, float* dZ, bf16* dZ16) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = Z[i] > 0.f ? dH[i] : 0.f;
+  dZ[i] = g;
+  dZ16[i] = __float2bfloat16(g);
+}
+
+// db[n] = sum_m dZ[m][n] in row order
+__global__ void k_colsum(int M, int N, const float* dZ, float* db) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int m = 0; m < M; m++) s += dZ[(int64_t)m * N + n];
+  db[n] = s;
+}
+
+__global__ void k_sum(int n, const float* x, float* out) {
+  __shared__ float sh[kT];
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+__global__ void k_adam(int64_t n, float* w, const float* g, float* m1, float* m2, float lr, float b1, float b2,
+                       float eps, float c1, float c2, bf16* w16) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float a = b1 * m1[i] + (1.f - b1) * gi;
+  const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+  m1[i] = a;
+  m2[i] = b;
+  const float wi = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+  w[i] = wi;
+  if (w16) w16[i] = __float2bfloat16(wi);
+}
+
+__global__ void k_to_bf16(int64_t n, const float* x, bf16* y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16(x[i]);
+}
+
+// coarse[c] = sum_j w_j r[e_j] over restriction row c (FP64 accumulation)
+__global__ void k_restrict(int nc, const int* rptr, const int* ridx, const float* rw, const double* r, float* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double s = 0.0;
+  for (int j = rptr[c]; j < rptr[c + 1]; j++) s += (double)rw[j] * r[ridx[j]];
+  out[c] = (float)s;
+}
+
+// z[e] += scale sum_j P_ej c[j]
+template <int NP>
+__global__ void k_prolong_add(int64_t n, const int* pidx, const float* pw, const float* c, const float* scale,
+                              double* z) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < NP; j++) {
+    const int ci = pidx[e * NP + j];
+    if (ci >= 0) s += pw[e * NP + j] * c[ci];
+  }
+  z[e] += (double)(*scale) * (double)s;
+}
+
+// one block: x16 = BF16(x / |x|), *scale_out = |x| sigma
+__global__ void k_normalize(int n, const float* x, bf16* x16, float sigma, float* scale_out) {
+  __shared__ float sh[kT];
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i] * x[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  const float nrm = sqrtf(sh[0]);
+  const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x16[i] = __float2bfloat16(x[i] * inv);
+  if (threadIdx.x == 0) *scale_out = nrm * sigma;
+}
+
+// inference layer (batch 1): h[row] = act(W[row] . x + b[row]), one warp per row
+__global__ void k_gemv_rows(int rows, int cols, const bf16* W, const bf16* x, const float* b, int relu, bf16* h16,
+                            float* hf) {
+  const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= rows) return;
+  float s = 0.f;
+  const bf16* w = W + (int64_t)row * cols;
+  for (int k = lane; k < cols; k += 32) s = fmaf(__bfloat162float(w[k]), __bfloat162float(x[k]), s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const float z = s + b[row];
+    const float a = relu ? fmaxf(z, 0.f) : z;
+    if (h16) h16[row] = __float2bfloat16(a);
+    if (hf) hf[row] = a;
+  }
+}
+
+// S[j] = ax - S[j] for samples j in [first, last): iterate averages -> error averages
+__global__ void k_err(int first, int last, int nc, const float* ax, float* S) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n = (int64_t)(last - first) * nc;
+  if (i >= n) return;
+  const int64_t j = (int64_t)first * nc + i;
+  S[j] = ax[i % nc] - S[j];
+}
+
+// norms[j] = |S_j| (one block per sample)
+__global__ void k_rownorm(int nc, const float* S, float* norms) {
+  __shared__ float sh[kT];
+  const float* x = S + (int64_t)blockIdx.x * nc;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) s += x[i] * x[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) norms[blockIdx.x] = sqrtf(sh[0]);
+}
+
+// batch row m from sample idx[m]: X = S_r / |S_r| (BF16), T = S_e / (|S_r| sigma), W = 1 / (|T|^2 B)
+__global__ void k_stage(int B, int nc, const int* idx, const float* S_r, const float* S_e, const float* norms,
+                        float sigma, bf16* X, float* T, float* W) {
+  __shared__ float sh[kT];
+  const int m = blockIdx.x;
+  const int j = idx[m];
+  const float nr = norms[j];
+  const float inv = nr > 0.f ? 1.f / nr : 0.f;
+  const float tinv = inv / sigma;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    X[(int64_t)m * nc + i] = __float2bfloat16(S_r[(int64_t)j * nc + i] * inv);
+    const float t = S_e[(int64_t)j * nc + i] * tinv;
+    T[(int64_t)m * nc + i] = t;
+    s += t * t;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) W[m] = sh[0] > 0.f ? 1.f / (sh[0] * (float)B) : 0.f;
+}
+
+__global__ void k_stage_raw(int64_t n, const float* Xf, bf16* X) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) X[i] = __float2bfloat16(Xf[i]);
+}
+
+int grid_of(int64_t n) { return (int)((n + kT - 1) / kT); }
+
+}  // namespace
+
+// ----------------------------------------------------------------- MLP ----
+
+void Mlp::param_views(float* base, float** W1, float** b1, float** W2, float** b2, float** W3, float** b3) const {
+  float* p = base;
+  *W1 = p; p += (size_t)H * nin;
+  *b1 = p; p += H;
+  *W2 = p; p += (size_t)H * H;
+  *b2 = p; p += H;
+  *W3 = p; p += (size_t)nout * H;
+  *b3 = p;
+}
+
+cudaError_t Mlp::forward_backward(int B, const bf16* X, const float* T, const float* wrow, bool grads,
+                                  cudaStream_t s) {
+  float *W1, *b1, *W2, *b2, *W3, *b3;
+  param_views(w, &W1, &b1, &W2, &b2, &W3, &b3);
+  const bf16* W1h = w16;
+  const bf16* W2h = W1h + (size_t)H * nin + H;
+  const bf16* W3h = W2h + (size_t)H * H + H;
+  const int g1 = grid_of((int64_t)B * H), g3 = grid_of((int64_t)B * nout);
+  gemm<false, true>(B, H, nin, X, nin, W1h, nin, Z1, H, 1.f, 0.f, s);
+  k_bias_act<<<g1, kT, 0, s>>>(B, H, Z1, b1, H1, 1);
+  gemm<false, true>(B, H, H, H1, H, W2h, H, Z2, H, 1.f, 0.f, s);
+  k_bias_act<<<g1, kT, 0, s>>>(B, H, Z2, b2, H2, 1);
+  gemm<false, true>(B, nout, H, H2, H, W3h, H, Y, nout, 1.f, 0.f, s);
+  k_bias_act<<<g3, kT, 0, s>>>(B, nout, Y, b3, nullptr, 0);
+  if (!T) return cudaGetLastError();
+  k_loss_grad<<<B, kT, 0, s>>>(B, nout, Y, T, wrow, dY, dY16, loss_row);
+  k_sum<<<1, kT, 0, s>>>(B, loss_row, loss);
+  if (!grads) return cudaGetLastError();
+  float *gW1, *gb1, *gW2, *gb2, *gW3, *gb3;
+  param_views(g, &gW1, &gb1, &gW2, &gb2, &gW3, &gb3);
+  // layer 3: gW3 = dY^T H2, gb3 = sum dY, dH2 = dY W3
+  gemm<true, false>(nout, H, B, dY16, nout, H2, H, gW3, H, 1.f, 0.f, s);
+  k_colsum<<<grid_of(nout), kT, 0, s>>>(B, nout, dY, gb3);
+  gemm<false, false>(B, H, nout, dY16, nout, W3h, H, dH, H, 1.f, 0.f, s);
+  k_relu_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z2, dZ, dZ16);
+  // layer 2
+  gemm<true, false>(H, H, B, dZ16, H, H1, H, gW2, H, 1.f, 0.f, s);
+  k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb2);
+  gemm<false, false>(B, H, H, dZ16, H, W2h, H, dH, H, 1.f, 0.f, s);
+  k_relu_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z1, dZ, dZ16);
+  // layer 1
+  gemm<true, false>(H, nin, B, dZ16, H, X, nin, gW1, nin, 1.f, 0.f, s);
+  k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb1);
+  return cudaGetLastError();
+}
+
+cudaError_t Mlp::adam_step(float lr, cudaStream_t s) {
+  step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+  const int64_t n = n_params();
+  k_adam<<<grid_of(n), kT, 0, s>>>(n, w, g, m1, m2, lr, b1, b2, 1e-8f, c1, c2, w16);
+  return cudaGetLastError();
+}
+
+cudaError_t Mlp::sync_bf16(cudaStream_t s) {
+  const int64_t n = n_params();
+  k_to_bf16<<<grid_of(n), kT, 0, s>>>(n, w, w16);
+  return cudaGetLastError();
+}
+
+cudaError_t Mlp::infer(const bf16* x16, float* y, cudaStream_t s) {
+  float *W1, *b1, *W2, *b2, *W3, *b3;
+  param_views(w, &W1, &b1, &W2, &b2, &W3, &b3);
+  const bf16* W1h = w16;
+  const bf16* W2h = W1h + (size_t)H * nin + H;
+  const bf16* W3h = W2h + (size_t)H * H + H;
+  k_gemv_rows<<<(H + 7) / 8, 256, 0, s>>>(H, nin, W1h, x16, b1, 1, H1, nullptr);
+  k_gemv_rows<<<(H + 7) / 8, 256, 0, s>>>(H, H, W2h, H1, b2, 1, H2, nullptr);
+  k_gemv_rows<<<(nout + 7) / 8, 256, 0, s>>>(nout, H, W3h, H2, b3, 0, nullptr, y);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ transfer, data ----
+
+cudaError_t coarse_restrict(const CoarseSpace& cs, bool average, const double* r, float* out, cudaStream_t s) {
+  k_restrict<<<grid_of(cs.nc), kT, 0, s>>>(cs.nc, cs.rptr, cs.ridx, average ? cs.aw : cs.rw, r, out);
+  return cudaGetLastError();
+}
+
+cudaError_t coarse_prolong_add(const CoarseSpace& cs, const float* c, const float* scale, double* z,
+                               cudaStream_t s) {
+  if (cs.np == 8) k_prolong_add<8><<<grid_of(cs.n), kT, 0, s>>>(cs.n, cs.pidx, cs.pw, c, scale, z);
+  else k_prolong_add<4><<<grid_of(cs.n), kT, 0, s>>>(cs.n, cs.pidx, cs.pw, c, scale, z);
+  return cudaGetLastError();
+}
+
+cudaError_t coarse_normalize(int n, const float* x, bf16* x16, float sigma, float* scale, cudaStream_t s) {
+  k_normalize<<<1, kT, 0, s>>>(n, x, x16, sigma, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t learned_err(int first, int last, int nc, const float* ax, float* S, cudaStream_t s) {
+  const int64_t n = (int64_t)(last - first) * nc;
+  if (n <= 0) return cudaSuccess;
+  k_err<<<grid_of(n), kT, 0, s>>>(first, last, nc, ax, S);
+  return cudaGetLastError();
+}
+
+cudaError_t learned_norms(int count, int nc, const float* S, float* norms, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  k_rownorm<<<count, kT, 0, s>>>(nc, S, norms);
+  return cudaGetLastError();
+}
+
+cudaError_t learned_stage(int B, int nc, const int* idx, const float* S_r, const float* S_e, const float* norms,
+                          float sigma, bf16* X, float* T, float* W, cudaStream_t s) {
+  k_stage<<<B, kT, 0, s>>>(B, nc, idx, S_r, S_e, norms, sigma, X, T, W);
+  return cudaGetLastError();
+}
+
+cudaError_t learned_stage_raw(int B, int nc, const float* Xf, bf16* X, cudaStream_t s) {
+  const int64_t n = (int64_t)B * nc;
+  k_stage_raw<<<grid_of(n), kT, 0, s>>>(n, Xf, X);
+  return cudaGetLastError();
+}
+
+}  // namespace pdx

@@ -1,0 +1,435 @@
+// Learned two-level preconditioner (host side) and step-by-step implicit
+// Newmark dynamics.
+//
+// The Newmark step restates pdfemDynamicNewmarkSolver_CSRformat
+// (pdsolve.cpp:6092-6290): predictor, K_N = beta dt^2 K + M assembled through
+// the scatter map (pdfemAssembleKNFR_CSRformat :6327-6397), K_N a_{n+1} = F,
+// update of displacement and velocity (updateDispVelo :6399-6422).  The
+// reference factorises K_N with PARDISO at every step; here the solve is a
+// Krylov method chosen per call:
+//   0-3  the methods of krylov_solve (Jacobi PCG, block-Jacobi PCG, BiCGStab,
+//        mixed PCG + FP64 refinement)
+//   4    block-Jacobi flexible CG: the plain method the learned one is judged by
+//   5    flexible CG with block-Jacobi plus the learned coarse correction; if
+//        it stalls, block-Jacobi flexible CG and then BiCGStab take over from
+//        the current iterate.
+// With `collect`, a method-4 solve stores one training pair per iteration:
+// the restricted residual P^T r_j and the coarse average of the error
+// x* - x_j, known once the solve has converged (the solver generates its own
+// training data).
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <random>
+
+#include "learned.h"
+
+namespace pdx {
+
+namespace {
+
+// directions kept for A-orthogonalisation with the nonlinear learned preconditioner
+constexpr int kLearnedTrunc = 8;
+
+struct Collector : IterHook {
+  Learned* L = nullptr;
+  cudaError_t on_iter(int, const double* x, const double* r, const double*, cudaStream_t s) override {
+    if (L->count >= L->cap) return cudaSuccess;
+    const int64_t o = (int64_t)L->count * L->cs.nc;
+    cudaError_t e = coarse_restrict(L->cs, false, r, L->S_r + o, s);
+    if (e == cudaSuccess) e = coarse_restrict(L->cs, true, x, L->S_x + o, s);
+    L->count++;
+    return e;
+  }
+};
+
+// Coarse grid over the bounding box of the nodes; every fine equation gets
+// the trilinear (bilinear in 2D) weights of the corners of its node's cell.
+void build_coarse(const pdx_model* m, const int cells_in[3], std::vector<int>& pidx, std::vector<float>& pw,
+                  std::vector<int>& rptr, std::vector<int>& ridx, std::vector<float>& rw, std::vector<float>& aw,
+                  int& nc, int& np, int cells[3]) {
+  const int D = m->mesh.dim, N = m->mesh.n_node;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int k = 0; k < N; k++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::min(lo[a], m->mesh.X[(size_t)k * 3 + a]);
+      hi[a] = std::max(hi[a], m->mesh.X[(size_t)k * 3 + a]);
+    }
+  for (int a = 0; a < 3; a++) cells[a] = a < D ? std::max(1, cells_in[a]) : 0;
+  const int nxn = cells[0] + 1, nyn = cells[1] + 1, nzn = D == 3 ? cells[2] + 1 : 1;
+  nc = nxn * nyn * nzn * D;
+  np = D == 3 ? 8 : 4;
+  const int64_t n = m->setup.n_eq;
+  pidx.assign((size_t)n * np, -1);
+  pw.assign((size_t)n * np, 0.f);
+  for (int k = 0; k < N; k++) {
+    int ci[3] = {0, 0, 0};
+    double t[3] = {0, 0, 0};
+    for (int a = 0; a < D; a++) {
+      const double len = hi[a] - lo[a];
+      const double u = len > 0 ? (m->mesh.X[(size_t)k * 3 + a] - lo[a]) / len * cells[a] : 0.0;
+      const int c = std::min(std::max((int)std::floor(u), 0), cells[a] - 1);
+      ci[a] = c;
+      t[a] = std::min(std::max(u - c, 0.0), 1.0);
+    }
+    for (int i = 0; i < D; i++) {
+      const int e = m->setup.eq[(size_t)k * D + i];
+      if (e < 0) continue;
+      for (int corner = 0; corner < np; corner++) {
+        const int dx = corner & 1, dy = (corner >> 1) & 1, dz = (corner >> 2) & 1;
+        double w = (dx ? t[0] : 1 - t[0]) * (dy ? t[1] : 1 - t[1]);
+        if (D == 3) w *= dz ? t[2] : 1 - t[2];
+        const int node = (ci[0] + dx) + nxn * ((ci[1] + dy) + nyn * (D == 3 ? ci[2] + dz : 0));
+        pidx[(size_t)e * np + corner] = node * D + i;
+        pw[(size_t)e * np + corner] = (float)w;
+      }
+    }
+  }
+  // transpose: restriction rows per coarse DOF, fine equations in order
+  rptr.assign(nc + 1, 0);
+  for (size_t j = 0; j < pidx.size(); j++)
+    if (pidx[j] >= 0 && pw[j] != 0.f) rptr[pidx[j] + 1]++;
+  for (int c = 0; c < nc; c++) rptr[c + 1] += rptr[c];
+  ridx.assign(rptr[nc], 0);
+  rw.assign(rptr[nc], 0.f);
+  std::vector<int> fill(rptr.begin(), rptr.end() - 1);
+  for (int64_t e = 0; e < n; e++)
+    for (int j = 0; j < np; j++) {
+      const int c = pidx[(size_t)e * np + j];
+      if (c < 0 || pw[(size_t)e * np + j] == 0.f) continue;
+      ridx[fill[c]] = (int)e;
+      rw[fill[c]++] = pw[(size_t)e * np + j];
+    }
+  aw.assign(rw.size(), 0.f);
+  for (int c = 0; c < nc; c++) {
+    double s = 0;
+    for (int j = rptr[c]; j < rptr[c + 1]; j++) s += rw[j];
+    for (int j = rptr[c]; j < rptr[c + 1]; j++) aw[j] = s > 0 ? (float)(rw[j] / s) : 0.f;
+  }
+}
+
+template <typename T>
+T* dev_upload(DevBuf& b, const std::vector<T>& h, cudaStream_t s) {
+  T* d = b.alloc<T>(h.size());
+  if (d && !h.empty()) cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+  return d;
+}
+
+pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* x, KrylovResult* kr) {
+  DevCsr A;
+  A.n = m->setup.n_eq;
+  A.nnz = (int64_t)m->setup.csr_ja.size();
+  A.ia = m->d_ia;
+  A.ja = m->d_ja;
+  A.a = m->d_Kval;
+  const double* b = m->d_tmp_eq[0];
+  const double tol = m->cmd.solve_tol;
+  const int maxit = m->cmd.solve_maxit;
+  const int bd = m->mesh.dim;
+  Learned* L = m->learned;
+  if (method <= 3) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
+  if (method == 4) {
+    Collector col;
+    const bool take = collect && L;
+    if (take) {
+      col.L = L;
+      col.every = 1;
+      L->solve_first = L->count;
+    }
+    pdx_status st = cuda_check(
+        krylov_fcg(A, b, x, tol, maxit, bd, nullptr, take ? &col : nullptr, 0, 1, m->stream, kr), "flexible CG");
+    if (st) return st;
+    if (take && kr->converged) {
+      st = cuda_check(coarse_restrict(L->cs, true, x, L->ax, m->stream), "restriction");
+      if (!st) st = cuda_check(learned_err(L->solve_first, L->count, L->cs.nc, L->ax, L->S_x, m->stream), "errors");
+      return st;
+    }
+    if (take) L->count = L->solve_first;   // drop the pairs of a solve that did not converge
+    return PDX_OK;
+  }
+  if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
+  pdx_status st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, 200, kLearnedTrunc, m->stream, kr),
+                             "learned flexible CG");
+  if (st || kr->converged) return st;
+  const int its = kr->iterations;
+  st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, nullptr, nullptr, 400, 1, m->stream, kr), "flexible CG");
+  kr->iterations += its;
+  if (st || kr->converged) return st;
+  const int its2 = kr->iterations;
+  st = cuda_check(krylov_solve(A, b, x, 2, tol, maxit, bd, m->stream, kr), "BiCGStab");
+  kr->iterations += its2;
+  return st;
+}
+
+}  // namespace
+
+void learned_destroy(pdx_model* m) {
+  if (!m->learned) return;
+  m->learned->buf.free_all();
+  delete m->learned;
+  m->learned = nullptr;
+}
+
+cudaError_t Learned::add(const double* r, double* z, cudaStream_t s) {
+  cudaError_t e = coarse_restrict(cs, false, r, rc, s);
+  if (e == cudaSuccess) e = coarse_normalize(cs.nc, rc, x16, sigma, scale, s);
+  if (e == cudaSuccess) e = net.infer(x16, y, s);
+  if (e == cudaSuccess) e = coarse_prolong_add(cs, y, scale, z, s);
+  return e;
+}
+
+}  // namespace pdx
+
+using namespace pdx;
+
+#define NEED_DEV(m)                                                                      \
+  do {                                                                                   \
+    if (!(m)) return set_error(PDX_ERR_INVALID, "null model");                           \
+    if (!(m)->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device"); \
+    cudaSetDevice((m)->device);                                                          \
+  } while (0)
+
+extern "C" {
+
+pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, uint64_t seed, int max_samples) {
+  NEED_DEV(m);
+  if (hidden <= 0 || max_samples <= 0) return set_error(PDX_ERR_INVALID, "hidden width and sample count must be > 0");
+  learned_destroy(m);
+  Learned* L = new Learned();
+  m->learned = L;
+  cudaStream_t s = m->stream;
+  std::vector<int> pidx, rptr, ridx;
+  std::vector<float> pw, rw, aw;
+  const int cin[3] = {cx, cy, cz};
+  int nc = 0, np = 0;
+  build_coarse(m, cin, pidx, pw, rptr, ridx, rw, aw, nc, np, L->cs.cells);
+  CoarseSpace& cs = L->cs;
+  cs.dim = m->mesh.dim;
+  cs.nc = nc;
+  cs.n = m->setup.n_eq;
+  cs.np = np;
+  cs.pidx = dev_upload(L->buf, pidx, s);
+  cs.pw = dev_upload(L->buf, pw, s);
+  cs.rptr = dev_upload(L->buf, rptr, s);
+  cs.ridx = dev_upload(L->buf, ridx, s);
+  cs.rw = dev_upload(L->buf, rw, s);
+  cs.aw = dev_upload(L->buf, aw, s);
+  // network: Xavier-uniform weights from the seed, zero biases
+  Mlp& net = L->net;
+  net.nin = nc;
+  net.nout = nc;
+  net.H = hidden;
+  net.Bmax = 64;
+  const int64_t npar = net.n_params();
+  std::vector<float> w0((size_t)npar, 0.f);
+  {
+    std::mt19937_64 rng(seed);
+    float *W1, *b1, *W2, *b2, *W3, *b3;
+    net.param_views(w0.data(), &W1, &b1, &W2, &b2, &W3, &b3);
+    auto fill = [&](float* p, int rows, int cols) {
+      const float a = std::sqrt(6.f / (float)(rows + cols));
+      std::uniform_real_distribution<float> u(-a, a);
+      for (int64_t i = 0; i < (int64_t)rows * cols; i++) p[i] = u(rng);
+    };
+    fill(W1, hidden, nc);
+    fill(W2, hidden, hidden);
+    fill(W3, nc, hidden);
+  }
+  net.w = dev_upload(L->buf, w0, s);
+  net.w16 = L->buf.alloc<__nv_bfloat16>(npar);
+  net.g = L->buf.alloc<float>(npar);
+  net.m1 = L->buf.alloc<float>(npar);
+  net.m2 = L->buf.alloc<float>(npar);
+  const int B = net.Bmax;
+  net.Z1 = L->buf.alloc<float>((size_t)B * hidden);
+  net.Z2 = L->buf.alloc<float>((size_t)B * hidden);
+  net.Y = L->buf.alloc<float>((size_t)B * nc);
+  net.dY = L->buf.alloc<float>((size_t)B * nc);
+  net.dH = L->buf.alloc<float>((size_t)B * hidden);
+  net.dZ = L->buf.alloc<float>((size_t)B * hidden);
+  net.H1 = L->buf.alloc<__nv_bfloat16>((size_t)B * hidden);
+  net.H2 = L->buf.alloc<__nv_bfloat16>((size_t)B * hidden);
+  net.dY16 = L->buf.alloc<__nv_bfloat16>((size_t)B * nc);
+  net.dZ16 = L->buf.alloc<__nv_bfloat16>((size_t)B * hidden);
+  net.loss_row = L->buf.alloc<float>(B);
+  net.loss = L->buf.alloc<float>(1);
+  L->rc = L->buf.alloc<float>(nc);
+  L->x16 = L->buf.alloc<__nv_bfloat16>(nc);
+  L->y = L->buf.alloc<float>(nc);
+  L->scale = L->buf.alloc<float>(1);
+  L->ax = L->buf.alloc<float>(nc);
+  L->cap = max_samples;
+  L->S_r = L->buf.alloc<float>((size_t)max_samples * nc);
+  L->S_x = L->buf.alloc<float>((size_t)max_samples * nc);
+  L->S_scale = L->buf.alloc<float>(max_samples);
+  L->bidx = L->buf.alloc<int>(B);
+  L->Xb = L->buf.alloc<__nv_bfloat16>((size_t)B * nc);
+  L->Tb = L->buf.alloc<float>((size_t)B * nc);
+  L->Wb = L->buf.alloc<float>(B);
+  for (void* p : L->buf.ptrs)
+    if (!p) return set_error(PDX_ERR_CUDA, "device allocation failed (learned preconditioner)");
+  cudaMemsetAsync(net.m1, 0, npar * 4, s);
+  cudaMemsetAsync(net.m2, 0, npar * 4, s);
+  pdx_status st = cuda_check(net.sync_bf16(s), "network set-up");
+  if (st) return st;
+  return cuda_check(cudaStreamSynchronize(s), "learned set-up");
+}
+
+int64_t pdx_learned_samples(const pdx_model* m) { return m && m->learned ? m->learned->count : 0; }
+
+pdx_status pdx_learned_train(pdx_model* m, int epochs, float lr, uint64_t seed, float* final_loss) {
+  NEED_DEV(m);
+  Learned* L = m->learned;
+  if (!L) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  if (L->count < 2) return set_error(PDX_ERR_INVALID, "not enough training pairs collected");
+  cudaStream_t s = m->stream;
+  const int nc = L->cs.nc, n = L->count, B = L->net.Bmax;
+  // per-sample |P^T r| and the target scale sigma = median |e_c| / |P^T r|
+  pdx_status st = cuda_check(learned_norms(n, nc, L->S_r, L->S_scale, s), "norms");
+  if (st) return st;
+  std::vector<float> nr(n), ne(n);
+  float* tmp = nullptr;
+  cudaMallocAsync(&tmp, n * sizeof(float), s);
+  learned_norms(n, nc, L->S_x, tmp, s);
+  cudaMemcpyAsync(nr.data(), L->S_scale, n * 4, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(ne.data(), tmp, n * 4, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(tmp, s);
+  st = cuda_check(cudaStreamSynchronize(s), "norms");
+  if (st) return st;
+  std::vector<float> ratio;
+  for (int j = 0; j < n; j++)
+    if (nr[j] > 0 && ne[j] > 0) ratio.push_back(ne[j] / nr[j]);
+  if (ratio.empty()) return set_error(PDX_ERR_NUMERIC, "training pairs are all zero");
+  std::nth_element(ratio.begin(), ratio.begin() + ratio.size() / 2, ratio.end());
+  L->sigma = ratio[ratio.size() / 2];
+  std::mt19937_64 rng(seed);
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  float last = 0.f;
+  for (int ep = 0; ep < epochs; ep++) {
+    std::shuffle(order.begin(), order.end(), rng);
+    double sum = 0;
+    int nbatch = 0;
+    for (int i0 = 0; i0 + 1 < n; i0 += B) {
+      const int b = std::min(B, n - i0);
+      cudaMemcpyAsync(L->bidx, order.data() + i0, b * sizeof(int), cudaMemcpyHostToDevice, s);
+      st = cuda_check(learned_stage(b, nc, L->bidx, L->S_r, L->S_x, L->S_scale, L->sigma, L->Xb, L->Tb, L->Wb, s),
+                      "stage");
+      if (!st) st = cuda_check(L->net.forward_backward(b, L->Xb, L->Tb, L->Wb, true, s), "forward/backward");
+      if (!st) st = cuda_check(L->net.adam_step(lr, s), "Adam");
+      if (st) return st;
+      float h = 0;
+      cudaMemcpyAsync(&h, L->net.loss, 4, cudaMemcpyDeviceToHost, s);
+      st = cuda_check(cudaStreamSynchronize(s), "training");
+      if (st) return st;
+      sum += h;
+      nbatch++;
+    }
+    last = nbatch ? (float)(sum / nbatch) : 0.f;
+  }
+  L->trained = true;
+  if (final_loss) *final_loss = last;
+  return PDX_OK;
+}
+
+pdx_status pdx_mlp_params(pdx_model* m, float* get, const float* set, int64_t* count) {
+  NEED_DEV(m);
+  Learned* L = m->learned;
+  if (!L) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  const int64_t npar = L->net.n_params();
+  if (count) *count = npar;
+  if (set) {
+    cudaMemcpyAsync(L->net.w, set, npar * 4, cudaMemcpyHostToDevice, m->stream);
+    L->net.sync_bf16(m->stream);
+  }
+  if (get) cudaMemcpyAsync(get, L->net.w, npar * 4, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "parameters");
+}
+
+pdx_status pdx_mlp_loss_grad(pdx_model* m, int batch, const float* x, const float* t, const float* w, float* loss,
+                             float* grad) {
+  NEED_DEV(m);
+  Learned* L = m->learned;
+  if (!L) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  if (batch <= 0 || batch > L->net.Bmax || !x || !t || !w) return set_error(PDX_ERR_INVALID, "bad batch");
+  cudaStream_t s = m->stream;
+  const int nc = L->cs.nc;
+  float* xf = nullptr;
+  cudaMallocAsync(&xf, (size_t)batch * nc * 4, s);
+  cudaMemcpyAsync(xf, x, (size_t)batch * nc * 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(L->Tb, t, (size_t)batch * nc * 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(L->Wb, w, (size_t)batch * 4, cudaMemcpyHostToDevice, s);
+  learned_stage_raw(batch, nc, xf, L->Xb, s);
+  cudaFreeAsync(xf, s);
+  pdx_status st = cuda_check(L->net.forward_backward(batch, L->Xb, L->Tb, L->Wb, true, s), "forward/backward");
+  if (st) return st;
+  if (loss) cudaMemcpyAsync(loss, L->net.loss, 4, cudaMemcpyDeviceToHost, s);
+  if (grad) cudaMemcpyAsync(grad, L->net.g, L->net.n_params() * 4, cudaMemcpyDeviceToHost, s);
+  return cuda_check(cudaStreamSynchronize(s), "loss/gradient");
+}
+
+pdx_status pdx_newmark_init(pdx_model* m) {
+  NEED_DEV(m);
+  if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "batched models run explicit dynamics only");
+  pdx_status st = pdx_explicit_init(m);
+  if (st) return st;
+  const size_t ne = (size_t)std::max(m->setup.n_eq, 1);
+  if (!m->d_vel) m->d_vel = m->buf.alloc<double>(ne);
+  if (!m->d_acc) m->d_acc = m->buf.alloc<double>(ne);
+  if (!m->d_vel || !m->d_acc) return set_error(PDX_ERR_CUDA, "device allocation failed");
+  cudaMemsetAsync(m->d_vel, 0, ne * 8, m->stream);
+  cudaMemsetAsync(m->d_acc, 0, ne * 8, m->stream);
+  m->cur = 0;
+  m->steps_done = 0;
+  m->newmark_ready = true;
+  return cuda_check(cudaStreamSynchronize(m->stream), "Newmark init");
+}
+
+pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_info* info) {
+  NEED_DEV(m);
+  if (!m->newmark_ready) return set_error(PDX_ERR_INVALID, "pdx_newmark_init first");
+  if (method < 0 || method > 5) return set_error(PDX_ERR_INVALID, "method must be 0..5");
+  const int ne = m->setup.n_eq;
+  double* u_all = m->d_u[0];
+  double* upred = m->d_u[1];
+  double* acc1 = m->d_tmp_eq[3];
+  double* ueq = m->d_tmp_eq[4];
+  const int n = (int)m->steps_done + 1;
+  pdx_status st = cuda_check(launch_newmark_predict(m->view, u_all, m->d_vel, m->d_acc, m->cmd.dt, m->cmd.beta,
+                                                    upred, m->stream), "Newmark predictor");
+  if (st) return st;
+  st = assemble_device(m, 3, upred, n - 1);
+  if (st) return st;
+  cudaMemcpyAsync(acc1, m->d_acc, (size_t)ne * 8, cudaMemcpyDeviceToDevice, m->stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, m->stream);
+  KrylovResult kr;
+  st = solve_newmark_system(m, method, collect != 0, acc1, &kr);
+  cudaEventRecord(e1, m->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (info) {
+    info->iterations = kr.iterations;
+    info->rel_residual = kr.rel_residual;
+    info->seconds = ms * 1e-3;
+    info->converged = kr.converged;
+  }
+  if (!kr.converged)
+    return set_error(PDX_ERR_NOCONV, "Newmark solve stopped at relative residual " + std::to_string(kr.rel_residual));
+  launch_gather_eq(m->view, u_all, ueq, m->stream);
+  launch_newmark_update(ne, m->d_vel, m->d_acc, acc1, m->cmd.dt, m->cmd.beta, m->cmd.gamma, ueq, m->d_vel,
+                        m->stream);
+  launch_scatter_eq(m->view, ueq, u_all, m->stream);
+  launch_advance_prescribed(m->view, u_all, m->stream);
+  cudaMemcpyAsync(m->d_acc, acc1, (size_t)ne * 8, cudaMemcpyDeviceToDevice, m->stream);
+  m->steps_done = n;
+  return cuda_check(cudaStreamSynchronize(m->stream), "Newmark step");
+}
+
+}  // extern "C"

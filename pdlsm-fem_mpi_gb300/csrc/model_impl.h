@@ -91,6 +91,8 @@ struct DevBuf {
   }
 };
 
+struct Learned;
+
 }  // namespace pdx
 
 struct pdx_model {
@@ -141,6 +143,11 @@ struct pdx_model {
   std::vector<int> node_mat;         // specimen of each node
   int* d_node_mat = nullptr;
   double* d_mat_nu = nullptr;
+  // implicit Newmark state (pdx_newmark_*) and the learned preconditioner
+  double* d_vel = nullptr;
+  double* d_acc = nullptr;
+  bool newmark_ready = false;
+  pdx::Learned* learned = nullptr;
   int cur = 0;                       // index of the buffer holding u_n
   int64_t steps_done = 0;
   cudaGraphExec_t graph = nullptr;
@@ -158,4 +165,5 @@ pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nb
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);
 bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& err);
+void learned_destroy(pdx_model* m);
 }  // namespace pdx

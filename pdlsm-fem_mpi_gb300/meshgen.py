@@ -374,6 +374,50 @@ def config_c4(n_spec: int = 256, seed: int = 0, nsteps: int = 2000, precision: s
     return out
 
 
+def penny_crack_box(nx: int = 201, ny: int = 101, nz: int = 41, h: float = 1e-3, radius_h: float = 10.0,
+                    tilt_deg: float = 30.0, n_tri: int = 16, pd_frac: float = 0.05, title: str = "pennyBox") -> Mesh:
+    """Hex8 box with an inclined penny crack (a fan of n_tri triangles, radius radius_h * h) at its centre,
+    tilted by tilt_deg about the y axis, and a PD zone of the elements closest to the crack disk
+    (pd_frac of all elements).  The crack centre sits at an element centre, so no node lies on it."""
+    c = np.array([(nx - 1) * h / 2 + 0.5 * h, (ny - 1) * h / 2 + 0.5 * h, (nz - 1) * h / 2 + 0.5 * h])
+    t = np.radians(tilt_deg)
+    nrm = np.array([np.sin(t), 0.0, np.cos(t)])
+    a1 = np.array([np.cos(t), 0.0, -np.sin(t)])
+    a2 = np.array([0.0, 1.0, 0.0])
+    r = radius_h * h
+    th = np.linspace(0.0, 2 * np.pi, n_tri + 1)
+    rim = [c + r * (np.cos(q) * a1 + np.sin(q) * a2) for q in th]
+    cracks = [np.array([c, rim[j], rim[j + 1]]) for j in range(n_tri)]
+
+    def disk_distance(p):
+        d = p - c
+        z = d @ nrm
+        inplane = d - np.outer(z, nrm)
+        rho = np.linalg.norm(inplane, axis=1)
+        return np.hypot(z, np.maximum(rho - r, 0.0))
+
+    n_el = (nx - 1) * (ny - 1) * (nz - 1)
+    _, _, centers = grid3d(nx, ny, nz, h)
+    dist = disk_distance(centers)
+    k = min(n_el - 1, int(pd_frac * n_el))
+    cut = np.partition(dist, k)[k]
+
+    def pd_mask(cent):
+        return disk_distance(cent) <= cut
+
+    return box3d(nx, ny, nz, h, pd_mask=pd_mask, cracks=cracks, title=title)
+
+
+def config_c5(nx: int = 201, ny: int = 101, nz: int = 41, nsteps: int = 200, dt_factor: float = 20.0,
+              radius_h: float = 10.0, n_tri: int = 16):
+    """3D implicit Newmark (beta 0.25, gamma 0.5): 200x100x40 Hex8 box, 5 % PD zone around an inclined penny
+    crack of radius 10 h, x faces pulled at 0.1 m/s.  dt = dt_factor x 0.8 x the explicit stable step (the C2
+    estimate at h = 1 mm): an implicit step much longer than an explicit one, so that K dominates K_N."""
+    mesh = penny_crack_box(nx=nx, ny=ny, nz=nz, h=1e-3, radius_h=radius_h, n_tri=n_tri, title="pennyBoxC5")
+    return mesh, dict(solver="DYNAMIC", dt=dt_factor * 0.8 * 1.69e-7, nsteps=nsteps, save=max(1, nsteps),
+                      factor=3.015, nlf=1.0, newmark=(0.5, 0.25), precision="FP64")
+
+
 CONFIGS = {"c1": config_c1, "c2": config_c2}
 
 

@@ -53,7 +53,8 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_internal_force", "pdx_explicit_init", "pdx_explicit_advance", "pdx_explicit_advance_timed",
             "pdx_explicit_step_host", "pdx_explicit_step_count", "pdx_get_state", "pdx_assemble_csr",
             "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc", "pdx_batch_create", "pdx_batch_size",
-            "pdx_batch_offsets"]
+            "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
+            "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -91,6 +92,17 @@ def lib() -> C.CDLL:
     L.pdx_run.argtypes = [_P, C.c_char_p]
     L.pdx_pcg_solve_noalloc.argtypes = [C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts), _P,
                                         C.POINTER(SolveInfo)]
+    _F = C.POINTER(C.c_float)
+    for name, args in (("pdx_newmark_init", [_P]),
+                       ("pdx_newmark_step", [_P, C.c_int, C.c_int, C.POINTER(SolveInfo)]),
+                       ("pdx_learned_setup", [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int]),
+                       ("pdx_learned_train", [_P, C.c_int, C.c_float, C.c_uint64, _F]),
+                       ("pdx_mlp_params", [_P, _F, _F, C.POINTER(C.c_int64)]),
+                       ("pdx_mlp_loss_grad", [_P, C.c_int, _F, _F, _F, _F, _F])):
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = C.c_int
+    L.pdx_learned_samples.argtypes = [_P]
+    L.pdx_learned_samples.restype = C.c_int64
     L.pdx_batch_create.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(_P)]
     L.pdx_batch_create.restype = C.c_int
     L.pdx_batch_size.argtypes = [_P]
@@ -151,6 +163,52 @@ class Model:
         _check(L.pdx_model_get_info(h, C.byref(inf)))
         self.info = inf
         return self
+
+    # ---- implicit Newmark and the learned preconditioner ----
+    def newmark_init(self) -> None:
+        _check(lib().pdx_newmark_init(self._h))
+
+    def newmark_step(self, method: int, collect: bool = False) -> "SolveInfo":
+        info = SolveInfo()
+        _check(lib().pdx_newmark_step(self._h, method, 1 if collect else 0, C.byref(info)))
+        return info
+
+    def learned_setup(self, cells, hidden: int = 128, seed: int = 0, max_samples: int = 4096) -> None:
+        c = list(cells) + [1] * (3 - len(cells))
+        _check(lib().pdx_learned_setup(self._h, c[0], c[1], c[2], hidden, seed, max_samples))
+
+    def learned_samples(self) -> int:
+        return int(lib().pdx_learned_samples(self._h))
+
+    def learned_train(self, epochs: int = 100, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_float()
+        _check(lib().pdx_learned_train(self._h, epochs, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def mlp_params(self, set_to: Optional[np.ndarray] = None) -> np.ndarray:
+        fp = C.POINTER(C.c_float)
+        n = C.c_int64()
+        _check(lib().pdx_mlp_params(self._h, None, None, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.float32)
+        src = None
+        if set_to is not None:
+            keep = np.ascontiguousarray(set_to, dtype=np.float32)
+            src = keep.ctypes.data_as(fp)
+        _check(lib().pdx_mlp_params(self._h, out.ctypes.data_as(fp), src, None))
+        return out
+
+    def mlp_loss_grad(self, x: np.ndarray, t: np.ndarray, w: np.ndarray):
+        fp = C.POINTER(C.c_float)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        n = C.c_int64()
+        _check(lib().pdx_mlp_params(self._h, None, None, C.byref(n)))
+        grad = np.zeros(n.value, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().pdx_mlp_loss_grad(self._h, x.shape[0], x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+                                       w.ctypes.data_as(fp), C.byref(loss), grad.ctypes.data_as(fp)))
+        return loss.value, grad
 
     def batch_offsets(self):
         """(node_off, member_off, eq_off), n+1 entries each, of a batched model."""

@@ -1,0 +1,99 @@
+"""Learned two-level preconditioner: the network's gradients against the CPU
+oracle (oracle/mlp_oracle.py, itself checked against finite differences), and
+what the trained preconditioner gains over plain block-Jacobi flexible CG on
+an implicit Newmark problem at the same true FP64 residual (1e-8)."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import meshgen
+import mlp_oracle
+import pdx
+from conftest import rel
+
+
+def test_oracle_backward_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    n, H, B = 7, 5, 3
+    npar = H * n + H + H * H + H + n * H + n
+    p = rng.standard_normal(npar) * 0.5
+    X = rng.standard_normal((B, n))
+    T = rng.standard_normal((B, n))
+    w = rng.uniform(0.5, 1.5, B)
+    _, g = mlp_oracle.loss_grad(p, n, H, X, T, w, bf16=False)
+    eps = 1e-6
+    fd = np.zeros(npar)
+    for i in range(npar):
+        dp = np.zeros(npar)
+        dp[i] = eps
+        fd[i] = (mlp_oracle.loss_grad(p + dp, n, H, X, T, w, bf16=False)[0] -
+                 mlp_oracle.loss_grad(p - dp, n, H, X, T, w, bf16=False)[0]) / (2 * eps)
+    assert rel(g, fd) < 1e-7
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, -2.5, 3.0e-3], dtype=np.float32)
+    r = mlp_oracle.to_bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0 + 2 ** -6 and r[3] == -2.5
+    assert abs(r[4] - 3.0e-3) <= 3.0e-3 * 2 ** -8
+
+
+def small_newmark_case(dt_factor=20.0):
+    d = tempfile.mkdtemp()
+    mesh, kw = meshgen.config_c5(nx=41, ny=21, nz=11, nsteps=40, radius_h=3, dt_factor=dt_factor)
+    return meshgen.write_case(mesh, d, "c5s", **kw)
+
+
+@pytest.mark.gpu
+def test_network_gradient_matches_oracle(built):
+    H = 32
+    n = (4 * 3 * 3) * 3
+    with pdx.Model(small_newmark_case(), device=0) as m:
+        m.learned_setup((3, 2, 2), hidden=H, seed=5, max_samples=8)
+        p = m.mlp_params()
+        assert p.size == H * n + H + H * H + H + n * H + n
+        rng = np.random.default_rng(1)
+        p = (rng.standard_normal(p.size) * 0.2).astype(np.float32)
+        m.mlp_params(set_to=p)
+        B = 16
+        X = rng.standard_normal((B, n)).astype(np.float32)
+        T = rng.standard_normal((B, n)).astype(np.float32)
+        w = rng.uniform(0.5, 1.5, B).astype(np.float32)
+        loss, g = m.mlp_loss_grad(X, T, w)
+    lo, go = mlp_oracle.loss_grad(p.astype(np.float64), n, H, X, T, w.astype(np.float64), bf16=True)
+    assert abs(loss - lo) <= 1e-3 * abs(lo)
+    # BF16 operands, FP32 accumulation on the GPU; FP64 accumulation in the oracle
+    assert rel(g, go) < 1e-2
+
+
+@pytest.mark.gpu
+def test_learned_preconditioner_gains_over_plain_fcg(built):
+    cmd = small_newmark_case()
+    its_plain, its_learned = [], []
+    with pdx.Model(cmd, device=0) as a:
+        a.newmark_init()
+        for _ in range(15):
+            a.newmark_step(4)
+        for _ in range(5):
+            i = a.newmark_step(4)
+            assert i.converged and i.rel_residual <= 1e-8
+            its_plain.append(i.iterations)
+        ua = a.state()[0]
+    with pdx.Model(cmd, device=0) as b:
+        b.learned_setup((8, 4, 2), hidden=128, seed=0, max_samples=4096)
+        b.newmark_init()
+        for _ in range(15):
+            b.newmark_step(4, collect=True)
+        n_pairs = b.learned_samples()
+        assert n_pairs > 200
+        loss = b.learned_train(epochs=100, lr=1e-3, seed=0)
+        for _ in range(5):
+            i = b.newmark_step(5)
+            assert i.converged and i.rel_residual <= 1e-8
+            its_learned.append(i.iterations)
+        ub = b.state()[0]
+    print(f"\ntrained on {n_pairs} pairs, final loss {loss:.3e}; iterations to 1e-8: "
+          f"plain block-Jacobi FCG {its_plain}, learned {its_learned}")
+    assert rel(ub, ua) < 1e-6
+    assert sum(its_learned) < sum(its_plain)
