@@ -122,6 +122,65 @@ def cpu_sample_batch(cmds, target_s: float = 15.0, threads: int = 0):
     return bonds_steps / el, used, el, o_threads()
 
 
+def bench_implicit(args):
+    """C5: implicit Newmark; solve time to a 1e-8 true FP64 residual per step for the learned two-level flexible CG
+    and for block-Jacobi flexible CG (the plain method), each from the same state after the training steps."""
+    import meshgen
+    import pdx
+    tmp = tempfile.mkdtemp(prefix="pdx_bench_")
+    nsteps = args.train_steps + args.steps + 1
+    if args.c5_size == "full":
+        mesh, kw = meshgen.config_c5(nsteps=nsteps)
+        cells = (25, 12, 5)
+    else:
+        mesh, kw = meshgen.config_c5(nx=61, ny=31, nz=13, radius_h=5, nsteps=nsteps)
+        cells = (8, 4, 2)
+    cmd = meshgen.write_case(mesh, tmp, "c5", **kw)
+    res = {}
+    for method in (4, 5):
+        with pdx.Model(cmd, device=0) as m:
+            if method == 5:
+                m.learned_setup(cells, hidden=128, seed=0, max_samples=args.train_steps * 400)
+            m.newmark_init()
+            t0 = time.perf_counter()
+            for _ in range(args.train_steps):
+                m.newmark_step(4, collect=(method == 5))
+            t_collect = time.perf_counter() - t0
+            loss, t_train, pairs = None, 0.0, 0
+            if method == 5:
+                pairs = m.learned_samples()
+                t0 = time.perf_counter()
+                loss = m.learned_train(epochs=100, lr=1e-3, seed=0)
+                t_train = time.perf_counter() - t0
+            sec, its, resid = [], [], []
+            for _ in range(args.steps):
+                i = m.newmark_step(method)
+                sec.append(i.seconds)
+                its.append(i.iterations)
+                resid.append(i.rel_residual)
+            u = m.state()[0]
+            res[method] = dict(sec=float(np.mean(sec)), its=float(np.mean(its)), resid=float(max(resid)), u=u,
+                               loss=loss, t_train=t_train, t_collect=t_collect, pairs=pairs, n_eq=m.info.n_eq,
+                               nnz=m.info.nnz)
+    p, l = res[4], res[5]
+    du = float(np.linalg.norm(l["u"] - p["u"]) / max(np.linalg.norm(p["u"]), 1e-300))
+    line = {"metric": "implicit Newmark solve time to 1e-8 true residual (s per step)", "value": l["sec"],
+            "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.train_steps, "ms_per_step": l["sec"] * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
+            "data": "synthetic (seeded meshgen config_c5)",
+            "config": {"workload": f"c5 ({args.c5_size}): Hex8 box, inclined penny crack, 5% PD zone, Newmark "
+                                   f"beta 0.25 gamma 0.5, {p['n_eq']} equations, nnz {p['nnz']}",
+                       "coarse_cells": cells, "hidden": 128, "train_steps": args.train_steps},
+            "plain": {"method": "block-Jacobi flexible CG", "s_per_step": p["sec"], "iterations": p["its"],
+                      "max_rel_residual": p["resid"]},
+            "learned": {"method": "flexible CG, block-Jacobi + learned coarse correction", "s_per_step": l["sec"],
+                        "iterations": l["its"], "max_rel_residual": l["resid"], "training_pairs": l["pairs"],
+                        "final_loss": l["loss"], "train_s": l["t_train"], "collect_s": l["t_collect"]},
+            "speedup_vs_plain": p["sec"] / l["sec"] if l["sec"] > 0 else None,
+            "u_rel_diff_learned_vs_plain": du}
+    print(json.dumps(line))
+
+
 def make_workload(tmp: str, nsteps: int, precision: str):
     import meshgen
     mesh, kw = meshgen.config_c2(nsteps=nsteps, precision=precision)
@@ -193,10 +252,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: default, -1: timed on the model)")
     ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: default, -1: timed)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
-                    help="c2: 3D box with hole (default); c4: batch of uneven 2D plates in one launch")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4", "c5"],
+                    help="c2: 3D box with hole (default); c1: 2D strip plate; c4: batch of uneven 2D plates in "
+                         "one launch; c5: implicit Newmark, learned vs plain preconditioner")
     ap.add_argument("--specimens", type=int, default=256, help="c4: number of specimens")
+    ap.add_argument("--c5-size", default="full", choices=["full", "small"],
+                    help="c5: 201x101x41 nodes (full) or 61x31x13 (small)")
+    ap.add_argument("--train-steps", type=int, default=20, help="c5: Newmark steps that collect training pairs")
     args = ap.parse_args()
+    if args.workload == "c5":
+        return bench_implicit(args)
     ws, rank, local = dist_env()
     dist = None
     if ws > 1:
@@ -211,6 +276,15 @@ def main():
                               "s0=2e-3+-5%",
                   "precision": args.precision, "inputs_vs_l2": "bond data streamed per step exceeds the 129 MB L2",
                   "step": "one central-difference step (failure + force + update)"}
+    elif args.workload == "c1":
+        import meshgen
+        mesh, kw = meshgen.config_c1(nsteps=nsteps_cmd)
+        kw["precision"] = args.precision
+        cmd = meshgen.write_case(mesh, tmp, "c1", **kw)
+        config = {"workload": "c1: 2D explicit 101x101-node plate, Q4 + central PD strip 41 nodes wide, 10 mm "
+                              "edge pre-crack, s0=1e-3",
+                  "precision": args.precision, "inputs_vs_l2": "L2-resident (about 2 MB per step)",
+                  "step": "one central-difference step (failure + force + update)"}
     else:
         cmd = make_batch_workload(tmp, args.specimens, nsteps_cmd, args.precision)
         config = {"workload": f"c4: {args.specimens} 2D plates of 60x60..300x300 nodes (seeded), hole or edge "
@@ -220,14 +294,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        rate, n, el, cores = cpu_sample(cmd, target_s=20.0) if args.workload == "c2" else \
+        rate, n, el, cores = cpu_sample(cmd, target_s=20.0) if args.workload != "c4" else \
             cpu_sample_batch(cmd, target_s=20.0)
         line = {"metric": "explicit PD bond-updates/s", "value": rate, "unit": "bond-updates/s", "n_gpus": args.gpus,
                 "steps": n, "warmup": 0, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": rate, "unit": "bond-updates/s", "cores": cores, "kind": "port",
-                                 "sample": (f"{n} explicit steps of the full C2 model on {cores} host threads"
-                                            if args.workload == "c2" else
+                                 "sample": (f"{n} explicit steps of the full {args.workload.upper()} model on "
+                                            f"{cores} host threads" if args.workload != "c4" else
                                             f"4 explicit steps of each of the first {n} specimens on {cores} "
                                             "host threads")},
                 "e2e": {"value": rate, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -235,7 +309,7 @@ def main():
         return
     import pdx
     prec = 1 if args.precision == "MIXED" else 0
-    if args.workload == "c2":
+    if args.workload != "c4":
         model = pdx.Model(cmd, device=local, precision=prec, lanes=args.lanes, fe_lanes=args.fe_lanes)
     else:
         model = pdx.Model.batch(cmd, device=local, precision=prec, lanes=args.lanes, fe_lanes=args.fe_lanes)
@@ -292,14 +366,15 @@ def main():
                     "d2h_bytes_per_step": info.n_eq * 8, "steps": args.e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
-                         "traffic": profile_traffic() if args.precision == "MIXED" else None,
+                         "traffic": (profile_traffic() if args.precision == "MIXED" and args.workload == "c2"
+                                     else None),
                          "traffic_unit": "bytes per launch (ncu, profiles/k_step_mixed_c2.md)", "peak_kind": kind,
                          "algorithmic_bytes_per_step": alg["bytes"], "kernel": "k_step"},
             "gpu_launches": args.steps, "clocks": clk,
             "model": {"n_node": info.n_node, "n_fam": info.n_fam, "n_bond": info.n_bond, "n_eq": info.n_eq,
                       "n_fe": info.n_fe, "lanes": info.lanes, "fe_lanes": info.fe_lanes}}
     if rank == 0 and not args.no_cpu_baseline:
-        if args.workload == "c2":
+        if args.workload != "c4":
             rate, n, el, cores = cpu_sample(cmd, target_s=15.0)
             sample = f"{n} explicit steps of the full model (FP64 oracle) on {cores} threads"
         else:
