@@ -2,7 +2,7 @@
 
 Restates in numpy the 3-layer MLP of the learned two-level preconditioner
 (pdlsm-fem_mpi_gb300/csrc/k_learned.cu, Mlp::forward_backward): parameters in
-one FP32 block (W1 [H x n], b1, W2 [H x H], b2, W3 [n x H], b3), ReLU hidden
+one FP32 block (W1 [H x n], b1, W2 [H x H], b2, W3 [n x H], b3), tanh hidden
 layers, loss sum_b w_b |y_b - t_b|^2.  With ``bf16=True`` every GEMM operand
 is rounded to bfloat16 (round to nearest even) where the GPU kernels round
 it, and products accumulate in float64; with ``bf16=False`` the computation
@@ -42,9 +42,9 @@ def loss_grad(p: np.ndarray, n: int, H: int, X: np.ndarray, T: np.ndarray, w: np
     W1, b1, W2, b2, W3, b3 = split(p, n, H)
     Xr, W1r, W2r, W3r = r(X), r(W1), r(W2), r(W3)
     Z1 = Xr @ W1r.T + b1
-    H1 = r(np.maximum(Z1, 0.0))
+    H1 = r(np.tanh(Z1))
     Z2 = H1 @ W2r.T + b2
-    H2 = r(np.maximum(Z2, 0.0))
+    H2 = r(np.tanh(Z2))
     Y = H2 @ W3r.T + b3
     D = Y - T
     loss = float(np.sum(w[:, None] * D * D))
@@ -52,11 +52,11 @@ def loss_grad(p: np.ndarray, n: int, H: int, X: np.ndarray, T: np.ndarray, w: np
     dYr = r(dY)
     gW3 = dYr.T @ H2
     gb3 = dY.sum(axis=0)
-    dZ2 = (dYr @ W3r) * (Z2 > 0)
+    dZ2 = (dYr @ W3r) * (1.0 - np.tanh(Z2) ** 2)
     dZ2r = r(dZ2)
     gW2 = dZ2r.T @ H1
     gb2 = dZ2.sum(axis=0)
-    dZ1 = (dZ2r @ W2r) * (Z1 > 0)
+    dZ1 = (dZ2r @ W2r) * (1.0 - np.tanh(Z1) ** 2)
     dZ1r = r(dZ1)
     gW1 = dZ1r.T @ Xr
     gb1 = dZ1.sum(axis=0)

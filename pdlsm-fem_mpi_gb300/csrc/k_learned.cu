@@ -7,9 +7,13 @@
 // grid by R~ = diag(1 / row sums of P^T) P^T (the training target of an
 // error).
 //
-// Network: y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 with x = R r / |R r|;
+// Network: y = W3 tanh(W2 tanh(W1 x + b1) + b2) + b3 with x = R r / |R r|;
 // the coarse correction added to the preconditioned residual is
-// P (|R r| sigma y), sigma a fixed target scale.  Training (forward, backward,
+// P (|R r| sigma y), sigma a fixed target scale.  The map it learns is close
+// to the linear, odd coarse solve; tanh keeps the network near-odd and
+// near-linear on inputs unlike its training set (ReLU did not), so the
+// correction stays useful once it has removed the smooth error the training
+// residuals were made of.  Training (forward, backward,
 // Adam) runs with BF16 GEMM operands and FP32 accumulation in the tiled
 // kernels below; inference is one GEMV chain per Krylov iteration.
 // Reductions have a fixed order and there are no atomics, so results are
@@ -94,13 +98,13 @@ void gemm(int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, f
   k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta);
 }
 
-// Z[m][n] += bias[n]; H = BF16(relu(Z)) (or Z without relu)
-__global__ void k_bias_act(int M, int N, float* Z, const float* bias, bf16* H, int relu) {
+// Z[m][n] += bias[n]; H = BF16(tanh(Z)) (or Z without activation)
+__global__ void k_bias_act(int M, int N, float* Z, const float* bias, bf16* H, int act) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)M * N) return;
   const float z = Z[i] + bias[i % N];
   Z[i] = z;
-  if (H) H[i] = __float2bfloat16(relu ? fmaxf(z, 0.f) : z);
+  if (H) H[i] = __float2bfloat16(act ? tanhf(z) : z);
 }
 
 // dY = 2 w_m (Y - T); loss_row[m] = w_m |Y_m - T_m|^2 (one block per row)
@@ -126,11 +130,12 @@ __global__ void k_loss_grad(int M, int N, const float* Y, const float* T, const 
   if (threadIdx.x == 0) loss_row[m] = w[m] * sh[0];
 }
 
-// dZ = dH (Z > 0)
-__global__ void k_relu_back(int64_t n, const float* dH, const float* Z, float* dZ, bf16* dZ16) {
+// dZ = dH (1 - tanh(Z)^2)
+__global__ void k_act_back(int64_t n, const float* dH, const float* Z, float* dZ, bf16* dZ16) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float g = Z[i] > 0.f ? dH[i] : 0.f;
+  const float th = tanhf(Z[i]);
+  const float g = dH[i] * (1.f - th * th);
   dZ[i] = g;
   dZ16[i] = __float2bfloat16(g);
 }
@@ -218,7 +223,7 @@ __global__ void k_normalize(int n, const float* x, bf16* x16, float sigma, float
 }
 
 // inference layer (batch 1): h[row] = act(W[row] . x + b[row]), one warp per row
-__global__ void k_gemv_rows(int rows, int cols, const bf16* W, const bf16* x, const float* b, int relu, bf16* h16,
+__global__ void k_gemv_rows(int rows, int cols, const bf16* W, const bf16* x, const float* b, int act, bf16* h16,
                             float* hf) {
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
@@ -230,7 +235,7 @@ __global__ void k_gemv_rows(int rows, int cols, const bf16* W, const bf16* x, co
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) {
     const float z = s + b[row];
-    const float a = relu ? fmaxf(z, 0.f) : z;
+    const float a = act ? tanhf(z) : z;
     if (h16) h16[row] = __float2bfloat16(a);
     if (hf) hf[row] = a;
   }
@@ -330,12 +335,12 @@ cudaError_t Mlp::forward_backward(int B, const bf16* X, const float* T, const fl
   gemm<true, false>(nout, H, B, dY16, nout, H2, H, gW3, H, 1.f, 0.f, s);
   k_colsum<<<grid_of(nout), kT, 0, s>>>(B, nout, dY, gb3);
   gemm<false, false>(B, H, nout, dY16, nout, W3h, H, dH, H, 1.f, 0.f, s);
-  k_relu_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z2, dZ, dZ16);
+  k_act_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z2, dZ, dZ16);
   // layer 2
   gemm<true, false>(H, H, B, dZ16, H, H1, H, gW2, H, 1.f, 0.f, s);
   k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb2);
   gemm<false, false>(B, H, H, dZ16, H, W2h, H, dH, H, 1.f, 0.f, s);
-  k_relu_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z1, dZ, dZ16);
+  k_act_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z1, dZ, dZ16);
   // layer 1
   gemm<true, false>(H, nin, B, dZ16, H, X, nin, gW1, nin, 1.f, 0.f, s);
   k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb1);

@@ -28,7 +28,7 @@ struct CoarseSpace {
   float* aw = nullptr;        // P^T weights divided by the row sums (coarse average)
 };
 
-// 3-layer MLP nin -> H -> H -> nout with ReLU hidden layers.  Parameters in
+// 3-layer MLP nin -> H -> H -> nout with tanh hidden layers.  Parameters in
 // one FP32 block (W1, b1, W2, b2, W3, b3, row-major) with a BF16 copy for the
 // GEMMs, Adam moments, and the activations of one batch (<= Bmax rows).
 struct Mlp {
