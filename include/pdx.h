@@ -186,6 +186,16 @@ pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_inf
  * pdx_newmark_step(m, 4, 1, ...) collects (at most max_samples). */
 pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, uint64_t seed, int max_samples);
 int64_t pdx_learned_samples(const pdx_model* m);
+/* More training pairs from the solver: nprobe block-Jacobi flexible CG solves
+ * of the last Newmark matrix K_N with right-hand sides uniform in [-1, 1)
+ * drawn from `seed`; every iterate of a converged solve gives a pair.  The
+ * Newmark right-hand sides of successive steps are alike, and probes widen
+ * the set of residuals the network sees.  Needs one pdx_newmark_step first. */
+pdx_status pdx_learned_probe(pdx_model* m, int nprobe, uint64_t seed);
+/* Copy the collected pairs out: r (count x nc) = P^T r_j, e (count x nc) =
+ * coarse averages of the errors x* - x_j.  With r = e = NULL only *count
+ * and *nc are written. */
+pdx_status pdx_learned_pairs(const pdx_model* m, float* r, float* e, int64_t* count, int* nc);
 /* Adam over all collected pairs for `epochs` epochs (batches of 64, order
  * shuffled from `seed`); final_loss = mean relative squared error of the
  * last epoch. */

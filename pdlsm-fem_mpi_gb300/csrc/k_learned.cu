@@ -295,6 +295,17 @@ __global__ void k_stage_raw(int64_t n, const float* Xf, bf16* X) {
   if (i < n) X[i] = __float2bfloat16(Xf[i]);
 }
 
+// b[i] uniform in [-1, 1) from a 64-bit mix of (seed, i) (splitmix64 finaliser)
+__global__ void k_rand_rhs(int64_t n, uint64_t seed, double* b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t z = seed + 0x9e3779b97f4a7c15ull * (uint64_t)(i + 1);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  b[i] = (double)(z >> 11) * 0x1.0p-52 - 1.0;
+}
+
 int grid_of(int64_t n) { return (int)((n + kT - 1) / kT); }
 
 }  // namespace
@@ -415,6 +426,12 @@ cudaError_t learned_stage(int B, int nc, const int* idx, const float* S_r, const
 cudaError_t learned_stage_raw(int B, int nc, const float* Xf, bf16* X, cudaStream_t s) {
   const int64_t n = (int64_t)B * nc;
   k_stage_raw<<<grid_of(n), kT, 0, s>>>(n, Xf, X);
+  return cudaGetLastError();
+}
+
+cudaError_t learned_random_rhs(int64_t n, uint64_t seed, double* b, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_rand_rhs<<<grid_of(n), kT, 0, s>>>(n, seed, b);
   return cudaGetLastError();
 }
 

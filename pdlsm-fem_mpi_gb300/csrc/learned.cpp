@@ -16,7 +16,7 @@
 // With `collect`, a method-4 solve stores one training pair per iteration:
 // the restricted residual P^T r_j and the coarse average of the error
 // x* - x_j, known once the solve has converged (the solver generates its own
-// training data).
+// training data); pdx_learned_probe adds solves with random right-hand sides.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -30,6 +30,8 @@ namespace {
 
 // directions kept for A-orthogonalisation with the nonlinear learned preconditioner
 constexpr int kLearnedTrunc = 8;
+// training pairs are kept while |P^T r_j| >= kTailCut * tol * |P^T r_0|
+constexpr double kTailCut = 1e3;
 
 struct Collector : IterHook {
   Learned* L = nullptr;
@@ -115,40 +117,65 @@ T* dev_upload(DevBuf& b, const std::vector<T>& h, cudaStream_t s) {
   return d;
 }
 
-pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* x, KrylovResult* kr) {
+DevCsr model_csr(const pdx_model* m) {
   DevCsr A;
   A.n = m->setup.n_eq;
   A.nnz = (int64_t)m->setup.csr_ja.size();
   A.ia = m->d_ia;
   A.ja = m->d_ja;
   A.a = m->d_Kval;
+  return A;
+}
+
+// Block-Jacobi flexible CG on the model's current matrix.  With L, every
+// iterate gives a training pair; the pairs are kept only if the solve
+// converges, and only up to the point where |P^T r_j| comes within kTailCut
+// of the tolerance: the converged x stands in for x*, and past that point
+// x* - x_j is mostly the error of the stand-in.
+pdx_status plain_solve(pdx_model* m, const double* b, double* x, Learned* L, KrylovResult* kr) {
+  Collector col;
+  if (L) {
+    col.L = L;
+    col.every = 1;
+    L->solve_first = L->count;
+  }
+  pdx_status st = cuda_check(krylov_fcg(model_csr(m), b, x, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim,
+                                        nullptr, L ? &col : nullptr, 0, 1, m->stream, kr), "flexible CG");
+  if (st || !L) return st;
+  if (!kr->converged) {
+    L->count = L->solve_first;
+    return PDX_OK;
+  }
+  st = cuda_check(coarse_restrict(L->cs, true, x, L->ax, m->stream), "restriction");
+  if (!st) st = cuda_check(learned_err(L->solve_first, L->count, L->cs.nc, L->ax, L->S_x, m->stream), "errors");
+  if (st) return st;
+  const int first = L->solve_first, cnt = L->count - first;
+  if (cnt < 1) return PDX_OK;
+  const int64_t nc = L->cs.nc;
+  std::vector<float> nr((size_t)cnt);
+  st = cuda_check(learned_norms(cnt, (int)nc, L->S_r + first * nc, L->S_scale + first, m->stream), "norms");
+  if (!st) cudaMemcpyAsync(nr.data(), L->S_scale + first, (size_t)cnt * 4, cudaMemcpyDeviceToHost, m->stream);
+  if (!st) st = cuda_check(cudaStreamSynchronize(m->stream), "norms");
+  if (st) return st;
+  const double cut = kTailCut * m->cmd.solve_tol * nr[0];
+  int keep = 0;
+  while (keep < cnt && nr[keep] >= cut) keep++;
+  L->count = first + keep;
+  return PDX_OK;
+}
+
+pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* x, KrylovResult* kr) {
+  const DevCsr A = model_csr(m);
   const double* b = m->d_tmp_eq[0];
   const double tol = m->cmd.solve_tol;
   const int maxit = m->cmd.solve_maxit;
   const int bd = m->mesh.dim;
   Learned* L = m->learned;
   if (method <= 3) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
-  if (method == 4) {
-    Collector col;
-    const bool take = collect && L;
-    if (take) {
-      col.L = L;
-      col.every = 1;
-      L->solve_first = L->count;
-    }
-    pdx_status st = cuda_check(
-        krylov_fcg(A, b, x, tol, maxit, bd, nullptr, take ? &col : nullptr, 0, 1, m->stream, kr), "flexible CG");
-    if (st) return st;
-    if (take && kr->converged) {
-      st = cuda_check(coarse_restrict(L->cs, true, x, L->ax, m->stream), "restriction");
-      if (!st) st = cuda_check(learned_err(L->solve_first, L->count, L->cs.nc, L->ax, L->S_x, m->stream), "errors");
-      return st;
-    }
-    if (take) L->count = L->solve_first;   // drop the pairs of a solve that did not converge
-    return PDX_OK;
-  }
+  if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
-  pdx_status st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, 200, kLearnedTrunc, m->stream, kr),
+  // the learned correction is dropped if it has not cut the residual 10x within 60 iterations
+  pdx_status st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, 60, kLearnedTrunc, m->stream, kr),
                              "learned flexible CG");
   if (st || kr->converged) return st;
   const int its = kr->iterations;
@@ -276,6 +303,36 @@ pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, u
 }
 
 int64_t pdx_learned_samples(const pdx_model* m) { return m && m->learned ? m->learned->count : 0; }
+
+pdx_status pdx_learned_probe(pdx_model* m, int nprobe, uint64_t seed) {
+  NEED_DEV(m);
+  Learned* L = m->learned;
+  if (!L) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  if (!m->newmark_ready || m->steps_done < 1) return set_error(PDX_ERR_INVALID, "run a Newmark step first");
+  const int64_t ne = m->setup.n_eq;
+  double* b = m->d_tmp_eq[5];
+  double* x = m->d_tmp_eq[6];
+  for (int p = 0; p < nprobe; p++) {
+    pdx_status st = cuda_check(learned_random_rhs(ne, seed + (uint64_t)p * 0x51ed27ull, b, m->stream), "probe rhs");
+    if (st) return st;
+    cudaMemsetAsync(x, 0, (size_t)ne * 8, m->stream);
+    KrylovResult kr;
+    st = plain_solve(m, b, x, L, &kr);
+    if (st) return st;
+  }
+  return cuda_check(cudaStreamSynchronize(m->stream), "probe solves");
+}
+
+pdx_status pdx_learned_pairs(const pdx_model* m, float* r, float* e, int64_t* count, int* nc) {
+  if (!m || !m->learned) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  const Learned* L = m->learned;
+  if (count) *count = L->count;
+  if (nc) *nc = L->cs.nc;
+  const size_t bytes = (size_t)L->count * L->cs.nc * 4;
+  if (r) cudaMemcpyAsync(r, L->S_r, bytes, cudaMemcpyDeviceToHost, m->stream);
+  if (e) cudaMemcpyAsync(e, L->S_x, bytes, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "training pairs");
+}
 
 pdx_status pdx_learned_train(pdx_model* m, int epochs, float lr, uint64_t seed, float* final_loss) {
   NEED_DEV(m);

@@ -64,6 +64,7 @@ cudaError_t learned_norms(int count, int nc, const float* S, float* norms, cudaS
 cudaError_t learned_stage(int B, int nc, const int* idx, const float* S_r, const float* S_e, const float* norms,
                           float sigma, __nv_bfloat16* X, float* T, float* W, cudaStream_t s);
 cudaError_t learned_stage_raw(int B, int nc, const float* Xf, __nv_bfloat16* X, cudaStream_t s);
+cudaError_t learned_random_rhs(int64_t n, uint64_t seed, double* b, cudaStream_t s);
 
 // Everything the learned preconditioner of one model owns.
 struct Learned : CoarseCorrection {

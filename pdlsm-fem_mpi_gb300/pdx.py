@@ -54,7 +54,8 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_explicit_step_host", "pdx_explicit_step_count", "pdx_get_state", "pdx_assemble_csr",
             "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc", "pdx_batch_create", "pdx_batch_size",
             "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
-            "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad"]
+            "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad", "pdx_learned_probe",
+            "pdx_learned_pairs"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -98,7 +99,9 @@ def lib() -> C.CDLL:
                        ("pdx_learned_setup", [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int]),
                        ("pdx_learned_train", [_P, C.c_int, C.c_float, C.c_uint64, _F]),
                        ("pdx_mlp_params", [_P, _F, _F, C.POINTER(C.c_int64)]),
-                       ("pdx_mlp_loss_grad", [_P, C.c_int, _F, _F, _F, _F, _F])):
+                       ("pdx_mlp_loss_grad", [_P, C.c_int, _F, _F, _F, _F, _F]),
+                       ("pdx_learned_probe", [_P, C.c_int, C.c_uint64]),
+                       ("pdx_learned_pairs", [_P, _F, _F, C.POINTER(C.c_int64), C.POINTER(C.c_int)])):
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
     L.pdx_learned_samples.argtypes = [_P]
@@ -179,6 +182,19 @@ class Model:
 
     def learned_samples(self) -> int:
         return int(lib().pdx_learned_samples(self._h))
+
+    def learned_probe(self, nprobe: int, seed: int = 1) -> None:
+        _check(lib().pdx_learned_probe(self._h, nprobe, seed))
+
+    def learned_pairs(self):
+        """(P^T r_j, coarse errors) of the collected pairs, each (count, nc) float32."""
+        cnt, nc = C.c_int64(), C.c_int()
+        _check(lib().pdx_learned_pairs(self._h, None, None, C.byref(cnt), C.byref(nc)))
+        r = np.zeros((cnt.value, nc.value), dtype=np.float32)
+        e = np.zeros_like(r)
+        fp = C.POINTER(C.c_float)
+        _check(lib().pdx_learned_pairs(self._h, r.ctypes.data_as(fp), e.ctypes.data_as(fp), None, None))
+        return r, e
 
     def learned_train(self, epochs: int = 100, lr: float = 1e-3, seed: int = 0) -> float:
         loss = C.c_float()

@@ -81,12 +81,15 @@ def test_learned_preconditioner_gains_over_plain_fcg(built):
             its_plain.append(i.iterations)
         ua = a.state()[0]
     with pdx.Model(cmd, device=0) as b:
-        b.learned_setup((8, 4, 2), hidden=128, seed=0, max_samples=4096)
+        b.learned_setup((8, 4, 2), hidden=128, seed=0, max_samples=8192)
         b.newmark_init()
         for _ in range(15):
             b.newmark_step(4, collect=True)
+        n_steps = b.learned_samples()
+        b.learned_probe(20, seed=1)
         n_pairs = b.learned_samples()
-        assert n_pairs > 200
+        # tails near the tolerance are dropped: about half of each solve is kept
+        assert n_steps > 200 and n_pairs > n_steps + 20 * 30
         loss = b.learned_train(epochs=100, lr=1e-3, seed=0)
         for _ in range(5):
             i = b.newmark_step(5)
