@@ -140,7 +140,7 @@ def bench_implicit(args):
     for method in (4, 5):
         with pdx.Model(cmd, device=0) as m:
             if method == 5:
-                m.learned_setup(cells, hidden=128, seed=0, max_samples=args.train_steps * 400)
+                m.learned_setup(cells, hidden=128, seed=0, max_samples=(args.train_steps + args.probes) * 200)
             m.newmark_init()
             t0 = time.perf_counter()
             for _ in range(args.train_steps):
@@ -148,6 +148,10 @@ def bench_implicit(args):
             t_collect = time.perf_counter() - t0
             loss, t_train, pairs = None, 0.0, 0
             if method == 5:
+                if args.probes:
+                    t0 = time.perf_counter()
+                    m.learned_probe(args.probes, seed=1)
+                    t_collect += time.perf_counter() - t0
                 pairs = m.learned_samples()
                 t0 = time.perf_counter()
                 loss = m.learned_train(epochs=100, lr=1e-3, seed=0)
@@ -170,7 +174,8 @@ def bench_implicit(args):
             "data": "synthetic (seeded meshgen config_c5)",
             "config": {"workload": f"c5 ({args.c5_size}): Hex8 box, inclined penny crack, 5% PD zone, Newmark "
                                    f"beta 0.25 gamma 0.5, {p['n_eq']} equations, nnz {p['nnz']}",
-                       "coarse_cells": cells, "hidden": 128, "train_steps": args.train_steps},
+                       "coarse_cells": cells, "hidden": 128, "train_steps": args.train_steps,
+                       "probe_solves": args.probes},
             "plain": {"method": "block-Jacobi flexible CG", "s_per_step": p["sec"], "iterations": p["its"],
                       "max_rel_residual": p["resid"]},
             "learned": {"method": "flexible CG, block-Jacobi + learned coarse correction", "s_per_step": l["sec"],
@@ -259,6 +264,8 @@ def main():
     ap.add_argument("--c5-size", default="full", choices=["full", "small"],
                     help="c5: 201x101x41 nodes (full) or 61x31x13 (small)")
     ap.add_argument("--train-steps", type=int, default=20, help="c5: Newmark steps that collect training pairs")
+    ap.add_argument("--probes", type=int, default=60,
+                    help="c5: random right-hand-side solves that add training pairs")
     args = ap.parse_args()
     if args.workload == "c5":
         return bench_implicit(args)

@@ -192,6 +192,13 @@ int64_t pdx_learned_samples(const pdx_model* m);
  * Newmark right-hand sides of successive steps are alike, and probes widen
  * the set of residuals the network sees.  Needs one pdx_newmark_step first. */
 pdx_status pdx_learned_probe(pdx_model* m, int nprobe, uint64_t seed);
+/* Learned-solve settings (after pdx_learned_setup): trunc = directions kept
+ * for A-orthogonalisation (1..32, default 1; the learned correction is not
+ * linear, and more directions keep the search directions A-orthogonal when
+ * it varies more from one residual to the next), stall_window =
+ * iterations after which the learned correction is given up if the residual
+ * has not fallen 10x (default 60; 0 = never). */
+pdx_status pdx_learned_options(pdx_model* m, int trunc, int stall_window);
 /* Copy the collected pairs out: r (count x nc) = P^T r_j, e (count x nc) =
  * coarse averages of the errors x* - x_j.  With r = e = NULL only *count
  * and *nc are written. */

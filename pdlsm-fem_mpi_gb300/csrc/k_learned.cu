@@ -15,7 +15,8 @@
 // correction stays useful once it has removed the smooth error the training
 // residuals were made of.  Training (forward, backward,
 // Adam) runs with BF16 GEMM operands and FP32 accumulation in the tiled
-// kernels below; inference is one GEMV chain per Krylov iteration.
+// kernels below; inference of one residual is one block-wide kernel
+// (k_infer_block) per Krylov iteration.
 // Reductions have a fixed order and there are no atomics, so results are
 // reproducible.
 #include <cuda_bf16.h>
@@ -182,12 +183,26 @@ __global__ void k_to_bf16(int64_t n, const float* x, bf16* y) {
 }
 
 // coarse[c] = sum_j w_j r[e_j] over restriction row c (FP64 accumulation)
-__global__ void k_restrict(int nc, const int* rptr, const int* ridx, const float* rw, const double* r, float* out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
+// out[c] = sum_j rw[j] r[ridx[j]] over row c of P^T; one block per row,
+// thread-strided FP64 sums combined in a fixed order (same bits on every run)
+__global__ void __launch_bounds__(kT) k_restrict(int nc, const int* rptr, const int* ridx, const float* rw,
+                                                 const double* r, float* out) {
+  __shared__ double red[kT / 32];
+  const int c = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double s = 0.0;
-  for (int j = rptr[c]; j < rptr[c + 1]; j++) s += (double)rw[j] * r[ridx[j]];
-  out[c] = (float)s;
+  const int j1 = rptr[c + 1];
+  for (int j = rptr[c] + threadIdx.x; j < j1; j += kT) s += (double)rw[j] * r[ridx[j]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < kT / 32; w++) t += red[w];
+    out[c] = (float)t;
+  }
 }
 
 // z[e] += scale sum_j P_ej c[j]
@@ -239,6 +254,114 @@ __global__ void k_gemv_rows(int rows, int cols, const bf16* W, const bf16* x, co
     if (h16) h16[row] = __float2bfloat16(a);
     if (hf) hf[row] = a;
   }
+}
+
+// Inference copy of the BF16 weights with rows padded to a multiple of 8
+// (16-byte rows): W1 (H x ldi), W2 (H x ldh), W3 (nout x ldh); pads are 0.
+__global__ void k_pack_infer(int nin, int H, int nout, int ldi, int ldh, const bf16* w16, bf16* wi) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n1 = (int64_t)H * ldi, n2 = (int64_t)H * ldh, n3 = (int64_t)nout * ldh;
+  if (i >= n1 + n2 + n3) return;
+  const bf16* W2 = w16 + (int64_t)H * nin + H;
+  const bf16* W3 = W2 + (int64_t)H * H + H;
+  bf16 v = __float2bfloat16(0.f);
+  if (i < n1) {
+    const int row = (int)(i / ldi), col = (int)(i % ldi);
+    if (col < nin) v = w16[(int64_t)row * nin + col];
+  } else if (i < n1 + n2) {
+    const int64_t k = i - n1;
+    const int row = (int)(k / ldh), col = (int)(k % ldh);
+    if (col < H) v = W2[(int64_t)row * H + col];
+  } else {
+    const int64_t k = i - n1 - n2;
+    const int row = (int)(k / ldh), col = (int)(k % ldh);
+    if (col < H) v = W3[(int64_t)row * H + col];
+  }
+  wi[i] = v;
+}
+
+// One layer of the one-block inference: out[row] = W[row] . in (+ b, tanh),
+// G consecutive threads per row (G a power of 2 <= 32), each summing every
+// G-th 16-byte slice (8 BF16) of the row; the G partials are combined by a
+// butterfly within the group.  W rows have ld elements, ld % 8 == 0; `in` is
+// in shared memory.  Rows are taken in passes of blockDim / G.
+template <int G>
+__device__ __forceinline__ void layer_rows(int rows, int ld, const bf16* __restrict__ W, const bf16* in,
+                                           const float* b, bool act, bf16* out16, float* outf) {
+  const int ld8 = ld / 8;
+  const int sub = threadIdx.x & (G - 1);
+  for (int row0 = 0; row0 < rows; row0 += blockDim.x / G) {
+    const int row = row0 + threadIdx.x / G;
+    float s = 0.f;
+    if (row < rows) {
+      const uint4* w = reinterpret_cast<const uint4*>(W + (int64_t)row * ld);
+      const uint4* x = reinterpret_cast<const uint4*>(in);
+      for (int k = sub; k < ld8; k += G) {
+        const uint4 a = __ldg(w + k);
+        const uint4 v = x[k];
+        const __nv_bfloat162* a2 = reinterpret_cast<const __nv_bfloat162*>(&a);
+        const __nv_bfloat162* v2 = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float2 fa = __bfloat1622float2(a2[q]);
+          const float2 fv = __bfloat1622float2(v2[q]);
+          s = fmaf(fa.x, fv.x, s);
+          s = fmaf(fa.y, fv.y, s);
+        }
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (row < rows && sub == 0) {
+      const float z = s + b[row];
+      if (out16) out16[row] = __float2bfloat16(act ? tanhf(z) : z);
+      if (outf) outf[row] = act ? tanhf(z) : z;
+    }
+  }
+}
+
+// The whole inference of one residual in one block: |x|, x16 = BF16(x / |x|),
+// two tanh layers and the linear output layer; *scale_out = |x| sigma.
+__global__ void __launch_bounds__(1024) k_infer_block(int nin, int H, int nout, int ldi, int ldh, const float* x,
+                                                      float sigma, const bf16* __restrict__ wi, const float* b1,
+                                                      const float* b2, const float* b3, float* y, float* scale_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  bf16* xs = reinterpret_cast<bf16*>(smem_raw);
+  bf16* h1 = xs + ldi;
+  bf16* h2 = h1 + ldh;
+  __shared__ float red[32];
+  __shared__ float nrm_sh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < nin; i += blockDim.x) s += x[i] * x[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (warp == 0) {
+    float t = lane < nw ? red[lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) nrm_sh = sqrtf(t);
+  }
+  __syncthreads();
+  const float nrm = nrm_sh;
+  const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
+  for (int i = threadIdx.x; i < ldi; i += blockDim.x) xs[i] = __float2bfloat16(i < nin ? x[i] * inv : 0.f);
+  for (int i = H + threadIdx.x; i < ldh; i += blockDim.x) {
+    h1[i] = __float2bfloat16(0.f);
+    h2[i] = __float2bfloat16(0.f);
+  }
+  __syncthreads();
+  const bf16* W1 = wi;
+  const bf16* W2 = W1 + (int64_t)H * ldi;
+  const bf16* W3 = W2 + (int64_t)H * ldh;
+  layer_rows<8>(H, ldi, W1, xs, b1, true, h1, nullptr);
+  __syncthreads();
+  layer_rows<8>(H, ldh, W2, h1, b2, true, h2, nullptr);
+  __syncthreads();
+  layer_rows<2>(nout, ldh, W3, h2, b3, false, nullptr, y);
+  if (threadIdx.x == 0) *scale_out = nrm * sigma;
 }
 
 // S[j] = ax - S[j] for samples j in [first, last): iterate averages -> error averages
@@ -373,6 +496,29 @@ cudaError_t Mlp::sync_bf16(cudaStream_t s) {
   return cudaGetLastError();
 }
 
+int64_t Mlp::n_infer() const {
+  const int ldi = (nin + 7) / 8 * 8, ldh = (H + 7) / 8 * 8;
+  return (int64_t)H * ldi + (int64_t)H * ldh + (int64_t)nout * ldh;
+}
+
+bool Mlp::block_infer_ok() const { return nin <= kInferMaxIn && nout <= kInferMaxIn && H <= kInferMaxH; }
+
+cudaError_t Mlp::pack_infer(cudaStream_t s) {
+  if (!wi) return cudaSuccess;
+  const int ldi = (nin + 7) / 8 * 8, ldh = (H + 7) / 8 * 8;
+  k_pack_infer<<<grid_of(n_infer()), kT, 0, s>>>(nin, H, nout, ldi, ldh, w16, wi);
+  return cudaGetLastError();
+}
+
+cudaError_t Mlp::infer_block(const float* x, float sigma, float* y, float* scale, cudaStream_t s) {
+  float *W1, *b1, *W2, *b2, *W3, *b3;
+  param_views(w, &W1, &b1, &W2, &b2, &W3, &b3);
+  const int ldi = (nin + 7) / 8 * 8, ldh = (H + 7) / 8 * 8;
+  const size_t smem = (size_t)(ldi + 2 * ldh) * sizeof(bf16);
+  k_infer_block<<<1, 1024, smem, s>>>(nin, H, nout, ldi, ldh, x, sigma, wi, b1, b2, b3, y, scale);
+  return cudaGetLastError();
+}
+
 cudaError_t Mlp::infer(const bf16* x16, float* y, cudaStream_t s) {
   float *W1, *b1, *W2, *b2, *W3, *b3;
   param_views(w, &W1, &b1, &W2, &b2, &W3, &b3);
@@ -388,7 +534,8 @@ cudaError_t Mlp::infer(const bf16* x16, float* y, cudaStream_t s) {
 // ------------------------------------------------------ transfer, data ----
 
 cudaError_t coarse_restrict(const CoarseSpace& cs, bool average, const double* r, float* out, cudaStream_t s) {
-  k_restrict<<<grid_of(cs.nc), kT, 0, s>>>(cs.nc, cs.rptr, cs.ridx, average ? cs.aw : cs.rw, r, out);
+  if (cs.nc <= 0) return cudaSuccess;
+  k_restrict<<<cs.nc, kT, 0, s>>>(cs.nc, cs.rptr, cs.ridx, average ? cs.aw : cs.rw, r, out);
   return cudaGetLastError();
 }
 

@@ -28,8 +28,6 @@ namespace pdx {
 
 namespace {
 
-// directions kept for A-orthogonalisation with the nonlinear learned preconditioner
-constexpr int kLearnedTrunc = 8;
 // training pairs are kept while |P^T r_j| >= kTailCut * tol * |P^T r_0|
 constexpr double kTailCut = 1e3;
 
@@ -174,8 +172,9 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
   if (method <= 3) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
   if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
-  // the learned correction is dropped if it has not cut the residual 10x within 60 iterations
-  pdx_status st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, 60, kLearnedTrunc, m->stream, kr),
+  pdx_status st = cuda_check(L->net.pack_infer(m->stream), "inference weights");
+  if (st) return st;
+  st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, L->stall_window, L->trunc, m->stream, kr),
                              "learned flexible CG");
   if (st || kr->converged) return st;
   const int its = kr->iterations;
@@ -199,8 +198,14 @@ void learned_destroy(pdx_model* m) {
 
 cudaError_t Learned::add(const double* r, double* z, cudaStream_t s) {
   cudaError_t e = coarse_restrict(cs, false, r, rc, s);
-  if (e == cudaSuccess) e = coarse_normalize(cs.nc, rc, x16, sigma, scale, s);
-  if (e == cudaSuccess) e = net.infer(x16, y, s);
+  if (e == cudaSuccess) {
+    if (net.wi) {
+      e = net.infer_block(rc, sigma, y, scale, s);
+    } else {
+      e = coarse_normalize(cs.nc, rc, x16, sigma, scale, s);
+      if (e == cudaSuccess) e = net.infer(x16, y, s);
+    }
+  }
   if (e == cudaSuccess) e = coarse_prolong_add(cs, y, scale, z, s);
   return e;
 }
@@ -264,6 +269,7 @@ pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, u
   }
   net.w = dev_upload(L->buf, w0, s);
   net.w16 = L->buf.alloc<__nv_bfloat16>(npar);
+  if (net.block_infer_ok()) net.wi = L->buf.alloc<__nv_bfloat16>(net.n_infer());
   net.g = L->buf.alloc<float>(npar);
   net.m1 = L->buf.alloc<float>(npar);
   net.m2 = L->buf.alloc<float>(npar);
@@ -303,6 +309,14 @@ pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, u
 }
 
 int64_t pdx_learned_samples(const pdx_model* m) { return m && m->learned ? m->learned->count : 0; }
+
+pdx_status pdx_learned_options(pdx_model* m, int trunc, int stall_window) {
+  if (!m || !m->learned) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
+  if (trunc < 1 || trunc > 32 || stall_window < 0) return set_error(PDX_ERR_INVALID, "trunc in 1..32, stall window >= 0");
+  m->learned->trunc = trunc;
+  m->learned->stall_window = stall_window;
+  return PDX_OK;
+}
 
 pdx_status pdx_learned_probe(pdx_model* m, int nprobe, uint64_t seed) {
   NEED_DEV(m);

@@ -28,6 +28,9 @@ struct CoarseSpace {
   float* aw = nullptr;        // P^T weights divided by the row sums (coarse average)
 };
 
+constexpr int kInferMaxIn = 8192;
+constexpr int kInferMaxH = 1024;
+
 // 3-layer MLP nin -> H -> H -> nout with tanh hidden layers.  Parameters in
 // one FP32 block (W1, b1, W2, b2, W3, b3, row-major) with a BF16 copy for the
 // GEMMs, Adam moments, and the activations of one batch (<= Bmax rows).
@@ -53,6 +56,14 @@ struct Mlp {
   cudaError_t sync_bf16(cudaStream_t s);
   // one input x16 (nin, BF16) -> y (nout, FP32); uses rows 0 of H1 and H2
   cudaError_t infer(const __nv_bfloat16* x16, float* y, cudaStream_t s);
+  // Inference copy of the BF16 weights, rows padded to 16 bytes, for the
+  // one-block inference kernel (inputs up to kInferMaxIn, width up to kInferMaxH)
+  __nv_bfloat16* wi = nullptr;
+  int64_t n_infer() const;
+  bool block_infer_ok() const;
+  cudaError_t pack_infer(cudaStream_t s);
+  // x (nin, FP32, not normalised) -> y; *scale = |x| sigma; one block
+  cudaError_t infer_block(const float* x, float sigma, float* y, float* scale, cudaStream_t s);
 };
 
 cudaError_t coarse_restrict(const CoarseSpace& cs, bool average, const double* r, float* out, cudaStream_t s);
@@ -72,6 +83,9 @@ struct Learned : CoarseCorrection {
   Mlp net;
   DevBuf buf;
   float sigma = 1.f;          // target scale: the network predicts errors / (|R r| sigma)
+  int trunc = 1;              // directions kept for A-orthogonalisation in the learned solve
+  int stall_window = 60;      // the learned correction is dropped if the residual has not
+                              // fallen 10x within this many iterations
   bool trained = false;
   // inference scratch
   float* rc = nullptr;        // nc
