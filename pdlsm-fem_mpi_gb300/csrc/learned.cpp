@@ -11,8 +11,11 @@
 //        mixed PCG + FP64 refinement)
 //   4    block-Jacobi flexible CG: the plain method the learned one is judged by
 //   5    flexible CG with block-Jacobi plus the learned coarse correction; if
-//        it stalls, block-Jacobi flexible CG and then BiCGStab take over from
-//        the current iterate.
+//        it stalls or needs more iterations than the plain solves did,
+//        block-Jacobi flexible CG and then BiCGStab take over from the current
+//        iterate.  Plain block-Jacobi FCG is also the judge: after two learned
+//        solves in a row slower than the plain ones, method 5 runs the plain
+//        method until the network is retrained (pdx_learned_active tells).
 // With `collect`, a method-4 solve stores one training pair per iteration:
 // the restricted residual P^T r_j and the coarse average of the error
 // x* - x_j, known once the solve has converged (the solver generates its own
@@ -172,10 +175,14 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
   if (method <= 3) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
   if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
+  if (L->disabled) return plain_solve(m, b, x, nullptr, kr);
   pdx_status st = cuda_check(L->net.pack_infer(m->stream), "inference weights");
   if (st) return st;
-  st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, L, nullptr, L->stall_window, L->trunc, m->stream, kr),
-                             "learned flexible CG");
+  // A learned solve that needs more iterations than the plain ones has lost:
+  // it is cut there and plain flexible CG finishes from the current iterate.
+  const int cap = L->plain_n > 0 ? std::min(maxit, (int)std::ceil(L->plain_its)) : maxit;
+  st = cuda_check(krylov_fcg(A, b, x, tol, cap, bd, L, nullptr, L->stall_window, L->trunc, m->stream, kr),
+                  "learned flexible CG");
   if (st || kr->converged) return st;
   const int its = kr->iterations;
   st = cuda_check(krylov_fcg(A, b, x, tol, maxit, bd, nullptr, nullptr, 400, 1, m->stream, kr), "flexible CG");
@@ -310,6 +317,10 @@ pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, u
 
 int64_t pdx_learned_samples(const pdx_model* m) { return m && m->learned ? m->learned->count : 0; }
 
+int pdx_learned_active(const pdx_model* m) {
+  return m && m->learned && m->learned->trained && !m->learned->disabled ? 1 : 0;
+}
+
 pdx_status pdx_learned_options(pdx_model* m, int trunc, int stall_window) {
   if (!m || !m->learned) return set_error(PDX_ERR_INVALID, "pdx_learned_setup first");
   if (trunc < 1 || trunc > 32 || stall_window < 0) return set_error(PDX_ERR_INVALID, "trunc in 1..32, stall window >= 0");
@@ -399,6 +410,8 @@ pdx_status pdx_learned_train(pdx_model* m, int epochs, float lr, uint64_t seed, 
     last = nbatch ? (float)(sum / nbatch) : 0.f;
   }
   L->trained = true;
+  L->losses = 0;
+  L->disabled = false;
   if (final_loss) *final_loss = last;
   return PDX_OK;
 }
@@ -493,6 +506,22 @@ pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_inf
   }
   if (!kr.converged)
     return set_error(PDX_ERR_NOCONV, "Newmark solve stopped at relative residual " + std::to_string(kr.rel_residual));
+  if (Learned* L = m->learned) {
+    if (method == 4) {
+      L->plain_its = (L->plain_its * L->plain_n + kr.iterations) / (L->plain_n + 1);
+      L->plain_n++;
+      if (!collect) {
+        L->plain_sec = (L->plain_sec * L->plain_sec_n + ms * 1e-3) / (L->plain_sec_n + 1);
+        L->plain_sec_n++;
+      }
+    } else if (method == 5 && L->trained && !L->disabled) {
+      // judged by time where plain solve times are known, else by iterations
+      const bool lost = L->plain_sec_n > 0 ? ms * 1e-3 >= L->plain_sec
+                                           : (L->plain_n > 0 && kr.iterations >= L->plain_its);
+      L->losses = lost ? L->losses + 1 : 0;
+      if (L->losses >= 2) L->disabled = true;
+    }
+  }
   launch_gather_eq(m->view, u_all, ueq, m->stream);
   launch_newmark_update(ne, m->d_vel, m->d_acc, acc1, m->cmd.dt, m->cmd.beta, m->cmd.gamma, ueq, m->d_vel,
                         m->stream);

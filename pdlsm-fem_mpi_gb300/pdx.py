@@ -55,7 +55,7 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc", "pdx_batch_create", "pdx_batch_size",
             "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
             "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad", "pdx_learned_probe",
-            "pdx_learned_pairs", "pdx_learned_options"]
+            "pdx_learned_pairs", "pdx_learned_options", "pdx_learned_active"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -105,6 +105,8 @@ def lib() -> C.CDLL:
                        ("pdx_learned_pairs", [_P, _F, _F, C.POINTER(C.c_int64), C.POINTER(C.c_int)])):
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
+    L.pdx_learned_active.argtypes = [_P]
+    L.pdx_learned_active.restype = C.c_int
     L.pdx_learned_samples.argtypes = [_P]
     L.pdx_learned_samples.restype = C.c_int64
     L.pdx_batch_create.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(_P)]
@@ -186,6 +188,9 @@ class Model:
 
     def learned_probe(self, nprobe: int, seed: int = 1) -> None:
         _check(lib().pdx_learned_probe(self._h, nprobe, seed))
+
+    def learned_active(self) -> bool:
+        return bool(lib().pdx_learned_active(self._h))
 
     def learned_options(self, trunc: int = 1, stall_window: int = 60) -> None:
         _check(lib().pdx_learned_options(self._h, trunc, stall_window))

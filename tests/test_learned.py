@@ -100,3 +100,29 @@ def test_learned_preconditioner_gains_over_plain_fcg(built):
           f"plain block-Jacobi FCG {its_plain}, learned {its_learned}")
     assert rel(ub, ua) < 1e-6
     assert sum(its_learned) < sum(its_plain)
+
+
+@pytest.mark.gpu
+def test_plain_solver_judges_and_replaces_a_bad_network(built):
+    """Plain block-Jacobi flexible CG is the judge: with a network that only
+    adds noise the learned solves are cut at the plain iteration count, and
+    after two losses method 5 runs the plain method itself."""
+    cmd = small_newmark_case()
+    with pdx.Model(cmd, device=0) as b:
+        b.learned_setup((8, 4, 2), hidden=32, seed=0, max_samples=4096)
+        b.newmark_init()
+        plain = [b.newmark_step(4, collect=True).iterations for _ in range(3)]
+        b.learned_train(epochs=1, lr=1e-3, seed=0)
+        assert b.learned_active()
+        p = b.mlp_params()
+        rng = np.random.default_rng(5)
+        p = (rng.standard_normal(p.size) * 3.0).astype(np.float32)
+        b.mlp_params(set_to=p)
+        its = []
+        for _ in range(4):
+            i = b.newmark_step(5)
+            assert i.converged and i.rel_residual <= 1e-8
+            its.append(i.iterations)
+        assert not b.learned_active()
+        # once switched off, a method-5 step is a plain solve
+        assert abs(its[-1] - np.mean(plain)) <= 20
