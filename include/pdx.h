@@ -248,6 +248,18 @@ pdx_status pdx_batch_offsets(const pdx_model* m, int64_t* node_off, int64_t* mem
  * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM). */
 pdx_status pdx_run(pdx_model* m, const char* results_dir);
 
+/* Quasi-static increments one at a time, the loop body of
+ * pdfemQuasiStaticSolver_CSRformat (pdsolve.cpp:6464-6590) with the direct
+ * PARDISO solve replaced by a Krylov method: pdx_quasi_init resets the state
+ * (initial DOF values, pre-crack bond states); each pdx_quasi_step assembles
+ * K and f_ext - K u through the scatter map, solves K du = f_ext - K u to the
+ * command file's tolerance with `method` (as pdx_solve_opts; BiCGStab takes
+ * over if it does not converge), updates u, applies FC 3 bond failure,
+ * recomputes the stresses and advances the prescribed DOFs.  info->seconds
+ * is the device time of the solve alone. */
+pdx_status pdx_quasi_init(pdx_model* m);
+pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* info);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,14 +36,13 @@ std::string out_name(const pdx_model* m, const std::string& dir, const std::stri
   return dir + "/" + m->mesh.title + "_" + tag + ".vtk";
 }
 
-pdx_status solve_device(pdx_model* m, const double* b, double* x, KrylovResult* kr) {
+pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int method, KrylovResult* kr) {
   DevCsr A;
   A.n = m->setup.n_eq;
   A.nnz = (int64_t)m->setup.csr_ja.size();
   A.ia = m->d_ia;
   A.ja = m->d_ja;
   A.a = m->d_Kval;
-  int method = m->cmd.solve_method;
   cudaError_t e = krylov_solve(A, b, x, method, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
   pdx_status st = cuda_check(e, "Krylov solve");
   if (st) return st;
@@ -58,6 +57,10 @@ pdx_status solve_device(pdx_model* m, const double* b, double* x, KrylovResult* 
       return set_error(PDX_ERR_NOCONV, "Krylov solve stopped at relative residual " + std::to_string(kr->rel_residual));
   }
   return PDX_OK;
+}
+
+pdx_status solve_device(pdx_model* m, const double* b, double* x, KrylovResult* kr) {
+  return solve_device_method(m, b, x, m->cmd.solve_method, kr);
 }
 
 pdx_status run_explicit(pdx_model* m, const std::string& dir) {
@@ -111,35 +114,57 @@ pdx_status run_static(pdx_model* m, const std::string& dir) {
   return PDX_OK;
 }
 
+// One quasi-static increment n, the body of the increment loop of
+// pdfemQuasiStaticSolver_CSRformat (pdsolve.cpp:6464-6590): K du = f_ext - K u
+// solved by `method` (BiCGStab if it does not converge), u += du, then bond
+// failure (FC 3) and the stresses of the new state.  The prescribed DOFs are
+// advanced by the caller.  With solve_ms, the solve is timed with CUDA events.
+pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, float* solve_ms) {
+  double* u_all = m->d_u[0];
+  const int ne = m->setup.n_eq;
+  double* du = m->d_tmp_eq[1];
+  double* ueq = m->d_tmp_eq[2];
+  pdx_status st = assemble_device(m, 2, u_all, n - 1);
+  if (st) return st;
+  cudaMemsetAsync(du, 0, (size_t)ne * 8, m->stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (solve_ms) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, m->stream);
+  }
+  st = solve_device_method(m, m->d_tmp_eq[0], du, method, kr);
+  if (solve_ms) {
+    cudaEventRecord(e1, m->stream);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(solve_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  if (st) return st;
+  launch_gather_eq(m->view, u_all, ueq, m->stream);
+  launch_axpby_scale(ne, du, 1.0, ueq, 1.0, m->stream);
+  launch_scatter_eq(m->view, ueq, u_all, m->stream);
+  m->steps_done = n;
+  if (m->view.fail3) {
+    st = model_stress(m, u_all, true, false);
+    if (st) return st;
+    if (m->mixed) launch_shadow(m->view, u_all, m->d_uf[0], m->stream);
+    st = explicit_step_launch(m, 2, n);
+    if (st) return st;
+    return model_stress(m, u_all, false, true);
+  }
+  return model_stress(m, u_all, true, true);
+}
+
 pdx_status run_quasi(pdx_model* m, const std::string& dir) {
   pdx_status st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
   if (st) return st;
   double* u_all = m->d_u[0];
   m->cur = 0;
-  const int ne = m->setup.n_eq;
-  double* du = m->d_tmp_eq[1];
-  double* ueq = m->d_tmp_eq[2];
   for (int n = 1; n <= m->cmd.nsteps; n++) {
-    st = assemble_device(m, 2, u_all, n - 1);
-    if (st) return st;
-    cudaMemsetAsync(du, 0, (size_t)ne * 8, m->stream);
     KrylovResult kr;
-    st = solve_device(m, m->d_tmp_eq[0], du, &kr);
-    if (st) return st;
-    launch_gather_eq(m->view, u_all, ueq, m->stream);
-    launch_axpby_scale(ne, du, 1.0, ueq, 1.0, m->stream);
-    launch_scatter_eq(m->view, ueq, u_all, m->stream);
-    m->steps_done = n;
-    if (m->view.fail3) {
-      st = model_stress(m, u_all, true, false);
-      if (st) return st;
-      if (m->mixed) launch_shadow(m->view, u_all, m->d_uf[0], m->stream);
-      st = explicit_step_launch(m, 2, n);
-      if (st) return st;
-      st = model_stress(m, u_all, false, true);
-    } else {
-      st = model_stress(m, u_all, true, true);
-    }
+    st = quasi_increment(m, n, m->cmd.solve_method, &kr, nullptr);
     if (st) return st;
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps || n == 1) {
       HostState h;
@@ -217,4 +242,38 @@ extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
     case 2: return run_quasi(m, dir);
     default: return set_error(PDX_ERR_PARSE, "solver flag is wrong");
   }
+}
+
+extern "C" pdx_status pdx_quasi_init(pdx_model* m) {
+  if (!m) return set_error(PDX_ERR_INVALID, "null model");
+  if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
+  if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
+  cudaSetDevice(m->device);
+  pdx_status st = pdx_explicit_init(m);
+  if (st) return st;
+  m->cur = 0;
+  m->steps_done = 0;
+  return PDX_OK;
+}
+
+extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* info) {
+  if (!m) return set_error(PDX_ERR_INVALID, "null model");
+  if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
+  if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
+  if (method < 0 || method > 3) return set_error(PDX_ERR_INVALID, "method must be 0..3");
+  if (m->cmd.fail_flag == 1 || m->cmd.fail_flag == 2)
+    return set_error(PDX_ERR_UNSUPPORTED, "failure criteria FC 1 / FC 2 are not implemented (FC 0 and FC 3 are)");
+  cudaSetDevice(m->device);
+  KrylovResult kr;
+  float ms = 0.f;
+  pdx_status st = quasi_increment(m, (int)m->steps_done + 1, method, &kr, &ms);
+  if (info) {
+    info->iterations = kr.iterations;
+    info->rel_residual = kr.rel_residual;
+    info->seconds = ms * 1e-3;
+    info->converged = kr.converged;
+  }
+  if (st) return st;
+  launch_advance_prescribed(m->view, m->d_u[0], m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static increment");
 }

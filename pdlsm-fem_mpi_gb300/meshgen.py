@@ -311,6 +311,16 @@ def config_c1(n: int = 101, nsteps: int = 1000):
                       fc="3 1e-3", precision="FP64")
 
 
+def config_c3(n: int = 401, nsteps: int = 50):
+    """2D quasi-static: 401x401-node 200 mm plate (h = 0.5 mm), PD band over the middle 30% of the
+    width, 40 mm (0.2 W) edge pre-crack, top edge pulled 1e-6 m per increment, s0 = 1e-3, FP64."""
+    L = 0.2 * (n - 1) / 400
+    mesh = plate_strip_crack(n=n, L=L, strip_frac=0.3, crack_len=0.2 * L, title="plateStripC3")
+    mesh.ebcs[2].velocity = 1e-6
+    return mesh, dict(solver="QUASI-STATIC", dt=1.0, nsteps=nsteps, save=max(1, nsteps), factor=3.015, nlf=1.0,
+                      fc="3 1e-3", precision="FP64")
+
+
 def config_c2(nx: int = 121, ny: int = 61, nz: int = 21, nsteps: int = 5000, precision: str = "MIXED"):
     """3D explicit: 120x60x20 mm Hex8 box, 8 mm hole, 40x40 PD zone, s0 = 2e-3 +-5% per bond."""
     mesh = box_hole(nx=nx, ny=ny, nz=nz, h=1e-3, radius=8e-3, pd_x=40, pd_y=40, title="boxHoleC2")

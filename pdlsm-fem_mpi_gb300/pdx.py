@@ -55,7 +55,8 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_solve_csr", "pdx_run", "pdx_pcg_solve_noalloc", "pdx_batch_create", "pdx_batch_size",
             "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
             "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad", "pdx_learned_probe",
-            "pdx_learned_pairs", "pdx_learned_options", "pdx_learned_active"]
+            "pdx_learned_pairs", "pdx_learned_options", "pdx_learned_active",
+            "pdx_quasi_init", "pdx_quasi_step"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -102,6 +103,8 @@ def lib() -> C.CDLL:
                        ("pdx_mlp_loss_grad", [_P, C.c_int, _F, _F, _F, _F, _F]),
                        ("pdx_learned_probe", [_P, C.c_int, C.c_uint64]),
                        ("pdx_learned_options", [_P, C.c_int, C.c_int]),
+                       ("pdx_quasi_init", [_P]),
+                       ("pdx_quasi_step", [_P, C.c_int, C.POINTER(SolveInfo)]),
                        ("pdx_learned_pairs", [_P, _F, _F, C.POINTER(C.c_int64), C.POINTER(C.c_int)])):
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
@@ -169,6 +172,15 @@ class Model:
         _check(L.pdx_model_get_info(h, C.byref(inf)))
         self.info = inf
         return self
+
+    # ---- quasi-static increments ----
+    def quasi_init(self) -> None:
+        _check(lib().pdx_quasi_init(self._h))
+
+    def quasi_step(self, method: int = 1) -> "SolveInfo":
+        info = SolveInfo()
+        _check(lib().pdx_quasi_step(self._h, method, C.byref(info)))
+        return info
 
     # ---- implicit Newmark and the learned preconditioner ----
     def newmark_init(self) -> None:
