@@ -187,34 +187,34 @@ def bench_implicit(args):
 
 
 def bench_quasi(args):
-    """C3: quasi-static increments of the 401x401-node strip plate; device time of the solve to the 1e-8 true FP64
-    residual per increment for each Krylov method, each run from the initial state, beside a CPU direct solve
-    (SuperLU through scipy, the stand-in for the reference's PARDISO) of the first increment's system."""
+    """C3: the loaded quasi-static increment of the 401x401-node strip plate; device time of the solve to the 1e-8
+    true FP64 residual for each Krylov method, beside a CPU direct solve (SuperLU through scipy, the stand-in for
+    the reference's PARDISO) of the same system.  The reference's quasi-static rule puts the 1e-6 m top-edge pull
+    on at the first increment and holds it (setVaryEssentialBC with load ratio 1), so increment 1 is unloaded and
+    increment 2 carries the load; each timed sample re-initialises the model and times increment 2."""
     import meshgen
     import pdx
     tmp = tempfile.mkdtemp(prefix="pdx_bench_")
-    nsteps = args.warmup + args.steps + 1
-    mesh, kw = meshgen.config_c3(nsteps=nsteps)
+    mesh, kw = meshgen.config_c3(nsteps=2)
     cmd = meshgen.write_case(mesh, tmp, "c3", **kw)
     names = {0: "Jacobi PCG", 1: "block-Jacobi PCG", 2: "BiCGStab (Jacobi)", 3: "mixed FP32 PCG + FP64 refinement"}
     res, u_end = {}, {}
-    first = None
+    loaded = None
     for method in (1, 0, 3, 2):
         with pdx.Model(cmd, device=0, precision=0) as m:
-            if first is None:
-                v = m.array("u0").copy()
-                first = m.assemble(2, v)
-            m.quasi_init()
-            for _ in range(args.warmup):
-                m.quasi_step(method)
             sec, its, resid, wall = [], [], [], []
-            for _ in range(args.steps):
+            for rep in range(args.warmup + args.steps):
+                m.quasi_init()
+                m.quasi_step(method)
+                if loaded is None:
+                    loaded = m.assemble(2, m.state()[0])
                 t0 = time.perf_counter()
                 i = m.quasi_step(method)
-                wall.append(time.perf_counter() - t0)
-                sec.append(i.seconds)
-                its.append(i.iterations)
-                resid.append(i.rel_residual)
+                if rep >= args.warmup:
+                    wall.append(time.perf_counter() - t0)
+                    sec.append(i.seconds)
+                    its.append(i.iterations)
+                    resid.append(i.rel_residual)
             u_end[method] = m.state()[0]
             res[method] = dict(method=names[method], s_per_increment=float(np.mean(sec)),
                                increment_wall_s=float(np.mean(wall)), iterations=float(np.mean(its)),
@@ -223,8 +223,7 @@ def bench_quasi(args):
     ref = u_end[1]
     for k in res:
         res[k]["u_rel_diff_vs_block_jacobi"] = float(np.linalg.norm(u_end[k] - ref) / max(np.linalg.norm(ref), 1e-300))
-    # CPU direct stand-in on the first increment's system, and the GPU solve of the same system beside it
-    ia, ja, a, f = first
+    ia, ja, a, f = loaded
     cpu = None
     if not args.no_cpu_baseline:
         import scipy.sparse as sp
@@ -237,16 +236,16 @@ def bench_quasi(args):
         if not info.converged:
             x_gpu, info = pdx.solve_csr(ia, ja, a, f, method=2, rtol=1e-8, max_iter=20000)
         cpu = {"value": t_cpu, "unit": "s per increment (solve)", "cores": 1, "kind": "stand-in",
-               "sample": "the first increment's K du = f solved once by SuperLU (scipy spsolve, 1 thread); "
+               "sample": "the loaded increment's K du = f solved once by SuperLU (scipy spsolve, 1 thread); "
                          "the reference factorises with PARDISO",
                "gpu_vs_direct_rel_diff": float(np.linalg.norm(x_gpu - x_cpu) / max(np.linalg.norm(x_cpu), 1e-300))}
     best = min(res.values(), key=lambda r: r["s_per_increment"])
-    line = {"metric": "quasi-static solve time to 1e-8 true residual (s per increment)", "value": best["s_per_increment"],
-            "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+    line = {"metric": "quasi-static solve time to 1e-8 true residual (s per loaded increment)",
+            "value": best["s_per_increment"], "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": best["s_per_increment"] * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded meshgen config_c3)",
             "config": {"workload": f"c3: 2D quasi-static 401x401-node plate, PD band 30% of the width, 0.2 W "
-                                   f"pre-crack, 1e-6 m per increment, {n_eq} equations, nnz {nnz}",
+                                   f"pre-crack, 1e-6 m top-edge pull, {n_eq} equations, nnz {nnz}",
                        "best_method": best["method"]},
             "methods": [res[k] for k in (1, 0, 3, 2)], "cpu_baseline": cpu}
     print(json.dumps(line))

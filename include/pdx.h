@@ -255,8 +255,12 @@ pdx_status pdx_run(pdx_model* m, const char* results_dir);
  * K and f_ext - K u through the scatter map, solves K du = f_ext - K u to the
  * command file's tolerance with `method` (as pdx_solve_opts; BiCGStab takes
  * over if it does not converge), updates u, applies FC 3 bond failure,
- * recomputes the stresses and advances the prescribed DOFs.  info->seconds
- * is the device time of the solve alone. */
+ * recomputes the stresses and advances the prescribed DOFs by the
+ * reference's quasi-static rule (setVaryEssentialBC, pdsolve.cpp:5263-5311,
+ * load ratio 1 as FC 0 / FC 3 give): a varying EBC whose value is 0 takes
+ * dt * velocity, later increments hold it.  So increment 1 solves the
+ * unloaded state and increment 2 the loaded one.  info->seconds is the
+ * device time of the solve alone. */
 pdx_status pdx_quasi_init(pdx_model* m);
 pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* info);
 

@@ -167,6 +167,7 @@ cudaError_t launch_axpby_scale(int64_t n, const double* x, double alpha, double*
 cudaError_t launch_scatter_eq(const DevView& v, const double* u_eq, double* u_all, cudaStream_t s);
 cudaError_t launch_gather_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s);
 cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStream_t s);
+cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s);
 cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, double beta, double dt, cudaStream_t s);
 cudaError_t launch_shadow(const DevView& v, const double* u_all, float4* uf, cudaStream_t s);
 

@@ -118,7 +118,8 @@ pdx_status run_static(pdx_model* m, const std::string& dir) {
 // pdfemQuasiStaticSolver_CSRformat (pdsolve.cpp:6464-6590): K du = f_ext - K u
 // solved by `method` (BiCGStab if it does not converge), u += du, then bond
 // failure (FC 3) and the stresses of the new state.  The prescribed DOFs are
-// advanced by the caller.  With solve_ms, the solve is timed with CUDA events.
+// advanced by the caller, by the quasi-static rule of setVaryEssentialBC
+// (a varying EBC takes dt * velocity once, from 0, and holds).  With solve_ms, the solve is timed with CUDA events.
 pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, float* solve_ms) {
   double* u_all = m->d_u[0];
   const int ne = m->setup.n_eq;
@@ -172,7 +173,7 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
       if (st) return st;
       write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
     }
-    launch_advance_prescribed(m->view, u_all, m->stream);
+    launch_advance_prescribed_quasi(m->view, u_all, m->stream);
   }
   return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
 }
@@ -274,6 +275,6 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
     info->converged = kr.converged;
   }
   if (st) return st;
-  launch_advance_prescribed(m->view, m->d_u[0], m->stream);
+  launch_advance_prescribed_quasi(m->view, m->d_u[0], m->stream);
   return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static increment");
 }

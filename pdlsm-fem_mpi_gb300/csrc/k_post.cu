@@ -314,6 +314,18 @@ __global__ void k_advance_prescribed(DevView v, double* u_all) {
   if (v.eq[i] < 0 && ((v.bcflag[n] >> d) & 1u)) u_all[i] = u_all[i] + v.dtv[3 * n + d];
 }
 
+// Quasi-static rule of setVaryEssentialBC (pdsolve.cpp:5263-5311, solver
+// flag 2) with the load ratio 1 that FC 0 / FC 3 and every 3D model give: a
+// varying EBC moves by dt * velocity while its value is 0 and holds after.
+// Every node of an EBC carries the EBC's value, so the test is per DOF.
+template <int D>
+__global__ void k_advance_prescribed_quasi(DevView v, double* u_all) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)v.n_node * D) return;
+  const int n = (int)(i / D), d = (int)(i % D);
+  if (v.eq[i] < 0 && ((v.bcflag[n] >> d) & 1u) && u_all[i] == 0.0) u_all[i] = v.dtv[3 * n + d];
+}
+
 template <int D>
 __global__ void k_shadow(DevView v, const double* u, float4* uf) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -389,6 +401,14 @@ cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStrea
   const int blocks = (int)((n + 255) / 256);
   if (v.dim == 2) k_advance_prescribed<2><<<blocks, 256, 0, s>>>(v, u_all);
   else k_advance_prescribed<3><<<blocks, 256, 0, s>>>(v, u_all);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s) {
+  const int64_t n = (int64_t)v.n_node * v.dim;
+  const int blocks = (int)((n + 255) / 256);
+  if (v.dim == 2) k_advance_prescribed_quasi<2><<<blocks, 256, 0, s>>>(v, u_all);
+  else k_advance_prescribed_quasi<3><<<blocks, 256, 0, s>>>(v, u_all);
   return cudaGetLastError();
 }
 

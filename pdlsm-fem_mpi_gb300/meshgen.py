@@ -313,7 +313,8 @@ def config_c1(n: int = 101, nsteps: int = 1000):
 
 def config_c3(n: int = 401, nsteps: int = 50):
     """2D quasi-static: 401x401-node 200 mm plate (h = 0.5 mm), PD band over the middle 30% of the
-    width, 40 mm (0.2 W) edge pre-crack, top edge pulled 1e-6 m per increment, s0 = 1e-3, FP64."""
+    width, 40 mm (0.2 W) edge pre-crack, top edge pulled by 1e-6 m (dt * velocity; the reference's
+    quasi-static rule applies it at the first increment and holds it), s0 = 1e-3, FP64."""
     L = 0.2 * (n - 1) / 400
     mesh = plate_strip_crack(n=n, L=L, strip_frac=0.3, crack_len=0.2 * L, title="plateStripC3")
     mesh.ebcs[2].velocity = 1e-6

@@ -251,14 +251,20 @@ def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
 def test_quasi_static_increments_match_reference(built, method):
     """Three quasi-static increments, one pdx_quasi_step each, against the
     reference's direct-solve trajectory: the Krylov solves stop at a 1e-8 true
-    residual, so displacements agree to the conditioning times that."""
+    residual, so the free displacements agree to the conditioning times that
+    (errors relative to the last increment's free displacements)."""
     gq = golden("p21_quasi")
     with pdx.Model(case_cmd("p21", "p21_quasi"), device=0, precision=0) as m:
+        # the reference records an increment before advancing the prescribed
+        # DOFs and pdx_quasi_step returns after it: compare the free DOFs
+        free = m.array("eq").reshape(-1) >= 0
+        scale = np.linalg.norm(gq["u_traj"][-1].reshape(-1)[free])
         m.quasi_init()
         errs = []
         for i in range(3):
             info = m.quasi_step(method)
             assert info.converged and info.rel_residual <= 1e-8
-            errs.append(rel(m.state()[0], gq["u_traj"][i]))
+            d = m.state()[0].reshape(-1)[free] - gq["u_traj"][i].reshape(-1)[free]
+            errs.append(np.linalg.norm(d) / scale)
     print(f"\nmethod {method}: relative L2 error per increment {['%.1e' % e for e in errs]}")
     assert max(errs) < 1e-6
