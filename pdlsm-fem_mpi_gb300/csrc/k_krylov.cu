@@ -24,6 +24,7 @@ namespace pdx {
 namespace {
 
 constexpr int kRedBlocks = 1024;
+constexpr int kCgStallIts = 400;
 constexpr int kThreads = 256;
 
 template <typename T, int L>
@@ -177,29 +178,96 @@ __global__ void k_add_to(int64_t n, const float* d, double* x) {
     x[i] += (double)d[i];
 }
 
-// BiCGStab vector updates with device scalars
-__global__ void k_bicg_p(int64_t n, const double* rho, const double* rho_old, const double* alpha,
-                         const double* omega, const double* r, const double* v, double* p) {
-  const double beta = (*rho / *rho_old) * (*alpha / *omega);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = r[i] + beta * (p[i] - *omega * v[i]);
-}
-__global__ void k_bicg_alpha(const double* rho, const double* r0v, double* alpha) {
-  *alpha = *r0v != 0.0 ? *rho / *r0v : 0.0;
-}
-__global__ void k_bicg_s(int64_t n, const double* alpha, const double* r, const double* v, double* s) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s[i] = r[i] - *alpha * v[i];
-}
-__global__ void k_bicg_omega(const double* ts, const double* tt, double* omega) {
-  *omega = *tt != 0.0 ? *ts / *tt : 0.0;
-}
-__global__ void k_bicg_x(int64_t n, const double* alpha, const double* omega, const double* phat,
-                         const double* shat, const double* s, const double* t, double* x, double* r) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += *alpha * phat[i] + *omega * shat[i];
-    r[i] = s[i] - *omega * t[i];
+// Fused BiCGStab steps.  The dot products keep the fixed order of
+// k_dot_partial / k_dot_final (grid-stride partial sums, one block tree,
+// one final block), so the fused solve gives the same bits as separate
+// kernels; scalars stay on the device.
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
   }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// p = r + beta (p - omega v), beta = (rho / rho_prev)(alpha / omega); ph = D^-1 p
+__global__ void k_bicg_p2(int64_t n, const double* rho, const double* rho_prev, const double* alpha,
+                          const double* omega, const double* r, const double* v, const double* dinv, double* p,
+                          double* ph) {
+  const double beta = (*rho / *rho_prev) * (*alpha / *omega);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pi = r[i] + beta * (p[i] - *omega * v[i]);
+    p[i] = pi;
+    ph[i] = dinv[i] * pi;
+  }
+}
+
+// *out = num / (sum of the partials), 0 if the sum is 0
+__global__ void k_final_ratio(const double* part, int np, const double* num, double* out) {
+  __shared__ double sh[kThreads];
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  const double d = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = d != 0.0 ? *num / d : 0.0;
+}
+
+// s = r - alpha v; sh = D^-1 s
+__global__ void k_bicg_s2(int64_t n, const double* alpha, const double* r, const double* v, const double* dinv,
+                          double* s, double* sh) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double si = r[i] - *alpha * v[i];
+    s[i] = si;
+    sh[i] = dinv[i] * si;
+  }
+}
+
+// per-block partials of t.s and t.t
+__global__ void k_dot2_partial(int64_t n, const double* t, const double* s, double* part_ts, double* part_tt) {
+  __shared__ double sh[kThreads];
+  double a = 0, b = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    a += t[i] * s[i];
+    b += t[i] * t[i];
+  }
+  a = block_sum(a, sh);
+  b = block_sum(b, sh);
+  if (threadIdx.x == 0) {
+    part_ts[blockIdx.x] = a;
+    part_tt[blockIdx.x] = b;
+  }
+}
+
+// omega = (t.s) / (t.t), 0 if t.t is 0
+__global__ void k_final_omega(const double* part_ts, const double* part_tt, int np, double* omega) {
+  __shared__ double sh[kThreads];
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    a += part_ts[i];
+    b += part_tt[i];
+  }
+  a = block_sum(a, sh);
+  b = block_sum(b, sh);
+  if (threadIdx.x == 0) *omega = b != 0.0 ? a / b : 0.0;
+}
+
+// x += alpha ph + omega sh; r = s - omega t; per-block partials of r0 . r (the next rho)
+__global__ void k_bicg_x2(int64_t n, const double* alpha, const double* omega, const double* ph, const double* shat,
+                          const double* s, const double* t, const double* r0, double* x, double* r, double* part) {
+  __shared__ double sh[kThreads];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += *alpha * ph[i] + *omega * shat[i];
+    const double ri = s[i] - *omega * t[i];
+    r[i] = ri;
+    acc += r0[i] * ri;
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
 template <typename T>
@@ -269,6 +337,11 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
   }
   int it = 0;
   const int chunk = 10;
+  // CG is not made for the unsymmetric PD stiffness and can stall on it: the
+  // solve stops once the residual has not halved for kCgStallIts iterations
+  // (the caller then sees a true residual above rtol and may switch method)
+  double best = INFINITY;
+  int best_it = 0;
   while (it < max_iter) {
     for (int k = 0; k < chunk && it < max_iter; k++, it++) {
       spmv_t<T>(n, avg, ia, ja, aT, p, q, s);
@@ -283,7 +356,15 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
     double hr = 0;
     cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
-    if (!(std::sqrt(hr) > rtol * bnorm)) break;
+    const double rn = std::sqrt(hr);
+    if (!(rn > rtol * bnorm)) break;
+    if (!(rn == rn)) break;
+    if (rn < 0.5 * best) {
+      best = rn;
+      best_it = it;
+    } else if (it - best_it >= kCgStallIts) {
+      break;
+    }
   }
   return it;
 }
@@ -342,12 +423,8 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     cudaMallocAsync(&t, n * sizeof(double), s);
     cudaMallocAsync(&ph, n * sizeof(double), s);
     cudaMallocAsync(&sh, n * sizeof(double), s);
-    double* rho = dscal + 0;
-    double* rho_old = dscal + 1;
     double* alpha = dscal + 2;
     double* omega = dscal + 3;
-    double* tmp = dscal + 4;
-    double* tmp2 = dscal + 5;
     double* bb = dscal + 6;
     double* rr = dscal + 7;
     spmv(A, x, ax, s);
@@ -362,23 +439,27 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     const double bnorm = std::sqrt(hb);
+    // rho of the iteration and of the one before in two slots (no copies)
+    double* rhos = dscal + 12;
+    double* part2 = nullptr;
+    cudaMallocAsync(&part2, 2 * kRedBlocks * sizeof(double), s);
+    cudaMemcpyAsync(rhos + 1, ones, sizeof(double), cudaMemcpyHostToDevice, s);
+    c.dot<double>(n, r0, r, rhos);
     const int chunk = 10;
     while (bnorm > 0 && iters < max_iter) {
       for (int k = 0; k < chunk && iters < max_iter; k++, iters++) {
-        c.dot<double>(n, r0, r, rho);
-        k_bicg_p<<<g, kThreads, 0, s>>>(n, rho, rho_old, alpha, omega, r, v, p);
-        k_jacobi<double><<<g, kThreads, 0, s>>>(n, dinv, p, ph);
+        double* rho_cur = rhos + (iters & 1);
+        double* rho_prev = rhos + ((iters + 1) & 1);
+        k_bicg_p2<<<g, kThreads, 0, s>>>(n, rho_cur, rho_prev, alpha, omega, r, v, dinv, p, ph);
         spmv(A, ph, v, s);
-        c.dot<double>(n, r0, v, tmp);
-        k_bicg_alpha<<<1, 1, 0, s>>>(rho, tmp, alpha);
-        k_bicg_s<<<g, kThreads, 0, s>>>(n, alpha, r, v, ss);
-        k_jacobi<double><<<g, kThreads, 0, s>>>(n, dinv, ss, sh);
+        k_dot_partial<double><<<g, kThreads, 0, s>>>(n, r0, v, c.part);
+        k_final_ratio<<<1, kThreads, 0, s>>>(c.part, g, rho_cur, alpha);
+        k_bicg_s2<<<g, kThreads, 0, s>>>(n, alpha, r, v, dinv, ss, sh);
         spmv(A, sh, t, s);
-        c.dot<double>(n, t, ss, tmp);
-        c.dot<double>(n, t, t, tmp2);
-        k_bicg_omega<<<1, 1, 0, s>>>(tmp, tmp2, omega);
-        k_bicg_x<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, x, r);
-        k_copy_scalar<<<1, 1, 0, s>>>(rho, rho_old);
+        k_dot2_partial<<<g, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks);
+        k_final_omega<<<1, kThreads, 0, s>>>(part2, part2 + kRedBlocks, g, omega);
+        k_bicg_x2<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, r0, x, r, c.part);
+        k_dot_final<<<1, kThreads, 0, s>>>(c.part, g, rho_prev);   // rho of the next iteration
       }
       c.dot<double>(n, r, r, rr);
       double hr = 0;
@@ -386,6 +467,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
       cudaStreamSynchronize(s);
       if (!(std::sqrt(hr) > rtol * bnorm) || !std::isfinite(hr)) break;
     }
+    cudaFreeAsync(part2, s);
     cudaFreeAsync(r0, s); cudaFreeAsync(v, s); cudaFreeAsync(ss, s);
     cudaFreeAsync(t, s); cudaFreeAsync(ph, s); cudaFreeAsync(sh, s);
   } else if (method == 3) {
