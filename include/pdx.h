@@ -43,7 +43,7 @@ typedef struct pdx_options {
                       fix the order of the force sums: a tuned choice may change
                       results in the last bits from run to run. */
   int verbose;
-  int fe_lanes;    /* lanes per FE-only node in the step kernel (2, 4, 8); 0 = default (4);
+  int fe_lanes;    /* lanes per FE-only node in the step kernel (1, 2, 4, 8); 0 = default (3D 4, 2D 1);
                       < 0 = timed on the model */
 } pdx_options;
 

@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
 template <int D, int LP>
 cudaError_t fp64_dispatch_lf(StepArgs a, int lf, int blocks, cudaStream_t s) {
   switch (lf) {
+    case 1: k_step_fp64<D, LP, 1><<<blocks, 256, 0, s>>>(a); break;
     case 2: k_step_fp64<D, LP, 2><<<blocks, 256, 0, s>>>(a); break;
     case 4: k_step_fp64<D, LP, 4><<<blocks, 256, 0, s>>>(a); break;
     case 8: k_step_fp64<D, LP, 8><<<blocks, 256, 0, s>>>(a); break;
@@ -219,7 +220,7 @@ cudaError_t fp64_dispatch(StepArgs a, int lp, int lf, cudaStream_t s) {
 }  // namespace
 
 bool step_lanes_valid(int lp, int lf) {
-  return (lp == 4 || lp == 8 || lp == 16) && (lf == 2 || lf == 4 || lf == 8);
+  return (lp == 4 || lp == 8 || lp == 16) && (lf == 1 || lf == 2 || lf == 4 || lf == 8);
 }
 
 cudaError_t launch_step(const StepArgs& a, int mixed, int lp, int lf, cudaStream_t s) {

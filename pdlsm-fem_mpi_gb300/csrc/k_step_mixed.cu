@@ -284,6 +284,7 @@ __global__ void k_pack_bonds(DevView v, float pertf, float4* rec) {
 template <int D, int LP>
 cudaError_t mixed_dispatch_lf(const StepArgs& a, int lf, int blocks, size_t smem, cudaStream_t s) {
   switch (lf) {
+    case 1: k_step_mixed<D, LP, 1><<<blocks, 256, smem, s>>>(a); break;
     case 2: k_step_mixed<D, LP, 2><<<blocks, 256, smem, s>>>(a); break;
     case 4: k_step_mixed<D, LP, 4><<<blocks, 256, smem, s>>>(a); break;
     case 8: k_step_mixed<D, LP, 8><<<blocks, 256, smem, s>>>(a); break;

@@ -219,7 +219,7 @@ def test_c1_full_size_fp64_parity(built):
     assert np.array_equal(bs, bs_o)
 
 
-@pytest.mark.parametrize("lanes,fe_lanes", [(4, 2), (8, 4), (16, 8)])
+@pytest.mark.parametrize("lanes,fe_lanes", [(4, 1), (4, 2), (8, 4), (16, 8)])
 def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
     """A jittered Hex8 box (no shared node stencils: FE-only nodes take the
     element path) against the oracle, FP64 and mixed, at several lane counts."""
