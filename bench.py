@@ -132,6 +132,9 @@ def bench_implicit(args):
     if args.c5_size == "full":
         mesh, kw = meshgen.config_c5(nsteps=nsteps)
         cells = (25, 12, 5)
+    elif args.c5_size == "medium":
+        mesh, kw = meshgen.config_c5(nx=101, ny=51, nz=21, radius_h=5, nsteps=nsteps)
+        cells = (12, 6, 3)
     else:
         mesh, kw = meshgen.config_c5(nx=61, ny=31, nz=13, radius_h=5, nsteps=nsteps)
         cells = (8, 4, 2)
@@ -327,8 +330,8 @@ def main():
                          "one launch; c3: quasi-static increments, Krylov methods beside a CPU direct solve; "
                          "c5: implicit Newmark, learned vs plain preconditioner")
     ap.add_argument("--specimens", type=int, default=256, help="c4: number of specimens")
-    ap.add_argument("--c5-size", default="full", choices=["full", "small"],
-                    help="c5: 201x101x41 nodes (full) or 61x31x13 (small)")
+    ap.add_argument("--c5-size", default="full", choices=["full", "medium", "small"],
+                    help="c5: 201x101x41 nodes (full), 101x51x21 (medium) or 61x31x13 (small)")
     ap.add_argument("--train-steps", type=int, default=20, help="c5: Newmark steps that collect training pairs")
     ap.add_argument("--probes", type=int, default=60,
                     help="c5: random right-hand-side solves that add training pairs")
