@@ -124,20 +124,34 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
     load_u(node, uk);
     float4* R = a.brec;
     bool deferred = false;
+    // Two-stage pipeline per lane: records two bonds ahead, and the
+    // neighbour's node record of the next bond requested before the current
+    // bond is computed, so a record load and a gather are in flight while a
+    // bond is tested and summed.
     int b = b0 + lane;
-    float4 ra = make_float4(0, 0, 0, 0), rb = ra;
+    const float4 z4 = make_float4(0, 0, 0, 0);
+    float4 ra = z4, rb = z4, na = z4, nb = z4;
     if (b < b1) load_record<D>(R, b, ra, rb);
+    if (b + L < b1) load_record<D>(R, b + L, na, nb);
+    int m = b < b1 ? __float_as_int(D == 3 ? rb.z : ra.w) : -1;
+    Rec32 g;
+    g.a = z4;
+    g.b = z4;
+    if (m >= 0) g = ld_keep32(nr + 2 * m);
     while (b < b1) {
       const int bn = b + L;
-      float4 na = make_float4(0, 0, 0, 0), nb = na;
-      if (bn < b1) load_record<D>(R, bn, na, nb);
-      const int m = __float_as_int(D == 3 ? rb.z : ra.w);
+      float4 qa = z4, qb = z4;
+      if (bn + L < b1) load_record<D>(R, bn + L, qa, qb);
+      const int mn = bn < b1 ? __float_as_int(D == 3 ? nb.z : na.w) : -1;
+      Rec32 gn;
+      gn.a = z4;
+      gn.b = z4;
+      if (mn >= 0) gn = ld_keep32(nr + 2 * mn);
       if (m >= 0) {
-        const Rec32 nm = ld_keep32(nr + 2 * m);   // position, displacement + flags
-        const float4 um = nm.b;
+        const float4 um = g.b;
         bool cut = false;
         if (brk) {
-          const float4 xm = nm.a;
+          const float4 xm = g.a;
           const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
           const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
           const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
@@ -181,6 +195,10 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
       b = bn;
       ra = na;
       rb = nb;
+      na = qa;
+      nb = qb;
+      m = mn;
+      g = gn;
     }
     if (deferred) {
       // Rare: repeat the FP32 test on this lane's bonds and settle the ones
@@ -238,11 +256,13 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
   warp_update<D, L, true>(a, F, valid ? node : -1);
 }
 
-// Blocks per SM: 5 in 3D (48 registers); 6 in 2D (40 registers, a few spills
-// to L1), which took the 256-plate batch from 700 to 564 us per step (the 2D
-// step waits on its gathers; more resident warps hide more of them).
+// Blocks per SM: 4 in 3D (64 registers: the two-stage family pipeline holds
+// two bond records and a node record per lane; C2 47.0 us per step against
+// 48.5 with 5 blocks); 6 in 2D (40 registers, a few spills to L1), which took
+// the 256-plate batch from 700 to 564 us per step (the 2D step waits on its
+// gathers; more resident warps hide more of them).
 template <int D, int LP, int LF>
-__global__ void __launch_bounds__(256, D == 3 ? 5 : 6) k_step_mixed(StepArgs a) {
+__global__ void __launch_bounds__(256, D == 3 ? 4 : 6) k_step_mixed(StepArgs a) {
   extern __shared__ __align__(16) float s_ke[];
   const float* ke = a.v.ke32;
   if (a.ke_smem) {
