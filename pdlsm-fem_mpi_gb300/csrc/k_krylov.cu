@@ -533,12 +533,92 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
 // coarse correction the longer memory keeps the iteration from stalling.
 
 namespace {
-// p -= (zq / pq) pj
-__global__ void k_fcg_orth(int64_t n, const double* zq, const double* pq, const double* pj, double* p) {
-  const double c = *pq != 0.0 ? *zq / *pq : 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] -= c * pj[i];
+
+// Flexible CG in five kernels per iteration (plus the coarse correction):
+// k_fcg_zq (z . q_j for every kept direction), k_fcg_dir (new direction p and
+// the r . p partials), the SpMV, the p . q partials, k_fcg_update (x, r and
+// the block-Jacobi z).  Each block repeats the final reduction of the
+// partials in the order k_dot_final uses, so the fused iteration gives the
+// same bits as one kernel per operation.
+constexpr int kFcgMaxDirs = 32;
+
+struct FcgDirs {
+  const double* P[kFcgMaxDirs];
+  const double* Q[kFcgMaxDirs];
+  const double* pq[kFcgMaxDirs];   // p_j . q_j of each kept direction
+  int m;                           // kept directions, most recent first
+};
+
+// sum of np partials in the order of k_dot_final (thread-strided, then a tree)
+__device__ __forceinline__ double reduce_partials(const double* part, int np, double* sh) {
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  return block_sum(s, sh);
 }
+
+// part[j * gridDim.x + block] = partial of z . q_j
+__global__ void k_fcg_zq(int64_t n, const double* z, FcgDirs d, double* part) {
+  __shared__ double sh[kThreads];
+  for (int j = 0; j < d.m; j++) {
+    const double* q = d.Q[j];
+    double acc = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      acc += z[i] * q[i];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = acc;
+  }
+}
+
+// p = z - sum_j (z.q_j / p_j.q_j) p_j (most recent first); part_rp = partials of r . p
+__global__ void k_fcg_dir(int64_t n, const double* z, FcgDirs d, const double* part_zq, const double* r, double* p,
+                          double* part_rp) {
+  __shared__ double sh[kThreads];
+  __shared__ double coef[kFcgMaxDirs];
+  for (int j = 0; j < d.m; j++) {
+    const double zq = reduce_partials(part_zq + j * gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) coef[j] = *d.pq[j] != 0.0 ? zq / *d.pq[j] : 0.0;
+  }
+  __syncthreads();
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double pi = z[i];
+    for (int j = 0; j < d.m; j++) pi -= coef[j] * d.P[j][i];
+    p[i] = pi;
+    acc += r[i] * pi;
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part_rp[blockIdx.x] = acc;
+}
+
+// alpha = r.p / p.q from the partials; x += alpha p, r -= alpha q and
+// z = B^-1 r over the d x d diagonal blocks (a thread owns whole blocks)
+__global__ void k_fcg_update(int64_t nb, const int64_t* bptr, const double* binv, const double* part_rp,
+                             const double* part_pq, int np, double* pq_out, const double* p, const double* q, double* x,
+                             double* r, double* z) {
+  __shared__ double sh[kThreads];
+  const double rp = reduce_partials(part_rp, np, sh);
+  const double pq = reduce_partials(part_pq, np, sh);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *pq_out = pq;
+  const double alpha = pq != 0.0 ? rp / pq : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = bptr[i];
+    const int sz = (int)(bptr[i + 1] - r0);
+    double v[3] = {0, 0, 0};
+    for (int c = 0; c < sz; c++) {
+      const int64_t k = r0 + c;
+      x[k] = x[k] + alpha * p[k];
+      const double rk = r[k] - alpha * q[k];
+      r[k] = rk;
+      v[c] = rk;
+    }
+    for (int rr = 0; rr < sz; rr++) {
+      double a = 0;
+      for (int c = 0; c < sz; c++) a += binv[i * 9 + rr * 3 + c] * v[c];
+      z[r0 + rr] = a;
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol, int max_iter, int block_dim,
@@ -551,8 +631,6 @@ cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol,
   double* dscal = nullptr;
   cudaMallocAsync(&c.part, kRedBlocks * sizeof(double), s);
   cudaMallocAsync(&dscal, 16 * sizeof(double), s);
-  double* rp = dscal + 0;
-  double* zq = dscal + 1;
   double* rr = dscal + 2;
   double* bb = dscal + 3;
   // block-Jacobi: inverses of the d x d diagonal blocks of consecutive rows
@@ -567,7 +645,12 @@ cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol,
   cudaMemcpyAsync(bptr, hp.data(), (nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s);
   k_block_inverse<<<(int)((nb + 255) / 256), 256, 0, s>>>(nb, bptr, A.ia, A.ja, A.a, binv);
   // ring of the last `trunc` directions p_j, q_j = A p_j (and the new one)
-  const int mt = std::max(1, trunc) + 1;
+  const int mt = std::min(std::max(1, trunc), kFcgMaxDirs) + 1;
+  const int gb = (int)std::min<int64_t>((nb + kThreads - 1) / kThreads, kRedBlocks);
+  double *part_zq = nullptr, *part_rp = nullptr, *part_pq = nullptr;
+  cudaMallocAsync(&part_zq, (size_t)(mt - 1) * g * sizeof(double), s);
+  cudaMallocAsync(&part_rp, g * sizeof(double), s);
+  cudaMallocAsync(&part_pq, g * sizeof(double), s);
   std::vector<double*> P(mt, nullptr), Q(mt, nullptr);
   double *r, *z, *pqs;
   cudaMallocAsync(&r, n * sizeof(double), s);
@@ -603,17 +686,20 @@ cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol,
         const int slot = it % mt;
         double* p = P[slot];
         double* q = Q[slot];
-        cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-        for (int j = 1; j <= std::min(it, mt - 1); j++) {
+        FcgDirs d;
+        d.m = std::min(it, mt - 1);
+        for (int j = 1; j <= d.m; j++) {
           const int js = (it - j) % mt;
-          c.dot<double>(n, z, Q[js], zq);
-          k_fcg_orth<<<g, kThreads, 0, s>>>(n, zq, pqs + js, P[js], p);
+          d.P[j - 1] = P[js];
+          d.Q[j - 1] = Q[js];
+          d.pq[j - 1] = pqs + js;
         }
+        if (d.m > 0) k_fcg_zq<<<g, kThreads, 0, s>>>(n, z, d, part_zq);
+        k_fcg_dir<<<g, kThreads, 0, s>>>(n, z, d, part_zq, r, p, part_rp);
         spmv_t<double>(n, avg, A.ia, A.ja, A.a, p, q, s);
-        c.dot<double>(n, p, q, pqs + slot);
-        c.dot<double>(n, r, p, rp);
-        k_cg_update<double><<<g, kThreads, 0, s>>>(n, rp, pqs + slot, p, q, x, r);
-        precond(r, z);
+        k_dot_partial<double><<<g, kThreads, 0, s>>>(n, p, q, part_pq);
+        k_fcg_update<<<gb, kThreads, 0, s>>>(nb, bptr, binv, part_rp, part_pq, g, pqs + slot, p, q, x, r, z);
+        if (coarse && err == cudaSuccess) err = coarse->add(r, z, s);
         if (hook && (it + 1) % hook->every == 0 && err == cudaSuccess) err = hook->on_iter(it + 1, x, r, z, s);
       }
       c.dot<double>(n, r, r, rr);
@@ -656,6 +742,9 @@ cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol,
   }
   cudaFreeAsync(bptr, s);
   cudaFreeAsync(binv, s);
+  cudaFreeAsync(part_zq, s);
+  cudaFreeAsync(part_rp, s);
+  cudaFreeAsync(part_pq, s);
   cudaFreeAsync(c.part, s);
   cudaFreeAsync(dscal, s);
   if (err == cudaSuccess) err = cudaGetLastError();
