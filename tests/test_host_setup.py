@@ -1,6 +1,7 @@
 """Host setup (parsers + pdsolve::setDatModel restatement) against the
 reference's own setup dumps, and input-format round trips.  CPU only."""
 import os
+import tempfile
 
 import numpy as np
 import pytest
@@ -138,3 +139,34 @@ def test_command_keywords(built, tmp_path):
     assert np.all(u0[top, 1] == 1e-6)
     dtv = m.array("dtv").reshape(-1, 3)
     assert np.all(dtv[top, 1] == 1.0 * 2e-6)
+
+
+def test_c3_plate_matches_the_configuration_sizes():
+    """C3: 401x401 nodes, PD band over the middle 30 % of the width, 0.2 W
+    pre-crack; about 321.6k equations and 9.6e6 nonzeros."""
+    d = tempfile.mkdtemp()
+    mesh, kw = meshgen.config_c3(nsteps=2)
+    cmd = meshgen.write_case(mesh, d, "c3", **kw)
+    m = pdx.Model(cmd, device=-1)
+    i = m.info
+    assert i.dim == 2 and i.n_node == 401 * 401 and i.solver == 2
+    assert 315_000 < i.n_eq < 322_000
+    assert 9.4e6 < i.nnz < 9.8e6
+    assert i.n_fam > 0 and i.fail_flag == 3
+
+
+def test_step_at_a_time_entry_points_need_a_device():
+    """Quasi-static, Newmark and learned entry points on a host-only model
+    return NODEVICE (or INVALID before set-up) instead of computing on the CPU."""
+    host = pdx.Model(case_cmd("p21", "p21_quasi"), device=-1)
+    for call in (host.quasi_init, lambda: host.quasi_step(1), host.newmark_init, lambda: host.newmark_step(4),
+                 lambda: host.learned_setup((4, 4), hidden=8)):
+        with pytest.raises(pdx.PdxError) as e:
+            call()
+        assert e.value.code == 8
+    for call in (lambda: host.learned_options(1, 60), host.learned_pairs, lambda: host.learned_train(1)):
+        with pytest.raises(pdx.PdxError) as e:
+            call()
+        assert e.value.code in (4, 8)
+    assert host.learned_active() is False
+    assert host.learned_samples() == 0
