@@ -12,6 +12,7 @@
 //   ref_driver static   <cmd.in> <outdir>
 //   ref_driver newmark  <cmd.in> <outdir>
 //   ref_driver quasi    <cmd.in> <outdir>
+//   ref_driver explicit_fc2 <cmd.in> <outdir> <every>  (FC 2 after every step)
 //   ref_driver solve    <cmd.in>             (the reference's own pdfemSolver)
 //
 // Every loop below calls the reference's member functions in the order its own
@@ -250,7 +251,16 @@ void stretch_failure(datModel& d, pdsolve& sol) {
   d.ci_solvFlag = saved;
 }
 
-void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every) {
+// FC 2 after a step, as pdfemDynamicSolver_CSRformat does (pdsolve.cpp:6014-6016,
+// 6060-6064): nodal stresses, then the reference's maximum-principal-stress
+// criterion with the command file's Top-K
+void maxprisig_failure(datModel& d, pdsolve& sol) {
+  bool addLoad = true;
+  sol.calGlobalNodeStresses(d);
+  sol.failureCriterion_maxPriSig(d, d.ci_topk, addLoad);
+}
+
+void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every, bool fc2 = false) {
   if (s0 > 0) set_stretch_threshold(d, s0);
   int neq = num_eq(d);
   int nsteps = d.getnumTstep();
@@ -281,6 +291,7 @@ void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every) 
   matoperat.matAdd(Vu_np1, Vu_n, Vu_np1);
   sol.storeDisplacementResult(d, Vu_np1);
   if (s0 > 0) stretch_failure(d, sol);
+  if (fc2) maxprisig_failure(d, sol);
   std::vector<double> traj;
   std::vector<long long> traj_steps;
   auto snap = [&](int n) {
@@ -301,8 +312,9 @@ void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every) 
     MPI_Allreduce(sol.cdp_F, sol.cdp_FGlo, neq, MPI_DOUBLE, MPI_SUM, MPI_COMM_WORLD);
     sol.timeIntegration_LM(d, Vu_n, Vu_nm1, Vu_np1, neq);
     sol.storeDisplacementResult(d, Vu_np1);
-    if (n == nsteps) sol.calGlobalNodeStresses(d);
+    if (n == nsteps && !fc2) sol.calGlobalNodeStresses(d);
     if (s0 > 0) stretch_failure(d, sol);
+    if (fc2) maxprisig_failure(d, sol);
     if (n % every == 0 || n == nsteps) snap(n);
   }
   sol.calLocalDamage(d);
@@ -459,6 +471,8 @@ int main(int argc, char** argv) {
     out.f64("F", std::vector<double>(sol.cdp_F, sol.cdp_F + neq));
   } else if (mode == "explicit") {
     run_explicit(dat, sol, out, std::atof(argv[4]), std::atoi(argv[5]));
+  } else if (mode == "explicit_fc2") {
+    run_explicit(dat, sol, out, 0.0, std::atoi(argv[4]), true);
   } else if (mode == "static") run_static(dat, sol, out);
   else if (mode == "newmark") run_newmark(dat, sol, out);
   else if (mode == "quasi") run_quasi(dat, sol, out);

@@ -42,6 +42,7 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
     if (D == 2 && q->mesh.protype != p0->mesh.protype) { err = {3, who + "mixed plane stress / strain"}; return false; }
     if (q->cmd.solver != 0 || q->cmd.newmark) { err = {3, who + "only explicit dynamic runs can be batched"}; return false; }
     if (q->cmd.fail_flag != p0->cmd.fail_flag) { err = {3, who + "failure criteria differ"}; return false; }
+    if (q->cmd.fail_flag == 2) { err = {3, who + "FC 2 runs on single models only"}; return false; }
     if (q->cmd.precision != p0->cmd.precision) { err = {3, who + "precisions differ"}; return false; }
     if (q->cmd.s0_pert != p0->cmd.s0_pert || q->cmd.s0_seed != p0->cmd.s0_seed) {
       err = {3, who + "per-bond draws (seed, perturbation) must agree"}; return false;

@@ -172,6 +172,27 @@ static pdx_status upload_model(pdx_model* m) {
   m->d_tmp_all = m->buf.alloc<double>((size_t)N * D);
   for (int i = 0; i < kEqTemps; i++) m->d_tmp_eq[i] = m->buf.alloc<double>((size_t)std::max(s.n_eq, 1));
   m->d_Kval = m->buf.alloc<double>((size_t)std::max<int64_t>((int64_t)s.csr_ja.size(), 1));
+  // FC 2 (2D explicit): the families of each block's nodes, in the block's
+  // node order, and room for one candidate per bond
+  m->fc2 = m->cmd.fail_flag == 2 && D == 2 && m->batch.empty() && v.n_fam > 0;
+  if (m->fc2) {
+    const int nbx = s.nblocks[0], nby = s.nblocks[1];
+    std::vector<int> bptr(1, 0), bfam;
+    for (int b = 0; b < nbx * nby; b++) {
+      if (b < (int)s.block_nodes.size())
+        for (int node : s.block_nodes[b])
+          if (s.fam_of_node[node] >= 0) bfam.push_back(s.fam_of_node[node]);
+      bptr.push_back((int)bfam.size());
+    }
+    if (bfam.empty()) bfam.push_back(0);
+    m->d_fc2_blk_ptr = upload(m, bptr);
+    m->d_fc2_blk_fam = upload(m, bfam);
+    m->fc2_cap = (int)std::max<int64_t>(v.n_bond, 1);
+    m->d_fc2_val = m->buf.alloc<double>(m->fc2_cap);
+    m->d_fc2_bond = m->buf.alloc<int>(m->fc2_cap);
+    m->d_fc2_fam = m->buf.alloc<int>(m->fc2_cap);
+    m->d_fc2_count = m->buf.alloc<int>(1);
+  }
   // coefficients
   CoeffArgs ca{};
   ca.dim = D;
@@ -245,6 +266,74 @@ pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool ph
   a.sigma = sigma ? m->d_sigma : nullptr;
   a.phi = phi ? m->d_phi : nullptr;
   return cuda_check(launch_stress(a, m->stream), "stress kernel");
+}
+
+// FC 2 pass on the state just stepped to (the reference calls
+// calGlobalNodeStresses and then failureProcess after every explicit step,
+// pdsolve.cpp:6014-6016, 6060-6064): nodal stresses, candidates, Top-K
+// selection, cuts.  Top-K (K > 0) selects on the host: the K largest sigma1,
+// ties by bond index.
+pdx_status fc2_pass(pdx_model* m) {
+  if (!m->fc2) return PDX_OK;
+  pdx_status st = model_stress(m, m->d_u[m->cur], true, false);
+  if (st) return st;
+  const Setup& s = m->setup;
+  Fc2Args a{};
+  a.v = m->view;
+  a.sigma = m->d_sigma;
+  a.sigult = m->mesh.sigult;
+  a.half_min_delta = 0.5 * s.min_delta;
+  a.lbc0 = s.lbc[0];
+  a.lbc1 = s.lbc[1];
+  a.block_size = s.block_size;
+  a.nbx = s.nblocks[0];
+  a.nby = s.nblocks[1];
+  a.blk_ptr = m->d_fc2_blk_ptr;
+  a.blk_fam = m->d_fc2_blk_fam;
+  a.brec = m->mixed ? m->d_brec : nullptr;
+  a.cand_val = m->d_fc2_val;
+  a.cand_bond = m->d_fc2_bond;
+  a.cand_fam = m->d_fc2_fam;
+  a.count = m->d_fc2_count;
+  a.cap = m->fc2_cap;
+  cudaMemsetAsync(a.count, 0, sizeof(int), m->stream);
+  st = cuda_check(launch_fc2_candidates(a, m->stream), "FC 2 candidates");
+  if (st) return st;
+  const int K = m->cmd.topk;
+  if (K > 0) {
+    int n = 0;
+    cudaMemcpyAsync(&n, a.count, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+    st = cuda_check(cudaStreamSynchronize(m->stream), "FC 2 count");
+    if (st) return st;
+    n = std::min(n, a.cap);
+    if (n > K) {
+      std::vector<double> val(n);
+      std::vector<int> bond(n), fam(n), order(n);
+      cudaMemcpyAsync(val.data(), a.cand_val, (size_t)n * 8, cudaMemcpyDeviceToHost, m->stream);
+      cudaMemcpyAsync(bond.data(), a.cand_bond, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream);
+      cudaMemcpyAsync(fam.data(), a.cand_fam, (size_t)n * 4, cudaMemcpyDeviceToHost, m->stream);
+      st = cuda_check(cudaStreamSynchronize(m->stream), "FC 2 candidates");
+      if (st) return st;
+      for (int i = 0; i < n; i++) order[i] = i;
+      std::partial_sort(order.begin(), order.begin() + K, order.end(), [&](int x, int y) {
+        return val[x] != val[y] ? val[x] > val[y] : bond[x] < bond[y];
+      });
+      std::vector<double> v2(K);
+      std::vector<int> b2(K), f2(K);
+      for (int i = 0; i < K; i++) {
+        v2[i] = val[order[i]];
+        b2[i] = bond[order[i]];
+        f2[i] = fam[order[i]];
+      }
+      cudaMemcpyAsync(a.cand_val, v2.data(), (size_t)K * 8, cudaMemcpyHostToDevice, m->stream);
+      cudaMemcpyAsync(a.cand_bond, b2.data(), (size_t)K * 4, cudaMemcpyHostToDevice, m->stream);
+      cudaMemcpyAsync(a.cand_fam, f2.data(), (size_t)K * 4, cudaMemcpyHostToDevice, m->stream);
+      cudaMemcpyAsync(a.count, &K, sizeof(int), cudaMemcpyHostToDevice, m->stream);
+      st = cuda_check(cudaStreamSynchronize(m->stream), "FC 2 Top-K");
+      if (st) return st;
+    }
+  }
+  return cuda_check(launch_fc2_cut(a, m->stream), "FC 2 cuts");
 }
 
 static StepArgs step_args(pdx_model* m, int mode, int64_t step_index) {
@@ -747,7 +836,7 @@ static pdx_status build_graph(pdx_model* m, int gsteps) {
 }
 
 static pdx_status advance(pdx_model* m, int nsteps) {
-  const bool graphs = m->view.n_nbc == 0;
+  const bool graphs = m->view.n_nbc == 0 && !m->fc2;
   const int G = 64;
   int done = 0;
   pdx_status st = PDX_OK;
@@ -765,6 +854,8 @@ static pdx_status advance(pdx_model* m, int nsteps) {
       continue;
     }
     st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
+    if (st) return st;
+    st = fc2_pass(m);
     if (st) return st;
     m->steps_done++;
     done++;
@@ -809,6 +900,8 @@ pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double*
   if (m->mixed) launch_shadow(m->view, m->d_u[m->cur], m->d_uf[m->cur], m->stream);
   pdx_status st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
   if (st) return st;
+  st = fc2_pass(m);
+  if (st) return st;
   m->steps_done++;
   launch_gather_eq(m->view, m->d_u[m->cur], m->d_tmp_eq[2], m->stream);
   cudaMemcpyAsync(u_np1, m->d_tmp_eq[2], ne * 8, cudaMemcpyDeviceToHost, m->stream);
@@ -822,7 +915,8 @@ pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi
   const int N = m->mesh.n_node, D = m->mesh.dim;
   // the reference computes node stress before the step's failure pass and
   // damage after it (pdfemDynamicSolver_CSRformat :6060-6075)
-  pdx_status st = model_stress(m, m->d_u[m->cur], true, false);
+  // (with FC 2 the last pass computed the stresses before its cuts)
+  pdx_status st = m->fc2 && m->steps_done > 0 ? PDX_OK : model_stress(m, m->d_u[m->cur], true, false);
   if (st) return st;
   if (m->steps_done > 0 && m->view.fail3) st = explicit_step_launch(m, 2, m->steps_done);
   if (st) return st;

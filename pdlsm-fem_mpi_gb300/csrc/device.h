@@ -168,6 +168,26 @@ cudaError_t launch_scatter_eq(const DevView& v, const double* u_eq, double* u_al
 cudaError_t launch_gather_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s);
 cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStream_t s);
 cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s);
+
+// FC 2 (maximum principal stress, Top-K) bond breaking after an explicit step, 2D (k_fc2.cu)
+struct Fc2Args {
+  DevView v;
+  const double* sigma;      // n_node * 6 nodal stresses of the new state
+  double sigult;            // ultimate stress of the material
+  double half_min_delta;    // half-length of a cut segment: 0.5 * min(delta)
+  double lbc0, lbc1, block_size;   // the set-up's block grid
+  int nbx, nby;
+  const int* blk_ptr;       // nbx * nby + 1
+  const int* blk_fam;       // families of each block's nodes, in the block's node order
+  float4* brec;             // mixed-precision bond records (sign = state), or null
+  double* cand_val;         // candidates: sigma1, bond, family
+  int* cand_bond;
+  int* cand_fam;
+  int* count;               // number of candidates found (may exceed cap)
+  int cap;
+};
+cudaError_t launch_fc2_candidates(const Fc2Args& a, cudaStream_t s);
+cudaError_t launch_fc2_cut(const Fc2Args& a, cudaStream_t s);
 cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, double beta, double dt, cudaStream_t s);
 cudaError_t launch_shadow(const DevView& v, const double* u_all, float4* uf, cudaStream_t s);
 

@@ -233,10 +233,13 @@ extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
   cudaSetDevice(m->device);
   mkdir(results_dir, 0755);
   const std::string dir(results_dir);
-  if (m->cmd.fail_flag == 1 || m->cmd.fail_flag == 2) {
-    if (m->cmd.solver != 1)
-      return set_error(PDX_ERR_UNSUPPORTED, "failure criteria FC 1 / FC 2 are not implemented (FC 0 and FC 3 are)");
-  }
+  // FC 2 breaks bonds in explicit dynamic runs (after every step, as the
+  // reference does); FC 1, and FC 2 in the Newmark and quasi-static loops,
+  // are not built
+  const bool explicit_run = m->cmd.solver == 0 && !m->cmd.newmark;
+  if (m->cmd.solver != 1 && (m->cmd.fail_flag == 1 || (m->cmd.fail_flag == 2 && !explicit_run)))
+    return set_error(PDX_ERR_UNSUPPORTED,
+                     "failure criterion FC 1, and FC 2 outside explicit dynamics, are not implemented");
   switch (m->cmd.solver) {
     case 0: return m->cmd.newmark ? run_newmark(m, dir) : run_explicit(m, dir);
     case 1: return run_static(m, dir);

@@ -115,6 +115,15 @@ struct pdx_model {
   double* d_u[2] = {nullptr, nullptr};
   float4* d_uf[2] = {nullptr, nullptr};
   float4* d_brec = nullptr;          // mixed-precision bond records
+  // FC 2 bond breaking (2D explicit runs): block lists and candidate buffers
+  bool fc2 = false;
+  int* d_fc2_blk_ptr = nullptr;
+  int* d_fc2_blk_fam = nullptr;
+  double* d_fc2_val = nullptr;
+  int* d_fc2_bond = nullptr;
+  int* d_fc2_fam = nullptr;
+  int* d_fc2_count = nullptr;
+  int fc2_cap = 0;
   int ke_smem = 0;                   // floats of FE classes staged in shared memory
   uint32_t* d_state = nullptr;
   int* d_intact = nullptr;

@@ -8,7 +8,7 @@ The case inputs (.lis/.in) are copied here too, so the tests can rebuild the
 same models without the reference.
 
 Needs the reference tree (default /root/reference) and SciPy; it is run by
-hand, not by the tests:  python tests/golden/make_golden.py
+hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only]
 """
 from __future__ import annotations
 
@@ -148,5 +148,26 @@ def main() -> None:
     shutil.rmtree(work)
 
 
+def fc2_cases() -> None:
+    """FC 2 (maximum principal stress) on the 2D plate: sigma_ult = 3e7 Pa, all
+    candidates (Top-K 0) and the two largest per step (Top-K 2); 60 steps."""
+    work = tempfile.mkdtemp(prefix="golden_fc2_")
+    d2 = os.path.join(work, "p21")
+    for name, fc in (("p21_fc2", "2 0"), ("p21_fc2k", "2 2")):
+        m = plate_case()
+        m.sigult = 3e7
+        meshgen.write_case(m, d2, name, solver="DYNAMIC", dt=5e-8, nsteps=60, save=20, factor=3.015, nlf=1.0,
+                           fc=fc)
+    copy_inputs(d2, "p21")
+    save("p21_fc2", run(d2, "p21_fc2.in", "explicit_fc2", "20"))
+    save("p21_fc2k", run(d2, "p21_fc2k.in", "explicit_fc2", "20"))
+    shutil.rmtree(work)
+
+
 if __name__ == "__main__":
-    main()
+    if "--fc2-only" in sys.argv:
+        build_driver()
+        fc2_cases()
+    else:
+        main()
+        fc2_cases()

@@ -268,3 +268,40 @@ def test_quasi_static_increments_match_reference(built, method):
             errs.append(np.linalg.norm(d) / scale)
     print(f"\nmethod {method}: relative L2 error per increment {['%.1e' % e for e in errs]}")
     assert max(errs) < 1e-6
+
+
+@pytest.mark.parametrize("cmd", ["p21_fc2", "p21_fc2k"])
+def test_fc2_principal_stress_breaking_matches_reference(built, cmd):
+    """FC 2 after every explicit step (sigma_ult 3e7, Top-K 0 and 2) against the
+    reference's own run: trajectory, broken-bond set, damage and stresses."""
+    g = golden(cmd)
+    steps = list(g["u_traj_steps"])
+    with pdx.Model(case_cmd("p21", cmd), device=0, precision=0) as m:
+        m.explicit_init()
+        done, worst = 0, 0.0
+        for i, s in enumerate(steps):
+            m.explicit_advance(s + 1 - done)
+            done = s + 1
+            u, sig, phi, bs = m.state()
+            worst = max(worst, rel(u, g["u_traj"][i]))
+    broken = int((g["bond_state_final"] == 0).sum())
+    print(f"\n[{cmd}] FP64: worst displacement error {worst:.2e}, {broken} broken bonds in the reference, "
+          f"{int((bs != g['bond_state_final']).sum())} differences")
+    np.testing.assert_array_equal(bs, g["bond_state_final"])
+    assert worst < FP64_TOL
+    np.testing.assert_allclose(phi, g["phi_final"], rtol=0, atol=1e-15)
+    assert rel(sig, g["sigma_final"]) < FP64_TOL
+
+
+def test_fc2_mixed_precision_error_is_stated(built):
+    g = golden("p21_fc2")
+    with pdx.Model(case_cmd("p21", "p21_fc2"), device=0, precision=1) as m:
+        m.explicit_init()
+        m.explicit_advance(int(g["u_traj_steps"][-1]) + 1)
+        u, sig, phi, bs = m.state()
+    err = rel(u, g["u_traj"][-1])
+    nb_diff = int((bs != g["bond_state_final"]).sum())
+    print(f"\n[p21_fc2] mixed precision: displacement rel L2 error {err:.3e}, {nb_diff} bond-state differences "
+          f"of {int((g['bond_state_final'] == 0).sum())} broken")
+    assert err < 1e-3
+    assert nb_diff <= max(4, int(0.02 * (g["bond_state_final"] == 0).sum()))

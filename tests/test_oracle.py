@@ -116,3 +116,13 @@ def test_bond_uniform_is_uniform(built):
     u = np.array([orc.lib().orc_bond_uniform(5, k, m) for k in range(60) for m in range(60)])
     assert 0 <= u.min() and u.max() < 1
     assert abs(u.mean() - 0.5) < 0.02
+
+
+def test_fc2_fixtures_break_bonds():
+    """The FC 2 fixtures (the reference's own runs) break bonds beyond the
+    pre-crack, and Top-K 2 breaks fewer than Top-K 0."""
+    all_k = golden("p21_fc2")["bond_state_final"]
+    top2 = golden("p21_fc2k")["bond_state_final"]
+    pre = golden("p21_explicit")["bond_state_final"]
+    assert (all_k == 0).sum() > (top2 == 0).sum() > 144
+    assert all_k.shape == top2.shape == pre.shape
