@@ -107,10 +107,12 @@ pdx_status pdx_internal_force(pdx_model* m, const double* u_all, double* f_eq);
 
 /* Explicit central-difference solve (pdfemDynamicSolver_CSRformat,
  * pdsolve.cpp:5842-6090, lumped mass) with critical-stretch bond breaking
- * (FC 3).  pdx_explicit_init resets the state to the mesh's initial values and
- * the pre-crack bond states; pdx_explicit_advance runs n steps on the device
- * (the first call runs step 0, u1 = u0 + dt^2/2 a0).  Steps are launched as a
- * CUDA graph; no host synchronisation inside. */
+ * (FC 3) or maximum-principal-stress breaking with Top-K after every step
+ * (FC 2, 2D).  pdx_explicit_init resets the state to the mesh's initial values
+ * and the pre-crack bond states; pdx_explicit_advance runs n steps on the
+ * device (the first call runs step 0, u1 = u0 + dt^2/2 a0).  Steps are
+ * launched as CUDA graphs when no natural BC, FC 2 or RF output needs
+ * per-step work; FC 2 with Top-K > 0 reads the candidate count on the host. */
 pdx_status pdx_explicit_init(pdx_model* m);
 pdx_status pdx_explicit_advance(pdx_model* m, int nsteps);
 /* Same as advance, timed with CUDA events on the model's stream (ms). */
@@ -120,6 +122,14 @@ pdx_status pdx_explicit_advance_timed(pdx_model* m, int nsteps, double* ms);
  * prescribed values and bond states are the model's.  Copies are inside. */
 pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1);
 int64_t pdx_explicit_step_count(const pdx_model* m);
+/* Reaction forces of the RF keyword's essential BCs, one row per recorded
+ * step as calReacForc writes them (pdsolve.cpp:5347-5404): (U, RFx, RFy,
+ * RFz) with U the first RF EBC's current value and RF the sum of Ke u_e over
+ * the elements touching the RF nodes, taken at those nodes.  Rows are
+ * indexed by step: explicit runs record steps 0..n, quasi-static increments
+ * and Newmark steps 1..n (row 0 stays zero).  *count = rows recorded; rows
+ * (max_rows x 4) may be NULL. */
+pdx_status pdx_reaction_forces(const pdx_model* m, double* rows, int64_t max_rows, int64_t* count);
 
 /* Current state: u_all (N*d), node stress sigma (N*6, slots xx yy zz xy yz zx as
  * calGlobalNodeStresses pdsolve.cpp:9540-9604), damage phi (N, calLocalDamage

@@ -292,6 +292,16 @@ void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every, 
   sol.storeDisplacementResult(d, Vu_np1);
   if (s0 > 0) stretch_failure(d, sol);
   if (fc2) maxprisig_failure(d, sol);
+  // reaction forces (RF keyword) through the reference's own calReacForc,
+  // written at full precision and read back at the end
+  const bool rf = !d.civ_reacForceOfessBCId.empty();
+  const std::string rf_path = out.dir + "/rf.txt";
+  std::ofstream rf_out;
+  if (rf) {
+    rf_out.open(rf_path);
+    rf_out << std::setprecision(17);
+    sol.calReacForc(d, rf_out, 0);
+  }
   std::vector<double> traj;
   std::vector<long long> traj_steps;
   auto snap = [&](int n) {
@@ -315,7 +325,16 @@ void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every, 
     if (n == nsteps && !fc2) sol.calGlobalNodeStresses(d);
     if (s0 > 0) stretch_failure(d, sol);
     if (fc2) maxprisig_failure(d, sol);
+    if (rf) sol.calReacForc(d, rf_out, n);
     if (n % every == 0 || n == nsteps) snap(n);
+  }
+  if (rf) {
+    rf_out.close();
+    std::ifstream in(rf_path);
+    std::vector<double> rows;
+    double v;
+    while (in >> v) rows.push_back(v);
+    out.f64("rf_rows", rows, {(long long)(rows.size() / 5), 5});
   }
   sol.calLocalDamage(d);
   long long ns = (long long)traj_steps.size();

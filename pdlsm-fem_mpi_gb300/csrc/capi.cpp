@@ -193,6 +193,50 @@ static pdx_status upload_model(pdx_model* m) {
     m->d_fc2_fam = m->buf.alloc<int>(m->fc2_cap);
     m->d_fc2_count = m->buf.alloc<int>(1);
   }
+  // reaction forces (setReacForcNode, datModel.cpp:664-735): the nodes of the
+  // RF essential BCs, every element with one of them (in element order) with
+  // its stiffness, and a mask of its RF nodes
+  if (!m->cmd.rf_ids.empty() && m->batch.empty()) {
+    std::vector<int> rfn;
+    for (int id : m->cmd.rf_ids)
+      if (id >= 0 && id < (int)me.ebcs.size()) rfn.insert(rfn.end(), me.ebcs[id].nodes.begin(), me.ebcs[id].nodes.end());
+    std::sort(rfn.begin(), rfn.end());
+    rfn.erase(std::unique(rfn.begin(), rfn.end()), rfn.end());
+    const int nen = D == 2 ? 4 : 8, nd = nen * D;
+    std::vector<int> conn, mask;
+    std::vector<double> ke;
+    for (int e = 0; e < me.n_elem && !rfn.empty(); e++) {
+      int mk = 0;
+      for (int a = 0; a < me.elem_nn[e]; a++)
+        if (std::binary_search(rfn.begin(), rfn.end(), me.conn[(size_t)e * 8 + a])) mk |= 1 << a;
+      if (!mk || me.elem_nn[e] != nen) continue;
+      double xN[8][3];
+      for (int a = 0; a < nen; a++) {
+        const int node = me.conn[(size_t)e * 8 + a];
+        conn.push_back(node);
+        for (int c = 0; c < 3; c++) xN[a][c] = me.X[(size_t)node * 3 + c];
+      }
+      std::vector<double> K((size_t)nd * nd);
+      if (D == 2) ke_quad4(xN, p.D.data(), K.data());
+      else ke_hex8(xN, p.D.data(), K.data());
+      ke.insert(ke.end(), K.begin(), K.end());
+      mask.push_back(mk);
+    }
+    m->rf_n_el = (int)mask.size();
+    const int id0 = m->cmd.rf_ids[0];
+    if (id0 >= 0 && id0 < (int)me.ebcs.size() && !me.ebcs[id0].nodes.empty())
+      m->rf_uc_index = (int64_t)me.ebcs[id0].nodes[0] * D + me.ebcs[id0].dof;
+    m->rf = true;
+    m->rf_cap = (int64_t)m->cmd.nsteps + 2;
+    m->d_rf_hist = m->buf.alloc<double>((size_t)m->rf_cap * 4);
+    cudaMemsetAsync(m->d_rf_hist, 0, (size_t)m->rf_cap * 4 * 8, m->stream);
+    if (m->rf_n_el > 0) {
+      m->d_rf_conn = upload(m, conn);
+      m->d_rf_ke = upload(m, ke);
+      m->d_rf_mask = upload(m, mask);
+      m->d_rf_part = m->buf.alloc<double>((size_t)m->rf_n_el * nen * 3);
+    }
+  }
   // coefficients
   CoeffArgs ca{};
   ca.dim = D;
@@ -266,6 +310,23 @@ pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool ph
   a.sigma = sigma ? m->d_sigma : nullptr;
   a.phi = phi ? m->d_phi : nullptr;
   return cuda_check(launch_stress(a, m->stream), "stress kernel");
+}
+
+// Reaction-force row `row` of the current state (calReacForc, pdsolve.cpp:5347-5404).
+pdx_status rf_record(pdx_model* m, int64_t row) {
+  if (!m->rf || row < 0 || row >= m->rf_cap) return PDX_OK;
+  m->rf_rows = std::max(m->rf_rows, row + 1);
+  double* h = m->d_rf_hist + row * 4;
+  if (m->rf_n_el == 0) {
+    cudaMemsetAsync(h, 0, 4 * 8, m->stream);
+    if (m->rf_uc_index >= 0)
+      cudaMemcpyAsync(h, m->d_u[m->cur] + m->rf_uc_index, 8, cudaMemcpyDeviceToDevice, m->stream);
+    return cuda_check(cudaGetLastError(), "reaction forces");
+  }
+  const int nen = m->mesh.dim == 2 ? 4 : 8;
+  return cuda_check(launch_reaction(m->rf_n_el, nen, m->mesh.dim, m->d_rf_conn, m->d_rf_ke, m->d_rf_mask,
+                                    m->d_u[m->cur], m->rf_uc_index, m->d_rf_part, h, m->stream),
+                    "reaction forces");
 }
 
 // FC 2 pass on the state just stepped to (the reference calls
@@ -754,6 +815,7 @@ static pdx_status explicit_reset(pdx_model* m) {
   }
   m->cur = 0;
   m->steps_done = 0;
+  m->rf_rows = 0;
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit init");
 }
 
@@ -836,7 +898,7 @@ static pdx_status build_graph(pdx_model* m, int gsteps) {
 }
 
 static pdx_status advance(pdx_model* m, int nsteps) {
-  const bool graphs = m->view.n_nbc == 0 && !m->fc2;
+  const bool graphs = m->view.n_nbc == 0 && !m->fc2 && !m->rf;
   const int G = 64;
   int done = 0;
   pdx_status st = PDX_OK;
@@ -856,6 +918,7 @@ static pdx_status advance(pdx_model* m, int nsteps) {
     st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
     if (st) return st;
     st = fc2_pass(m);
+    if (!st) st = rf_record(m, m->steps_done);
     if (st) return st;
     m->steps_done++;
     done++;
@@ -901,6 +964,7 @@ pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double*
   pdx_status st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
   if (st) return st;
   st = fc2_pass(m);
+  if (!st) st = rf_record(m, m->steps_done);
   if (st) return st;
   m->steps_done++;
   launch_gather_eq(m->view, m->d_u[m->cur], m->d_tmp_eq[2], m->stream);
@@ -909,6 +973,17 @@ pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double*
 }
 
 int64_t pdx_explicit_step_count(const pdx_model* m) { return m ? m->steps_done : -1; }
+
+pdx_status pdx_reaction_forces(const pdx_model* m, double* rows, int64_t max_rows, int64_t* count) {
+  if (!m) return set_error(PDX_ERR_INVALID, "null model");
+  const int64_t n = m->rf ? m->rf_rows : 0;
+  if (count) *count = n;
+  if (!rows || n == 0 || max_rows <= 0) return PDX_OK;
+  if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
+  cudaSetDevice(m->device);
+  cudaMemcpyAsync(rows, m->d_rf_hist, (size_t)std::min(n, max_rows) * 4 * 8, cudaMemcpyDeviceToHost, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "reaction forces");
+}
 
 pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi, uint8_t* bond_state) {
   NEED_DEVICE(m);

@@ -186,6 +186,11 @@ struct Fc2Args {
   int* count;               // number of candidates found (may exceed cap)
   int cap;
 };
+// reaction forces of one step (k_post.cu): Fe = Ke u_e over the elements
+// touching the RF nodes, summed over those nodes in element order;
+// hist_row = (uc, RFx, RFy, RFz), uc = u_all[uc_index] (0 if uc_index < 0)
+cudaError_t launch_reaction(int n_el, int nen, int dim, const int* conn, const double* ke, const int* mask,
+                            const double* u_all, int64_t uc_index, double* part, double* hist_row, cudaStream_t s);
 cudaError_t launch_fc2_candidates(const Fc2Args& a, cudaStream_t s);
 cudaError_t launch_fc2_cut(const Fc2Args& a, cudaStream_t s);
 cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, double beta, double dt, cudaStream_t s);

@@ -7,6 +7,8 @@
 // The direct sparse solves of the reference become Krylov solves judged by
 // the true FP64 residual (SOLVE keyword; default BiCGStab, tolerance 1e-8).
 #include <cstdio>
+#include <fstream>
+#include <iomanip>
 #include <string>
 #include <sys/stat.h>
 #include <vector>
@@ -63,12 +65,30 @@ pdx_status solve_device(pdx_model* m, const double* b, double* x, KrylovResult* 
   return solve_device_method(m, b, x, m->cmd.solve_method, kr);
 }
 
+// <title>RF.out: the header and one row per recorded step, formatted as the
+// reference's stream is (default 6 significant digits in the dynamic
+// solvers, scientific with 4 digits in the quasi-static one)
+pdx_status write_rf(pdx_model* m, const std::string& dir, int first_row, bool scientific4) {
+  std::ofstream f(dir + "/" + m->mesh.title + "RF.out");
+  if (!f) return set_error(PDX_ERR_IO, "cannot write " + m->mesh.title + "RF.out");
+  if (scientific4) f << std::left << std::scientific << std::setprecision(4);
+  f << "Step\t" << "U\t" << "RFx\t" << "RFy\t" << "RFz\n";
+  int64_t n = 0;
+  pdx_status st = pdx_reaction_forces(m, nullptr, 0, &n);
+  if (st || n == 0) return st;
+  std::vector<double> rows((size_t)n * 4);
+  st = pdx_reaction_forces(m, rows.data(), n, nullptr);
+  if (st) return st;
+  for (int64_t r = first_row; r < n; r++)
+    f << r << "\t" << rows[r * 4] << "\t" << rows[r * 4 + 1] << "\t" << rows[r * 4 + 2] << "\t" << rows[r * 4 + 3]
+      << std::endl;
+  return PDX_OK;
+}
+
 pdx_status run_explicit(pdx_model* m, const std::string& dir) {
   if (!m->cmd.lumped) return set_error(PDX_ERR_UNSUPPORTED, "explicit dynamics needs LUMPMASS ON");
   pdx_status st = pdx_explicit_init(m);
   if (st) return st;
-  FILE* rf = std::fopen((dir + "/" + m->mesh.title + "RF.out").c_str(), "w");
-  if (rf) { std::fprintf(rf, "Step\tU\tRFx\tRFy\tRFz\n"); std::fclose(rf); }
   st = pdx_explicit_advance(m, 1);   // step 0: u1 = u0 + dt^2/2 a0
   if (st) return st;
   const int nsteps = m->cmd.nsteps, save = std::max(1, m->cmd.save_freq);
@@ -85,7 +105,7 @@ pdx_status run_explicit(pdx_model* m, const std::string& dir) {
     if (st) return st;
     write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
   }
-  return PDX_OK;
+  return write_rf(m, dir, 0, false);
 }
 
 pdx_status run_static(pdx_model* m, const std::string& dir) {
@@ -166,6 +186,7 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
   for (int n = 1; n <= m->cmd.nsteps; n++) {
     KrylovResult kr;
     st = quasi_increment(m, n, m->cmd.solve_method, &kr, nullptr);
+    if (!st) st = rf_record(m, n);
     if (st) return st;
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps || n == 1) {
       HostState h;
@@ -175,7 +196,9 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
     }
     launch_advance_prescribed_quasi(m->view, u_all, m->stream);
   }
-  return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
+  st = cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
+  if (st) return st;
+  return write_rf(m, dir, 1, true);
 }
 
 pdx_status run_newmark(pdx_model* m, const std::string& dir) {
@@ -207,6 +230,8 @@ pdx_status run_newmark(pdx_model* m, const std::string& dir) {
     launch_advance_prescribed(m->view, u_all, m->stream);
     std::swap(acc, acc1);
     m->steps_done = n;
+    st = rf_record(m, n);
+    if (st) return st;
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps) {
       st = model_stress(m, u_all, true, true);
       if (st) return st;
@@ -216,7 +241,9 @@ pdx_status run_newmark(pdx_model* m, const std::string& dir) {
       write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
     }
   }
-  return cuda_check(cudaStreamSynchronize(m->stream), "Newmark");
+  st = cuda_check(cudaStreamSynchronize(m->stream), "Newmark");
+  if (st) return st;
+  return write_rf(m, dir, 1, false);
 }
 
 }  // namespace
@@ -271,6 +298,7 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   KrylovResult kr;
   float ms = 0.f;
   pdx_status st = quasi_increment(m, (int)m->steps_done + 1, method, &kr, &ms);
+  if (!st) st = rf_record(m, m->steps_done);
   if (info) {
     info->iterations = kr.iterations;
     info->rel_residual = kr.rel_residual;

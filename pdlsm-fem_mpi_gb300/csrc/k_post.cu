@@ -404,6 +404,50 @@ cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStrea
   return cudaGetLastError();
 }
 
+// Reaction force of one step, as calReacForc (pdsolve.cpp:5347-5404): for
+// every element touching an RF node, Fe = Ke u_e (u_e = all DOF values of its
+// nodes); the entries of its RF nodes are summed over the elements in order.
+// Non-fused products and sums in the reference's order.
+__global__ void k_reaction(int n_el, int nen, int dim, const int* conn, const double* ke, const int* mask,
+                           const double* u_all, int64_t uc_index, double* part, double* hist_row) {
+  const int nd = nen * dim;
+  // part[(e * nen + a) * 3 + j] = Fe of RF node a, DOF j of element e
+  for (int e = threadIdx.x; e < n_el; e += blockDim.x) {
+    const double* K = ke + (int64_t)e * nd * nd;
+    for (int a = 0; a < nen; a++) {
+      if (!((mask[e] >> a) & 1)) continue;
+      for (int j = 0; j < dim; j++) {
+        const int r = a * dim + j;
+        double acc = 0.0;
+        for (int c = 0; c < nd; c++) {
+          const int node = conn[(int64_t)e * nen + c / dim];
+          acc = __dadd_rn(acc, __dmul_rn(K[(int64_t)r * nd + c], u_all[(int64_t)node * dim + c % dim]));
+        }
+        part[((int64_t)e * nen + a) * 3 + j] = acc;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[3] = {0, 0, 0};
+    for (int e = 0; e < n_el; e++)
+      for (int a = 0; a < nen; a++) {
+        if (!((mask[e] >> a) & 1)) continue;
+        for (int j = 0; j < dim; j++) t[j] = __dadd_rn(t[j], part[((int64_t)e * nen + a) * 3 + j]);
+      }
+    hist_row[0] = uc_index >= 0 ? u_all[uc_index] : 0.0;
+    hist_row[1] = t[0];
+    hist_row[2] = t[1];
+    hist_row[3] = t[2];
+  }
+}
+
+cudaError_t launch_reaction(int n_el, int nen, int dim, const int* conn, const double* ke, const int* mask,
+                            const double* u_all, int64_t uc_index, double* part, double* hist_row, cudaStream_t s) {
+  k_reaction<<<1, 256, 0, s>>>(n_el, nen, dim, conn, ke, mask, u_all, uc_index, part, hist_row);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s) {
   const int64_t n = (int64_t)v.n_node * v.dim;
   const int blocks = (int)((n + 255) / 256);

@@ -465,6 +465,7 @@ pdx_status pdx_newmark_init(pdx_model* m) {
   cudaMemsetAsync(m->d_acc, 0, ne * 8, m->stream);
   m->cur = 0;
   m->steps_done = 0;
+  m->rf_rows = 0;
   m->newmark_ready = true;
   return cuda_check(cudaStreamSynchronize(m->stream), "Newmark init");
 }
@@ -529,6 +530,8 @@ pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_inf
   launch_advance_prescribed(m->view, u_all, m->stream);
   cudaMemcpyAsync(m->d_acc, acc1, (size_t)ne * 8, cudaMemcpyDeviceToDevice, m->stream);
   m->steps_done = n;
+  pdx_status rs = rf_record(m, n);
+  if (rs) return rs;
   return cuda_check(cudaStreamSynchronize(m->stream), "Newmark step");
 }
 

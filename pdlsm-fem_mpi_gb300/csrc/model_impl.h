@@ -115,6 +115,18 @@ struct pdx_model {
   double* d_u[2] = {nullptr, nullptr};
   float4* d_uf[2] = {nullptr, nullptr};
   float4* d_brec = nullptr;          // mixed-precision bond records
+  // reaction forces (RF keyword): the elements touching the RF nodes, their
+  // stiffness and RF-node masks, and one history row (uc, RFx, RFy, RFz) per step
+  bool rf = false;
+  int rf_n_el = 0;
+  int64_t rf_uc_index = -1;          // u_all index of the first RF EBC's DOF, or -1
+  int* d_rf_conn = nullptr;
+  double* d_rf_ke = nullptr;
+  int* d_rf_mask = nullptr;
+  double* d_rf_part = nullptr;
+  double* d_rf_hist = nullptr;
+  int64_t rf_cap = 0;
+  int64_t rf_rows = 0;               // rows written so far (highest row + 1)
   // FC 2 bond breaking (2D explicit runs): block lists and candidate buffers
   bool fc2 = false;
   int* d_fc2_blk_ptr = nullptr;
@@ -170,6 +182,7 @@ pdx_status cuda_check(cudaError_t e, const char* what);
 void write_vtk(const pdx_model* m, const std::string& path, const std::vector<double>& u_all,
                const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);
 pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi);
+pdx_status rf_record(pdx_model* m, int64_t row);
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);

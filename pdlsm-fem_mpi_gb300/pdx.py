@@ -56,7 +56,7 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
             "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad", "pdx_learned_probe",
             "pdx_learned_pairs", "pdx_learned_options", "pdx_learned_active",
-            "pdx_quasi_init", "pdx_quasi_step"]
+            "pdx_quasi_init", "pdx_quasi_step", "pdx_reaction_forces"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
                        ("pdx_learned_probe", [_P, C.c_int, C.c_uint64]),
                        ("pdx_learned_options", [_P, C.c_int, C.c_int]),
                        ("pdx_quasi_init", [_P]),
+                       ("pdx_reaction_forces", [_P, _D, C.c_int64, C.POINTER(C.c_int64)]),
                        ("pdx_quasi_step", [_P, C.c_int, C.POINTER(SolveInfo)]),
                        ("pdx_learned_pairs", [_P, _F, _F, C.POINTER(C.c_int64), C.POINTER(C.c_int)])):
         getattr(L, name).argtypes = args
@@ -172,6 +173,15 @@ class Model:
         _check(L.pdx_model_get_info(h, C.byref(inf)))
         self.info = inf
         return self
+
+    def reaction_forces(self) -> np.ndarray:
+        """Rows (U, RFx, RFy, RFz) per recorded step (RF keyword), shape (count, 4)."""
+        n = C.c_int64()
+        _check(lib().pdx_reaction_forces(self._h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 4))
+        if n.value:
+            _check(lib().pdx_reaction_forces(self._h, out.ctypes.data_as(_D), n.value, None))
+        return out
 
     # ---- quasi-static increments ----
     def quasi_init(self) -> None:

@@ -8,7 +8,7 @@ The case inputs (.lis/.in) are copied here too, so the tests can rebuild the
 same models without the reference.
 
 Needs the reference tree (default /root/reference) and SciPy; it is run by
-hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only]
+hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only]
 """
 from __future__ import annotations
 
@@ -164,10 +164,26 @@ def fc2_cases() -> None:
     shutil.rmtree(work)
 
 
+def rf_cases() -> None:
+    """Reaction forces (RF 2: the top edge's essential BC) of the 2D plate over
+    60 explicit steps, no failure criterion."""
+    work = tempfile.mkdtemp(prefix="golden_rf_")
+    d2 = os.path.join(work, "p21")
+    meshgen.write_case(plate_case(), d2, "p21_rf", solver="DYNAMIC", dt=5e-8, nsteps=60, save=20, factor=3.015,
+                       nlf=1.0, extra=["RF 2"])
+    copy_inputs(d2, "p21")
+    save("p21_rf", run(d2, "p21_rf.in", "explicit", "0", "20"))
+    shutil.rmtree(work)
+
+
 if __name__ == "__main__":
-    if "--fc2-only" in sys.argv:
+    if "--fc2-only" in sys.argv or "--rf-only" in sys.argv:
         build_driver()
-        fc2_cases()
+        if "--fc2-only" in sys.argv:
+            fc2_cases()
+        if "--rf-only" in sys.argv:
+            rf_cases()
     else:
         main()
         fc2_cases()
+        rf_cases()

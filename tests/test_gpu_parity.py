@@ -305,3 +305,23 @@ def test_fc2_mixed_precision_error_is_stated(built):
           f"of {int((g['bond_state_final'] == 0).sum())} broken")
     assert err < 1e-3
     assert nb_diff <= max(4, int(0.02 * (g["bond_state_final"] == 0).sum()))
+
+
+def test_reaction_forces_match_reference(built, tmp_path):
+    """RF 2 (the top edge): the per-step rows (U, RFx, RFy, RFz) of 61 explicit
+    steps against the reference's calReacForc, through the API and in the
+    RF.out file pdx_run writes."""
+    g = golden("p21_rf")["rf_rows"]
+    scale = np.abs(g[:, 2:5]).max()
+    with pdx.Model(case_cmd("p21", "p21_rf"), device=0, precision=0) as m:
+        m.explicit_init()
+        m.explicit_advance(61)
+        rows = m.reaction_forces()
+        assert rows.shape == (61, 4)
+        np.testing.assert_allclose(rows[:, 0], g[:, 1], rtol=1e-14, atol=0)
+        assert np.abs(rows[:, 1:4] - g[:, 2:5]).max() <= 1e-10 * scale
+        m.run(str(tmp_path))
+    lines = open(tmp_path / "p21RF.out").read().splitlines()
+    assert lines[0] == "Step\tU\tRFx\tRFy\tRFz" and len(lines) == 62
+    last = [float(t) for t in lines[-1].split("\t")]
+    assert last[0] == 60 and abs(last[3] - g[-1, 3]) <= 1e-5 * abs(g[-1, 3])
