@@ -23,9 +23,12 @@ void append(std::vector<T>& dst, const std::vector<T>& src) {
 }
 
 // dst += src + off for entries >= 0, negative entries kept
+// (capacity grows geometrically: reserving the exact size on every append
+// would copy the whole array once per specimen)
 template <typename T, typename O>
 void append_off(std::vector<T>& dst, const std::vector<T>& src, O off) {
-  dst.reserve(dst.size() + src.size());
+  const size_t need = dst.size() + src.size();
+  if (dst.capacity() < need) dst.reserve(std::max(need, 2 * dst.capacity()));
   for (const T& x : src) dst.push_back(x >= 0 ? (T)(x + off) : x);
 }
 
@@ -66,14 +69,15 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
   P.fam_ptr.push_back(0);
   P.fe_adj_ptr.push_back(0);
   S.fam_off.push_back(0);
-  S.csr_ia.push_back(0);
+  // no CSR pattern or scatter maps: a batch runs explicit steps only (the
+  // assembly entry points refuse batched models)
   out->batch.clear();
   out->coeff_segs.clear();
   out->mat_D.clear();
   out->mat_nu.clear();
   out->node_mat.clear();
   int64_t node_off = 0, elem_off = 0, fam_off = 0, bond_off = 0, eq_off = 0, member_off = 0, fe_off = 0;
-  int64_t cls_off = 0, st_off = 0, corr_off = 0, wd_off = 0, nnz_off = 0, adj_off = 0, dcls_off = 0;
+  int64_t cls_off = 0, st_off = 0, corr_off = 0, wd_off = 0, adj_off = 0, dcls_off = 0;
   bool all_delta = true;
   const int NV = D == 2 ? 3 : 6;
   for (size_t i = 0; i < parts.size(); i++) {
@@ -119,8 +123,6 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
     append(S.fam_delta, s.fam_delta);
     append(S.fam_cdv, s.fam_cdv);
     append(S.bond_state, s.bond_state);
-    for (size_t r = 1; r < s.csr_ia.size(); r++) S.csr_ia.push_back(s.csr_ia[r] + nnz_off);
-    append_off(S.csr_ja, s.csr_ja, eq_off);
     // prepared arrays
     append(P.mass_node, p.mass_node);
     append(P.mass_eq, p.mass_eq);
@@ -175,9 +177,6 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
       P.st_dcls.insert(P.st_dcls.end(), p.feonly.size(), -1);
       if (p.n_st_cls > 0) all_delta = false;
     }
-    append(P.rel_bond, p.rel_bond);
-    append(P.rel_self, p.rel_self);
-    append(P.rel_fe, p.rel_fe);
     if (i == 0) { P.D = p.D; P.lambda = p.lambda; P.mu = p.mu; }
     // offsets
     node_off += m.n_node;
@@ -191,7 +190,6 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
     st_off += p.n_st_cls;
     corr_off += p.n_corr;
     wd_off += (int64_t)(p.wd.size() / ((size_t)D * NV));
-    nnz_off += (int64_t)s.csr_ja.size();
     adj_off += (int64_t)p.fe_adj.size();
     if (node_off > INT32_MAX || bond_off > INT32_MAX || (fe_off << 3) > INT32_MAX) {
       err = {3, "batch too large for 32-bit node, bond or element indices"};

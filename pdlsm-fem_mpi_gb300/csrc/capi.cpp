@@ -151,12 +151,14 @@ static pdx_status upload_model(pdx_model* m) {
   m->d_bgp = upload(m, p.bgp);
   m->d_L = upload(m, p.L);
   m->d_fam_cdv = upload(m, s.fam_cdv);
-  m->d_ia = upload(m, s.csr_ia);
-  std::vector<int> ja32(s.csr_ja.begin(), s.csr_ja.end());
-  m->d_ja = upload(m, ja32);
-  m->d_rel_bond = upload(m, p.rel_bond);
-  m->d_rel_self = upload(m, p.rel_self);
-  m->d_rel_fe = upload(m, p.rel_fe);
+  if (!s.csr_ia.empty()) {   // (batched models have no CSR pattern)
+    m->d_ia = upload(m, s.csr_ia);
+    std::vector<int> ja32(s.csr_ja.begin(), s.csr_ja.end());
+    m->d_ja = upload(m, ja32);
+    m->d_rel_bond = upload(m, p.rel_bond);
+    m->d_rel_self = upload(m, p.rel_self);
+    m->d_rel_fe = upload(m, p.rel_fe);
+  }
   for (int i = 0; i < 2; i++) {
     m->d_u[i] = m->buf.alloc<double>((size_t)N * D);
     m->d_uf[i] = m->buf.alloc<float4>((size_t)2 * N);
@@ -489,8 +491,21 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
   if (opts) o = *opts;
   pdx_model* m = new pdx_model();
   Error err{0, ""};
-  if (!read_command(cmd_path, m->cmd, m->mesh, m->base_dir, err) || !build_setup(m->mesh, m->cmd, m->setup, err) ||
-      !prepare_model(m, err)) {
+  // verbose > 1 reports the host set-up phases on stderr
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
+  bool ok = read_command(cmd_path, m->cmd, m->mesh, m->base_dir, err);
+  const auto t1 = clk::now();
+  ok = ok && build_setup(m->mesh, m->cmd, m->setup, err);
+  const auto t2 = clk::now();
+  ok = ok && prepare_model(m, err);
+  const auto t3 = clk::now();
+  if (o.verbose > 1) {
+    auto sec = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    std::fprintf(stderr, "pdx: set-up %s: read %.3f s, build_setup %.3f s, prepare %.3f s\n", cmd_path, sec(t0, t1),
+                 sec(t1, t2), sec(t2, t3));
+  }
+  if (!ok) {
     delete m;
     pdx_status code = err.code == 1 ? PDX_ERR_IO
                       : err.code == 3 ? PDX_ERR_UNSUPPORTED
@@ -557,6 +572,8 @@ pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_optio
   *out = nullptr;
   pdx_options o{0, -1, 0, 0, 0};
   if (opts) o = *opts;
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   // host set-up of every specimen, in parallel (independent models)
   std::vector<pdx_model*> parts(n, nullptr);
   std::vector<Error> errs(n, Error{0, ""});
@@ -588,6 +605,7 @@ pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_optio
       drop();
       return create_error(e);
     }
+  const auto t1 = clk::now();
   pdx_model* m = new pdx_model();
   Error err{0, ""};
   if (!merge_batch(parts, m, err)) {
@@ -597,7 +615,14 @@ pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_optio
   }
   m->base_dir = parts[0]->base_dir;
   drop();
-  return finish_create(m, o, out);
+  const auto t2 = clk::now();
+  const pdx_status st = finish_create(m, o, out);
+  if (o.verbose > 1) {
+    auto sec = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    std::fprintf(stderr, "pdx: batch of %d: specimen set-ups %.3f s, merge %.3f s, device set-up %.3f s\n", n,
+                 sec(t0, t1), sec(t1, t2), sec(t2, clk::now()));
+  }
+  return st;
 }
 
 pdx_status pdx_batch_offsets(const pdx_model* m, int64_t* node_off, int64_t* member_off, int64_t* eq_off) {
@@ -1022,6 +1047,7 @@ pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t
                             double* f) {
   NEED_DEVICE(m);
   if (mode < 1 || mode > 3) return set_error(PDX_ERR_INVALID, "mode must be 1, 2 or 3");
+  if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "batched models run explicit dynamics only");
   const int N = m->mesh.n_node, D = m->mesh.dim;
   const int64_t nnz = (int64_t)m->setup.csr_ja.size();
   const size_t nd = (size_t)N * D;

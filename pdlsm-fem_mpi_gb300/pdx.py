@@ -149,10 +149,11 @@ _ARRAY_DTYPES = {"eq": np.int32, "vol_node": np.float64, "vol_elem": np.float64,
 class Model:
     """A PDLSM-FEM model built from a reference command file."""
 
-    def __init__(self, cmd_path: str, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0):
+    def __init__(self, cmd_path: str, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0,
+                 verbose: int = 0):
         L = lib()
         h = _P()
-        opt = Options(device, precision, lanes, 0, fe_lanes)
+        opt = Options(device, precision, lanes, verbose, fe_lanes)
         _check(L.pdx_model_create_from_cmd(cmd_path.encode(), C.byref(opt), C.byref(h)))
         self._h = h
         inf = ModelInfo()
@@ -160,11 +161,12 @@ class Model:
         self.info = inf
 
     @classmethod
-    def batch(cls, cmd_paths, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0) -> "Model":
+    def batch(cls, cmd_paths, device: int = 0, precision: int = -1, lanes: int = 0, fe_lanes: int = 0,
+              verbose: int = 0) -> "Model":
         """Many specimens (one command file each) merged into one model (pdx_batch_create)."""
         L = lib()
         h = _P()
-        opt = Options(device, precision, lanes, 0, fe_lanes)
+        opt = Options(device, precision, lanes, verbose, fe_lanes)
         arr = (C.c_char_p * len(cmd_paths))(*[p.encode() for p in cmd_paths])
         _check(L.pdx_batch_create(arr, len(cmd_paths), C.byref(opt), C.byref(h)))
         self = cls.__new__(cls)
