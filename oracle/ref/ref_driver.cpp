@@ -13,6 +13,7 @@
 //   ref_driver newmark  <cmd.in> <outdir>
 //   ref_driver quasi    <cmd.in> <outdir>
 //   ref_driver explicit_fc2 <cmd.in> <outdir> <every>  (FC 2 after every step)
+//   ref_driver newmark_fc2  <cmd.in> <outdir>          (Newmark with FC 2 after every step)
 //   ref_driver solve    <cmd.in>             (the reference's own pdfemSolver)
 //
 // Every loop below calls the reference's member functions in the order its own
@@ -368,7 +369,7 @@ void run_static(datModel& d, pdsolve& sol, Dumper& out) {
   out.f64("phi", node_damage(d));
 }
 
-void run_newmark(datModel& d, pdsolve& sol, Dumper& out) {
+void run_newmark(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   d.ci_solvFlag = 0;
   int neq = num_eq(d);
   int nsteps = d.getnumTstep();
@@ -407,10 +408,16 @@ void run_newmark(datModel& d, pdsolve& sol, Dumper& out) {
     double* t = Va_n->cdp_vecCoeff;
     Va_n->cdp_vecCoeff = Va_np1->cdp_vecCoeff;
     Va_np1->cdp_vecCoeff = t;
+    if (fc2) maxprisig_failure(d, sol);   // pdsolve.cpp:6258-6261
     std::vector<double> u = all_dof_values(d);
     traj.insert(traj.end(), u.begin(), u.end());
   }
-  sol.calGlobalNodeStresses(d);
+  if (fc2) {
+    sol.calLocalDamage(d);
+    out.i64("bond_state_final", bond_states(d));
+  } else {
+    sol.calGlobalNodeStresses(d);
+  }
   out.f64("u_traj", traj, {(long long)nsteps, (long long)N, (long long)D});
   out.f64("v_final", std::vector<double>(Vv_n->cdp_vecCoeff, Vv_n->cdp_vecCoeff + neq));
   out.f64("a_final", std::vector<double>(Va_n->cdp_vecCoeff, Va_n->cdp_vecCoeff + neq));
@@ -494,6 +501,7 @@ int main(int argc, char** argv) {
     run_explicit(dat, sol, out, 0.0, std::atoi(argv[4]), true);
   } else if (mode == "static") run_static(dat, sol, out);
   else if (mode == "newmark") run_newmark(dat, sol, out);
+  else if (mode == "newmark_fc2") run_newmark(dat, sol, out, true);
   else if (mode == "quasi") run_quasi(dat, sol, out);
   else { std::fprintf(stderr, "unknown mode %s\n", mode.c_str()); return 2; }
   return 0;

@@ -230,7 +230,8 @@ pdx_status run_newmark(pdx_model* m, const std::string& dir) {
     launch_advance_prescribed(m->view, u_all, m->stream);
     std::swap(acc, acc1);
     m->steps_done = n;
-    st = rf_record(m, n);
+    st = fc2_pass(m);
+    if (!st) st = rf_record(m, n);
     if (st) return st;
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps) {
       st = model_stress(m, u_all, true, true);
@@ -260,13 +261,12 @@ extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
   cudaSetDevice(m->device);
   mkdir(results_dir, 0755);
   const std::string dir(results_dir);
-  // FC 2 breaks bonds in explicit dynamic runs (after every step, as the
-  // reference does); FC 1, and FC 2 in the Newmark and quasi-static loops,
-  // are not built
-  const bool explicit_run = m->cmd.solver == 0 && !m->cmd.newmark;
-  if (m->cmd.solver != 1 && (m->cmd.fail_flag == 1 || (m->cmd.fail_flag == 2 && !explicit_run)))
+  // FC 2 breaks bonds after every explicit or Newmark step, as the reference
+  // does; FC 1, and FC 2 in the quasi-static loop (load-ratio control), are
+  // not built
+  if (m->cmd.solver != 1 && (m->cmd.fail_flag == 1 || (m->cmd.fail_flag == 2 && m->cmd.solver == 2)))
     return set_error(PDX_ERR_UNSUPPORTED,
-                     "failure criterion FC 1, and FC 2 outside explicit dynamics, are not implemented");
+                     "failure criterion FC 1, and FC 2 in quasi-static runs, are not implemented");
   switch (m->cmd.solver) {
     case 0: return m->cmd.newmark ? run_newmark(m, dir) : run_explicit(m, dir);
     case 1: return run_static(m, dir);

@@ -530,7 +530,10 @@ pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_inf
   launch_advance_prescribed(m->view, u_all, m->stream);
   cudaMemcpyAsync(m->d_acc, acc1, (size_t)ne * 8, cudaMemcpyDeviceToDevice, m->stream);
   m->steps_done = n;
-  pdx_status rs = rf_record(m, n);
+  // FC 2 after the step, on the state with the advanced prescribed values
+  // (pdsolve.cpp:6249-6261), then the reaction forces
+  pdx_status rs = fc2_pass(m);
+  if (!rs) rs = rf_record(m, n);
   if (rs) return rs;
   return cuda_check(cudaStreamSynchronize(m->stream), "Newmark step");
 }

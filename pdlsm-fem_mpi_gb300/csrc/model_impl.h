@@ -183,6 +183,7 @@ void write_vtk(const pdx_model* m, const std::string& path, const std::vector<do
                const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);
 pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi);
 pdx_status rf_record(pdx_model* m, int64_t row);
+pdx_status fc2_pass(pdx_model* m);
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);

@@ -325,3 +325,22 @@ def test_reaction_forces_match_reference(built, tmp_path):
     assert lines[0] == "Step\tU\tRFx\tRFy\tRFz" and len(lines) == 62
     last = [float(t) for t in lines[-1].split("\t")]
     assert last[0] == 60 and abs(last[3] - g[-1, 3]) <= 1e-5 * abs(g[-1, 3])
+
+
+def test_fc2_in_newmark_steps_matches_reference(built):
+    """FC 2 after every Newmark step (10 steps, sigma_ult 3e7), the reference
+    solving K_N directly and this build with BiCGStab to 1e-13: displacement
+    trajectory and the broken-bond set."""
+    g = golden("p21_nmfc2")
+    with pdx.Model(case_cmd("p21", "p21_nmfc2"), device=0, precision=0) as m:
+        m.newmark_init()
+        worst = 0.0
+        for i in range(10):
+            info = m.newmark_step(2)
+            assert info.converged
+            u, _, _, bs = m.state()
+            worst = max(worst, rel(u, g["u_traj"][i]))
+    print(f"\n[p21_nmfc2] worst displacement error {worst:.2e}, "
+          f"{int((bs != g['bond_state_final']).sum())} bond differences of {int((g['bond_state_final'] == 0).sum())} broken")
+    np.testing.assert_array_equal(bs, g["bond_state_final"])
+    assert worst < 1e-9
