@@ -14,6 +14,7 @@
 //   ref_driver quasi    <cmd.in> <outdir>
 //   ref_driver explicit_fc2 <cmd.in> <outdir> <every>  (FC 2 after every step)
 //   ref_driver newmark_fc2  <cmd.in> <outdir>          (Newmark with FC 2 after every step)
+//   ref_driver quasi_fc2    <cmd.in> <outdir>          (quasi-static with FC 2 and its load ratio)
 //   ref_driver solve    <cmd.in>             (the reference's own pdfemSolver)
 //
 // Every loop below calls the reference's member functions in the order its own
@@ -424,7 +425,7 @@ void run_newmark(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   out.f64("sigma_final", node_sigma(d), {(long long)N, 6});
 }
 
-void run_quasi(datModel& d, pdsolve& sol, Dumper& out) {
+void run_quasi(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   d.ci_solvFlag = 2;
   int neq = num_eq(d);
   int nsteps = d.getnumTstep();
@@ -439,9 +440,18 @@ void run_quasi(datModel& d, pdsolve& sol, Dumper& out) {
   sol.setCSRIndexes_gloStiffMat(d);
   int comm = 0;
   long long n64 = neq;
-  std::vector<double> traj;
+  std::vector<double> traj, traj_after;
+  // with FC 2: the reference's loop body (pdsolve.cpp:6527-6578): stresses,
+  // failureProcess (cuts and the load ratio), reaction forces, then the load
+  // step only if nothing was cut
+  bool addLoad = true;
+  double rati = 1.0;
+  const bool rf = fc2 && !d.civ_reacForceOfessBCId.empty();
+  const std::string rf_path = out.dir + "/rf.txt";
+  std::ofstream rf_out, crack_out;
+  if (rf) { rf_out.open(rf_path); rf_out << std::setprecision(17); }
   for (int n = 1; n < nsteps + 1; n++) {
-    sol.pdfemQuasiStaticAssembleEquasSys_CSRformat(d, neq, true);
+    sol.pdfemQuasiStaticAssembleEquasSys_CSRformat(d, neq, addLoad);
     if (n == 1 || n == 2) {
       long long nnz = sol.cip_ia[neq];
       std::string s = std::to_string(n);
@@ -454,14 +464,37 @@ void run_quasi(datModel& d, pdsolve& sol, Dumper& out) {
                                        Vdu->cdp_vecCoeff, &comm);
     matoperat.matAdd(Vu_n, Vdu, Vu_n);
     sol.storeDisplacementResult(d, Vu_n);
+    if (fc2) {
+      sol.calGlobalNodeStresses(d);
+      rati = sol.failureProcess(d, d.ci_topk, addLoad, crack_out);
+      if (rf) sol.calReacForc(d, rf_out, n);
+    }
     std::vector<double> u = all_dof_values(d);
     traj.insert(traj.end(), u.begin(), u.end());
-    sol.setVaryNaturalBC(d);
-    sol.setVaryEssentialBC(d, 1.0);
+    if (!fc2 || addLoad) {
+      sol.setVaryNaturalBC(d);
+      sol.setVaryEssentialBC(d, fc2 ? rati : 1.0);
+    }
+    if (fc2) {
+      std::vector<double> ua = all_dof_values(d);
+      traj_after.insert(traj_after.end(), ua.begin(), ua.end());
+    }
   }
-  sol.calGlobalNodeStresses(d);
+  if (!fc2) sol.calGlobalNodeStresses(d);
   out.f64("u_traj", traj, {(long long)nsteps, (long long)N, (long long)D});
   out.f64("sigma_final", node_sigma(d), {(long long)N, 6});
+  if (fc2) {
+    out.f64("u_after", traj_after, {(long long)nsteps, (long long)N, (long long)D});
+    out.i64("bond_state_final", bond_states(d));
+    if (rf) {
+      rf_out.close();
+      std::ifstream in(rf_path);
+      std::vector<double> rows;
+      double v;
+      while (in >> v) rows.push_back(v);
+      out.f64("rf_rows", rows, {(long long)(rows.size() / 5), 5});
+    }
+  }
 }
 
 }  // namespace
@@ -503,6 +536,7 @@ int main(int argc, char** argv) {
   else if (mode == "newmark") run_newmark(dat, sol, out);
   else if (mode == "newmark_fc2") run_newmark(dat, sol, out, true);
   else if (mode == "quasi") run_quasi(dat, sol, out);
+  else if (mode == "quasi_fc2") run_quasi(dat, sol, out, true);
   else { std::fprintf(stderr, "unknown mode %s\n", mode.c_str()); return 2; }
   return 0;
 }

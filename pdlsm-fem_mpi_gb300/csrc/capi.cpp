@@ -194,6 +194,12 @@ static pdx_status upload_model(pdx_model* m) {
     m->d_fc2_bond = m->buf.alloc<int>(m->fc2_cap);
     m->d_fc2_fam = m->buf.alloc<int>(m->fc2_cap);
     m->d_fc2_count = m->buf.alloc<int>(1);
+    m->d_fc2_max = m->buf.alloc<double>(1);
+    std::vector<double> vel((size_t)N * 3, 0.0);
+    for (const EssentialBC& b : me.ebcs)
+      if (b.varying)
+        for (int node : b.nodes) vel[(size_t)node * 3 + b.dof] = b.velocity;
+    m->d_ebc_vel = upload(m, vel);
   }
   // reaction forces (setReacForcNode, datModel.cpp:664-735): the nodes of the
   // RF essential BCs, every element with one of them (in element order) with
@@ -336,7 +342,7 @@ pdx_status rf_record(pdx_model* m, int64_t row) {
 // pdsolve.cpp:6014-6016, 6060-6064): nodal stresses, candidates, Top-K
 // selection, cuts.  Top-K (K > 0) selects on the host: the K largest sigma1,
 // ties by bond index.
-pdx_status fc2_pass(pdx_model* m) {
+pdx_status fc2_pass(pdx_model* m, bool report) {
   if (!m->fc2) return PDX_OK;
   pdx_status st = model_stress(m, m->d_u[m->cur], true, false);
   if (st) return st;
@@ -359,10 +365,21 @@ pdx_status fc2_pass(pdx_model* m) {
   a.cand_fam = m->d_fc2_fam;
   a.count = m->d_fc2_count;
   a.cap = m->fc2_cap;
+  a.max_sigma1 = report ? m->d_fc2_max : nullptr;
   cudaMemsetAsync(a.count, 0, sizeof(int), m->stream);
+  if (report) cudaMemsetAsync(m->d_fc2_max, 0, sizeof(double), m->stream);
   st = cuda_check(launch_fc2_candidates(a, m->stream), "FC 2 candidates");
   if (st) return st;
   const int K = m->cmd.topk;
+  if (report) {
+    int nc = 0;
+    cudaMemcpyAsync(&nc, a.count, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+    cudaMemcpyAsync(&m->fc2_max, m->d_fc2_max, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+    st = cuda_check(cudaStreamSynchronize(m->stream), "FC 2 report");
+    if (st) return st;
+    nc = std::min(nc, a.cap);
+    m->fc2_kept = K > 0 ? std::min(nc, K) : nc;
+  }
   if (K > 0) {
     int n = 0;
     cudaMemcpyAsync(&n, a.count, sizeof(int), cudaMemcpyDeviceToHost, m->stream);

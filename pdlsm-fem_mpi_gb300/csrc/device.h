@@ -168,6 +168,10 @@ cudaError_t launch_scatter_eq(const DevView& v, const double* u_eq, double* u_al
 cudaError_t launch_gather_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s);
 cudaError_t launch_advance_prescribed(const DevView& v, double* u_all, cudaStream_t s);
 cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s);
+// the quasi-static rule with a load ratio (setVaryEssentialBC, FC 2): vel =
+// n_node*3 velocities of the varying EBC DOFs
+cudaError_t launch_advance_prescribed_ratio(const DevView& v, double* u_all, const double* vel, double dt,
+                                            double rati, cudaStream_t s);
 
 // FC 2 (maximum principal stress, Top-K) bond breaking after an explicit step, 2D (k_fc2.cu)
 struct Fc2Args {
@@ -185,6 +189,7 @@ struct Fc2Args {
   int* cand_fam;
   int* count;               // number of candidates found (may exceed cap)
   int cap;
+  double* max_sigma1;       // largest sigma1 over intact bonds (from 0), or null
 };
 // reaction forces of one step (k_post.cu): Fe = Ke u_e over the elements
 // touching the RF nodes, summed over those nodes in element order;

@@ -6,6 +6,7 @@
 //   quasi-static                    pdfemQuasiStaticSolver_CSRformat :6464-6590
 // The direct sparse solves of the reference become Krylov solves judged by
 // the true FP64 residual (SOLVE keyword; default BiCGStab, tolerance 1e-8).
+#include <cmath>
 #include <cstdio>
 #include <fstream>
 #include <iomanip>
@@ -145,7 +146,8 @@ pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, fl
   const int ne = m->setup.n_eq;
   double* du = m->d_tmp_eq[1];
   double* ueq = m->d_tmp_eq[2];
-  pdx_status st = assemble_device(m, 2, u_all, n - 1);
+  // natural BC row: the load steps applied so far (n - 1 unless FC 2 held the load)
+  pdx_status st = assemble_device(m, 2, u_all, m->quasi_load);
   if (st) return st;
   cudaMemsetAsync(du, 0, (size_t)ne * 8, m->stream);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -167,6 +169,12 @@ pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, fl
   launch_axpby_scale(ne, du, 1.0, ueq, 1.0, m->stream);
   launch_scatter_eq(m->view, ueq, u_all, m->stream);
   m->steps_done = n;
+  if (m->fc2) {
+    // FC 2 with the cut count and the largest sigma1 for the load ratio
+    st = fc2_pass(m, true);
+    if (st) return st;
+    return model_stress(m, u_all, false, true);
+  }
   if (m->view.fail3) {
     st = model_stress(m, u_all, true, false);
     if (st) return st;
@@ -178,11 +186,31 @@ pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, fl
   return model_stress(m, u_all, true, true);
 }
 
+// The load step after an increment (the end of the reference's increment
+// loop, pdsolve.cpp:6570-6578): with FC 2 the load advances only if the
+// increment cut no bond, scaled by the ratio rati = 1.001 sigma_ult / max
+// sigma1 (failureProcess :6615-6628); otherwise rati = 1 (a varying EBC
+// takes dt * velocity once, from 0, and holds).
+pdx_status quasi_advance(pdx_model* m) {
+  double* u_all = m->d_u[0];
+  if (m->fc2) {
+    if (m->fc2_kept > 0) return PDX_OK;   // bonds were cut: the load holds
+    const double sig = m->mesh.sigult, mx = m->fc2_max;
+    const double rati = std::fabs(mx) < 1e-20 * sig ? 1.0 : 1.001 * sig / mx;
+    m->quasi_load++;
+    return cuda_check(launch_advance_prescribed_ratio(m->view, u_all, m->d_ebc_vel, m->cmd.dt, rati, m->stream),
+                      "prescribed values");
+  }
+  m->quasi_load++;
+  return cuda_check(launch_advance_prescribed_quasi(m->view, u_all, m->stream), "prescribed values");
+}
+
 pdx_status run_quasi(pdx_model* m, const std::string& dir) {
   pdx_status st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
   if (st) return st;
   double* u_all = m->d_u[0];
   m->cur = 0;
+  m->quasi_load = 0;
   for (int n = 1; n <= m->cmd.nsteps; n++) {
     KrylovResult kr;
     st = quasi_increment(m, n, m->cmd.solve_method, &kr, nullptr);
@@ -194,7 +222,8 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
       if (st) return st;
       write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
     }
-    launch_advance_prescribed_quasi(m->view, u_all, m->stream);
+    st = quasi_advance(m);
+    if (st) return st;
   }
   st = cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
   if (st) return st;
@@ -261,12 +290,11 @@ extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
   cudaSetDevice(m->device);
   mkdir(results_dir, 0755);
   const std::string dir(results_dir);
-  // FC 2 breaks bonds after every explicit or Newmark step, as the reference
-  // does; FC 1, and FC 2 in the quasi-static loop (load-ratio control), are
-  // not built
-  if (m->cmd.solver != 1 && (m->cmd.fail_flag == 1 || (m->cmd.fail_flag == 2 && m->cmd.solver == 2)))
-    return set_error(PDX_ERR_UNSUPPORTED,
-                     "failure criterion FC 1, and FC 2 in quasi-static runs, are not implemented");
+  // FC 2 breaks bonds after every explicit or Newmark step and every
+  // quasi-static increment (with its load-ratio control), as the reference
+  // does; FC 1 is not built
+  if (m->cmd.solver != 1 && m->cmd.fail_flag == 1)
+    return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   switch (m->cmd.solver) {
     case 0: return m->cmd.newmark ? run_newmark(m, dir) : run_explicit(m, dir);
     case 1: return run_static(m, dir);
@@ -284,6 +312,7 @@ extern "C" pdx_status pdx_quasi_init(pdx_model* m) {
   if (st) return st;
   m->cur = 0;
   m->steps_done = 0;
+  m->quasi_load = 0;
   return PDX_OK;
 }
 
@@ -292,8 +321,8 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
   if (method < 0 || method > 3) return set_error(PDX_ERR_INVALID, "method must be 0..3");
-  if (m->cmd.fail_flag == 1 || m->cmd.fail_flag == 2)
-    return set_error(PDX_ERR_UNSUPPORTED, "failure criteria FC 1 / FC 2 are not implemented (FC 0 and FC 3 are)");
+  if (m->cmd.fail_flag == 1)
+    return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   cudaSetDevice(m->device);
   KrylovResult kr;
   float ms = 0.f;
@@ -306,6 +335,7 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
     info->converged = kr.converged;
   }
   if (st) return st;
-  launch_advance_prescribed_quasi(m->view, m->d_u[0], m->stream);
+  st = quasi_advance(m);
+  if (st) return st;
   return cuda_check(cudaStreamSynchronize(m->stream), "quasi-static increment");
 }

@@ -78,6 +78,10 @@ __global__ void k_fc2_candidates(Fc2Args a) {
     const double* sm = a.sigma + (int64_t)v.nbr[b] * 6;
     double e0, e1;
     const double l1 = eig_max2(0.5 * (s0 + sm[0]), 0.5 * (s3 + sm[3]), 0.5 * (s1 + sm[1]), &e0, &e1);
+    // the largest sigma1 over intact bonds, from 0 (the quasi-static load ratio;
+    // non-negative doubles order as their bit patterns)
+    if (a.max_sigma1 && l1 > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(a.max_sigma1), (unsigned long long)__double_as_longlong(l1));
     if (l1 > a.sigult) {
       const int i = atomicAdd(a.count, 1);
       if (i < a.cap) {

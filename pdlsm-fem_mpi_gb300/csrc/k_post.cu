@@ -448,6 +448,38 @@ cudaError_t launch_reaction(int n_el, int nen, int dim, const int* conn, const d
   return cudaGetLastError();
 }
 
+// setVaryEssentialBC (pdsolve.cpp:5263-5311, solver flag 2) with a load
+// ratio rati: a varying EBC at 0 moves by dt * velocity; otherwise by
+// dt * (rati - 1) * value, or dt * velocity if that step is larger, or not
+// at all if rati < 1.
+template <int D>
+__global__ void k_advance_prescribed_ratio(DevView v, double* u_all, const double* vel, double dt, double rati) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)v.n_node * D) return;
+  const int n = (int)(i / D), d = (int)(i % D);
+  if (!(v.eq[i] < 0 && ((v.bcflag[n] >> d) & 1u))) return;
+  const double value = u_all[i], velocity = vel[3 * n + d];
+  double dv;
+  if (value == 0.0) {
+    dv = velocity;
+  } else {
+    const double ndv = (rati - 1) * value;
+    if (fabs(ndv) > fabs(velocity)) dv = velocity;
+    else if (rati < 1) dv = 0;
+    else dv = ndv;
+  }
+  u_all[i] = value + dt * dv;
+}
+
+cudaError_t launch_advance_prescribed_ratio(const DevView& v, double* u_all, const double* vel, double dt,
+                                            double rati, cudaStream_t s) {
+  const int64_t n = (int64_t)v.n_node * v.dim;
+  const int blocks = (int)((n + 255) / 256);
+  if (v.dim == 2) k_advance_prescribed_ratio<2><<<blocks, 256, 0, s>>>(v, u_all, vel, dt, rati);
+  else k_advance_prescribed_ratio<3><<<blocks, 256, 0, s>>>(v, u_all, vel, dt, rati);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cudaStream_t s) {
   const int64_t n = (int64_t)v.n_node * v.dim;
   const int blocks = (int)((n + 255) / 256);

@@ -136,6 +136,11 @@ struct pdx_model {
   int* d_fc2_fam = nullptr;
   int* d_fc2_count = nullptr;
   int fc2_cap = 0;
+  double* d_fc2_max = nullptr;       // largest sigma1 of the last pass (quasi-static load ratio)
+  double* d_ebc_vel = nullptr;       // n_node*3 velocities of the varying EBC DOFs (quasi-static FC 2)
+  int fc2_kept = 0;                  // candidates cut by the last pass
+  double fc2_max = 0.0;
+  int quasi_load = 0;                // quasi-static load steps applied (natural-BC row)
   int ke_smem = 0;                   // floats of FE classes staged in shared memory
   uint32_t* d_state = nullptr;
   int* d_intact = nullptr;
@@ -183,7 +188,9 @@ void write_vtk(const pdx_model* m, const std::string& path, const std::vector<do
                const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);
 pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi);
 pdx_status rf_record(pdx_model* m, int64_t row);
-pdx_status fc2_pass(pdx_model* m);
+// FC 2 pass on the current state; with `report` it also reads back how many
+// candidates were cut (fc2_kept) and the largest sigma1 (fc2_max)
+pdx_status fc2_pass(pdx_model* m, bool report = false);
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);

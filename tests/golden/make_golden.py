@@ -151,7 +151,8 @@ def main() -> None:
 def fc2_cases() -> None:
     """FC 2 (maximum principal stress) on the 2D plate: sigma_ult = 3e7 Pa, all
     candidates (Top-K 0) and the two largest per step (Top-K 2), 60 explicit
-    steps; and 10 Newmark steps with all candidates."""
+    steps; 10 Newmark steps with all candidates; 20 quasi-static increments
+    with Top-K 4 and the reference's load-ratio control (RF 2 recorded)."""
     work = tempfile.mkdtemp(prefix="golden_fc2_")
     d2 = os.path.join(work, "p21")
     for name, fc in (("p21_fc2", "2 0"), ("p21_fc2k", "2 2")):
@@ -164,7 +165,13 @@ def fc2_cases() -> None:
     mn.sigult = 3e7
     meshgen.write_case(mn, d2, "p21_nmfc2", solver="DYNAMIC", dt=2e-7, nsteps=10, save=10, factor=3.015, nlf=1.0,
                        lumped=False, newmark=(0.5, 0.25), fc="2 0", extra=["SOLVE BICGSTAB 1e-13 20000"])
+    mq = plate_case()
+    mq.sigult = 3e7
+    mq.ebcs[2].velocity = 5e-6
+    meshgen.write_case(mq, d2, "p21_qfc2", solver="QUASI-STATIC", dt=1.0, nsteps=20, save=20, factor=3.015, nlf=1.0,
+                       lumped=False, fc="2 4", extra=["RF 2", "SOLVE BICGSTAB 1e-13 20000"])
     copy_inputs(d2, "p21")
+    save("p21_qfc2", run(d2, "p21_qfc2.in", "quasi_fc2"))
     save("p21_fc2", run(d2, "p21_fc2.in", "explicit_fc2", "20"))
     save("p21_fc2k", run(d2, "p21_fc2k.in", "explicit_fc2", "20"))
     save("p21_nmfc2", run(d2, "p21_nmfc2.in", "newmark_fc2"))

@@ -344,3 +344,27 @@ def test_fc2_in_newmark_steps_matches_reference(built):
           f"{int((bs != g['bond_state_final']).sum())} bond differences of {int((g['bond_state_final'] == 0).sum())} broken")
     np.testing.assert_array_equal(bs, g["bond_state_final"])
     assert worst < 1e-9
+
+
+def test_fc2_quasi_static_load_control_matches_reference(built):
+    """Quasi-static FC 2 with Top-K 4 (20 increments): after an increment that
+    cuts bonds the load holds, otherwise it steps by the ratio 1.001 sigma_ult /
+    max sigma1 (capped by the BC velocity).  The state after every increment,
+    the broken-bond set and the reaction forces against the reference."""
+    g = golden("p21_qfc2")
+    with pdx.Model(case_cmd("p21", "p21_qfc2"), device=0, precision=0) as m:
+        m.quasi_init()
+        worst = 0.0
+        for i in range(20):
+            info = m.quasi_step(2)
+            assert info.converged
+            u, _, _, bs = m.state()
+            worst = max(worst, rel(u, g["u_after"][i]))
+        rows = m.reaction_forces()
+    rf = g["rf_rows"]
+    print(f"\n[p21_qfc2] worst state error {worst:.2e}, {int((bs != g['bond_state_final']).sum())} bond differences "
+          f"of {int((g['bond_state_final'] == 0).sum())} broken")
+    np.testing.assert_array_equal(bs, g["bond_state_final"])
+    assert worst < 1e-9
+    assert rows.shape == (21, 4)
+    assert np.abs(rows[1:, 1:4] - rf[:, 2:5]).max() <= 1e-8 * np.abs(rf[:, 2:5]).max()
