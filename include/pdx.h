@@ -56,7 +56,8 @@ typedef struct pdx_model_info {
 } pdx_model_info;
 
 typedef struct pdx_solve_opts {
-  int method;      /* 0 Jacobi PCG, 1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 mixed PCG + FP64 refinement */
+  int method;      /* 0 Jacobi PCG, 1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 mixed PCG + FP64 refinement,
+                      6 GMRES(30) (Jacobi) */
   double rtol;     /* relative true residual ||b - A x|| / ||b|| */
   int max_iter;
   int use_x0;      /* 1: x holds the initial guess */
@@ -179,7 +180,7 @@ pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, co
  * K_N = beta dt^2 K + M assembled on the GPU (pdfemAssembleKNFR_CSRformat
  * :6327-6397), K_N a = F solved by `method`, update (updateDispVelo
  * :6399-6422).  The reference factorises K_N with PARDISO at every step.
- * method: 0-3 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
+ * method: 0-3 and 6 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
  * method); 5 flexible CG with block-Jacobi plus the learned coarse correction,
  * falling back to 4 and then BiCGStab when it stalls.  collect = 1 (method 4)
  * stores one training pair per iteration of the solve.  info: iterations,
@@ -263,8 +264,8 @@ pdx_status pdx_run(pdx_model* m, const char* results_dir);
  * PARDISO solve replaced by a Krylov method: pdx_quasi_init resets the state
  * (initial DOF values, pre-crack bond states); each pdx_quasi_step assembles
  * K and f_ext - K u through the scatter map, solves K du = f_ext - K u to the
- * command file's tolerance with `method` (as pdx_solve_opts; BiCGStab takes
- * over if it does not converge), updates u, applies FC 3 or FC 2 bond
+ * command file's tolerance with `method` (as pdx_solve_opts; BiCGStab and
+ * then GMRES(30) take over if it does not converge), updates u, applies FC 3 or FC 2 bond
  * failure, recomputes the stresses, records the reaction forces and advances
  * the prescribed DOFs by the reference's quasi-static rule
  * (setVaryEssentialBC, pdsolve.cpp:5263-5311): a varying EBC whose value is

@@ -1089,6 +1089,7 @@ pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const 
   if (n <= 0 || !ia || !ja || !a || !rhs || !x) return set_error(PDX_ERR_INVALID, "bad argument");
   pdx_solve_opts o{2, 1e-8, 20000, 0};
   if (opts) o = *opts;
+  if (o.method < 0 || (o.method > 3 && o.method != 6)) return set_error(PDX_ERR_INVALID, "method must be 0..3 or 6");
   const int64_t nnz = ia[n];
   std::vector<int> ja32(ja, ja + nnz);
   cudaStream_t s;

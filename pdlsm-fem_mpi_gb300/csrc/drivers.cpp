@@ -5,7 +5,8 @@
 //   static                          pdfemStaticSolver_CSRformat    :5557-5654
 //   quasi-static                    pdfemQuasiStaticSolver_CSRformat :6464-6590
 // The direct sparse solves of the reference become Krylov solves judged by
-// the true FP64 residual (SOLVE keyword; default BiCGStab, tolerance 1e-8).
+// the true FP64 residual (SOLVE keyword; default BiCGStab, tolerance 1e-8;
+// a solve that does not converge falls back to BiCGStab, then GMRES(30)).
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -51,8 +52,19 @@ pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int met
   if (st) return st;
   if (!kr->converged) {
     // BiCGStab as the fallback of a stalled CG on the unsymmetric stiffness
-    if (method != 2) {
+    if (method != 2 && method != 6) {
       e = krylov_solve(A, b, x, 2, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
+      st = cuda_check(e, "Krylov solve");
+      if (st) return st;
+    }
+    if (!kr->converged && method != 6) {
+      // GMRES(30) when BiCGStab does not converge: once a crack has cut a
+      // piece loose the stiffness is strongly unsymmetric and indefinite, and
+      // BiCGStab's residual grows without bound (the reference's direct
+      // solve has no such limit).  GMRES never lets its residual grow; it
+      // starts from zero after a non-finite BiCGStab iterate.
+      if (!(kr->rel_residual < 1.0)) cudaMemsetAsync(x, 0, (size_t)A.n * 8, m->stream);
+      e = krylov_solve(A, b, x, 6, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
       st = cuda_check(e, "Krylov solve");
       if (st) return st;
     }
@@ -320,7 +332,7 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   if (!m) return set_error(PDX_ERR_INVALID, "null model");
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
-  if (method < 0 || method > 3) return set_error(PDX_ERR_INVALID, "method must be 0..3");
+  if (method < 0 || (method > 3 && method != 6)) return set_error(PDX_ERR_INVALID, "method must be 0..3 or 6");
   if (m->cmd.fail_flag == 1)
     return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   cudaSetDevice(m->device);

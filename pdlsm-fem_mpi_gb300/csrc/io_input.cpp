@@ -223,8 +223,11 @@ bool read_command(const std::string& path, Command& c, Mesh& m, std::string& bas
       if (f < 0 || f > 3) c.warnings.push_back("the failure criterion is ignored");
       else if (f == 1 && t.size() > 3) { c.mr = std::atof(t[2].c_str()); c.dcf = std::atof(t[3].c_str()); }
       else if (f == 2 && t.size() > 2) c.topk = std::atoi(t[2].c_str());
-      else if (f == 3) {
-        if (t.size() < 3) return fail(err, 2, "FC 3 needs the critical stretch s0");
+      else if (f == 3 && t.size() < 3) {
+        // the reference reads a bare FC 3 and breaks no bond with it
+        c.fail_flag = 0;
+        c.warnings.push_back("FC 3 without a critical stretch: no bond breaking (as the reference)");
+      } else if (f == 3) {
         c.s0 = std::atof(t[2].c_str());
         if (t.size() > 3) c.s0_seed = std::strtoull(t[3].c_str(), nullptr, 10);
         if (t.size() > 4) c.s0_pert = std::atof(t[4].c_str());
@@ -247,7 +250,8 @@ bool read_command(const std::string& path, Command& c, Mesh& m, std::string& bas
       else if (t[1] == "BJPCG") c.solve_method = 1;
       else if (t[1] == "BICGSTAB") c.solve_method = 2;
       else if (t[1] == "MIXEDPCG") c.solve_method = 3;
-      else return fail(err, 2, "SOLVE must be PCG, BJPCG, BICGSTAB or MIXEDPCG");
+      else if (t[1] == "GMRES") c.solve_method = 6;
+      else return fail(err, 2, "SOLVE must be PCG, BJPCG, BICGSTAB, MIXEDPCG or GMRES");
       if (t.size() > 2) c.solve_tol = std::atof(t[2].c_str());
       if (t.size() > 3) c.solve_maxit = std::atoi(t[3].c_str());
     } else {

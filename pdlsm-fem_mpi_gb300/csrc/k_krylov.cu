@@ -8,11 +8,13 @@
 //             delta_k while row m uses A_m and delta_m)
 //   method 3  PCG in FP32 (FP32 matrix copy and vectors) inside FP64 iterative
 //             refinement: r = b - A x in FP64, A d ~= r in FP32, x += d
+//   method 6  GMRES(30), right Jacobi (the fallback once BiCGStab diverges)
 //
 // Convergence is always judged on the true FP64 residual ||b - A x|| / ||b||.
 // Scalars stay on the device; iterations are launched in chunks and the host
 // reads the residual once per chunk.  Reductions are two-pass (per-block
 // partials then one block) so results are bitwise reproducible.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -270,6 +272,77 @@ __global__ void k_bicg_x2(int64_t n, const double* alpha, const double* omega, c
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// Restarted GMRES: Arnoldi basis V (rows of length ld), classical
+// Gram-Schmidt applied twice, Givens rotations of the small Hessenberg column
+// on the host.  Partial sums keep a fixed order (grid-stride, block tree,
+// one final block per basis vector) as the other reductions here.
+constexpr int kGmresRestart = 30;
+constexpr int kMdotChunk = 8;
+
+// per-block partials of v_k . w for k in [k0, k0 + nk), nk <= kMdotChunk;
+// part[k * np + block]
+__global__ void k_mdot_partial(int64_t n, const double* V, int64_t ld, int k0, int nk, const double* w, double* part,
+                               int np) {
+  __shared__ double sh[kThreads];
+  double acc[kMdotChunk];
+#pragma unroll
+  for (int k = 0; k < kMdotChunk; k++) acc[k] = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double wi = w[i];
+#pragma unroll
+    for (int k = 0; k < kMdotChunk; k++)
+      if (k < nk) acc[k] += V[(int64_t)(k0 + k) * ld + i] * wi;
+  }
+#pragma unroll
+  for (int k = 0; k < kMdotChunk; k++) {
+    if (k < nk) {
+      const double t = block_sum(acc[k], sh);
+      if (threadIdx.x == 0) part[(int64_t)(k0 + k) * np + blockIdx.x] = t;
+    }
+  }
+}
+
+// out[k] = sum of part[k * np ...] (one block per k); acc[k] += out[k] if acc
+__global__ void k_mdot_final(const double* part, int np, double* out, double* acc) {
+  __shared__ double sh[kThreads];
+  const int k = blockIdx.x;
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[(int64_t)k * np + i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) {
+    out[k] = s;
+    if (acc) acc[k] += s;
+  }
+}
+
+// w -= sum_{k < nk} h[k] v_k
+__global__ void k_msub(int64_t n, const double* V, int64_t ld, int nk, const double* h, double* w) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = w[i];
+    for (int k = 0; k < nk; k++) s -= h[k] * V[(int64_t)k * ld + i];
+    w[i] = s;
+  }
+}
+
+// *hsub = ||w|| from its square; w /= ||w|| (left as is when the norm is 0)
+__global__ void k_gmres_normalise(int64_t n, const double* nn, double* hsub, double* w) {
+  const double nv = sqrt(*nn);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *hsub = nv;
+  if (!(nv > 0.0)) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = w[i] / nv;
+}
+
+// x += D^-1 sum_{k < nk} y[k] v_k
+__global__ void k_gmres_x(int64_t n, const double* V, int64_t ld, int nk, const double* y, const double* dinv,
+                          double* x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int k = 0; k < nk; k++) s += y[k] * V[(int64_t)k * ld + i];
+    x[i] += dinv[i] * s;
+  }
+}
+
 template <typename T>
 struct Work {
   T* buf = nullptr;
@@ -367,6 +440,114 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
     }
   }
   return it;
+}
+
+// GMRES(kGmresRestart) with right Jacobi preconditioning, A (D^-1 y) = b,
+// x = D^-1 y.  Unlike BiCGStab its residual never grows, so it also solves
+// the unsymmetric, indefinite stiffness of a cracked body on which BiCGStab
+// diverges; an empty row (a node with every bond broken) with a zero right
+// side keeps a zero solution.  Each cycle starts from the true residual; the
+// solve stops when the rotated residual |g_{j+1}| of a cycle and then the
+// true residual are at most rtol ||b||.  Returns iterations (mat-vecs).
+int gmres_core(Ctx& c, const DevCsr& A, const double* b, double* x, const double* dinv, double rtol, int max_iter,
+               double* dscal, double* z) {
+  cudaStream_t s = c.s;
+  const int64_t n = A.n;
+  const double avg = n ? (double)A.nnz / (double)n : 0.0;
+  const int M = kGmresRestart;
+  const int g = grid_for(n);
+  const int64_t ld = n;
+  double *V = nullptr, *part = nullptr, *hd = nullptr, *tmp = nullptr, *yd = nullptr;
+  cudaMallocAsync(&V, (size_t)(M + 1) * n * sizeof(double), s);
+  cudaMallocAsync(&part, (size_t)(M + 1) * g * sizeof(double), s);
+  cudaMallocAsync(&hd, (size_t)(M + 1) * M * sizeof(double), s);
+  cudaMallocAsync(&tmp, (size_t)(M + 1) * sizeof(double), s);
+  cudaMallocAsync(&yd, (size_t)M * sizeof(double), s);
+  double* bb = dscal + 8;
+  double* nn = dscal + 9;
+  c.dot<double>(n, b, b, bb);
+  double hb = 0;
+  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double bnorm = std::sqrt(hb);
+  std::vector<double> H((size_t)(M + 1) * M), cs(M), sn(M), gv(M + 1), y(M);
+  // v_k . w for k < nk into out (acc += out if given), in chunks of kMdotChunk
+  auto project = [&](int nk, const double* w, double* out, double* acc) {
+    for (int k0 = 0; k0 < nk; k0 += kMdotChunk)
+      k_mdot_partial<<<g, kThreads, 0, s>>>(n, V, ld, k0, std::min(kMdotChunk, nk - k0), w, part, g);
+    k_mdot_final<<<nk, kThreads, 0, s>>>(part, g, out, acc);
+  };
+  int its = 0;
+  while (bnorm > 0 && its < max_iter) {
+    double* v0 = V;
+    spmv_t<double>(n, avg, A.ia, A.ja, A.a, x, z, s);
+    k_residual<<<g, kThreads, 0, s>>>(n, b, z, v0);
+    c.dot<double>(n, v0, v0, nn);
+    double hr = 0;
+    cudaMemcpyAsync(&hr, nn, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const double beta = std::sqrt(hr);
+    if (!(beta > rtol * bnorm)) break;   // converged, or a NaN residual
+    k_gmres_normalise<<<g, kThreads, 0, s>>>(n, nn, tmp, v0);
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int k = 0;   // basis vectors of this cycle that enter the update
+    bool stop = false;
+    for (int j = 0; j < M && its < max_iter; j++) {
+      double* w = V + (int64_t)(j + 1) * ld;
+      double* hc = hd + (size_t)j * (M + 1);
+      k_jacobi<double><<<g, kThreads, 0, s>>>(n, dinv, V + (int64_t)j * ld, z);
+      spmv_t<double>(n, avg, A.ia, A.ja, A.a, z, w, s);
+      project(j + 1, w, hc, nullptr);
+      k_msub<<<g, kThreads, 0, s>>>(n, V, ld, j + 1, hc, w);
+      project(j + 1, w, tmp, hc);   // second Gram-Schmidt pass, added into the column
+      k_msub<<<g, kThreads, 0, s>>>(n, V, ld, j + 1, tmp, w);
+      c.dot<double>(n, w, w, nn);
+      k_gmres_normalise<<<g, kThreads, 0, s>>>(n, nn, hc + j + 1, w);
+      double* h = H.data() + (size_t)j * (M + 1);
+      cudaMemcpyAsync(h, hc, (size_t)(j + 2) * sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      its++;
+      for (int i = 0; i < j; i++) {
+        const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+        h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+        h[i] = t;
+      }
+      const double hsub = h[j + 1];
+      const double r = std::hypot(h[j], hsub);
+      if (!std::isfinite(r)) {
+        stop = true;   // a non-finite column: keep the iterate of the last cycle
+        break;
+      }
+      cs[j] = r > 0 ? h[j] / r : 1.0;
+      sn[j] = r > 0 ? hsub / r : 0.0;
+      h[j] = r;
+      h[j + 1] = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      k = j + 1;
+      if (std::fabs(gv[j + 1]) <= rtol * bnorm || !(hsub > 0.0)) break;
+    }
+    // y = R^-1 g (a zero pivot drops its direction)
+    for (int i = k - 1; i >= 0; i--) {
+      double t = gv[i];
+      for (int l = i + 1; l < k; l++) t -= H[(size_t)l * (M + 1) + i] * y[l];
+      const double d = H[(size_t)i * (M + 1) + i];
+      y[i] = d != 0.0 ? t / d : 0.0;
+    }
+    if (k > 0) {
+      cudaMemcpyAsync(yd, y.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
+      k_gmres_x<<<g, kThreads, 0, s>>>(n, V, ld, k, yd, dinv, x);
+      cudaStreamSynchronize(s);   // y leaves scope in the next cycle
+    }
+    if (stop || k == 0) break;
+  }
+  cudaFreeAsync(V, s);
+  cudaFreeAsync(part, s);
+  cudaFreeAsync(hd, s);
+  cudaFreeAsync(tmp, s);
+  cudaFreeAsync(yd, s);
+  return its;
 }
 
 }  // namespace
@@ -505,6 +686,8 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     cudaFreeAsync(wf, s);
     cudaFreeAsync(af, s); cudaFreeAsync(rf, s); cudaFreeAsync(df, s);
     cudaFreeAsync(zf, s); cudaFreeAsync(pf, s); cudaFreeAsync(qf, s);
+  } else if (method == 6) {
+    iters = gmres_core(c, A, b, x, dinv, rtol, max_iter, dscal, z);
   }
   // true residual
   spmv(A, x, ax, s);

@@ -8,7 +8,7 @@
 // reference factorises K_N with PARDISO at every step; here the solve is a
 // Krylov method chosen per call:
 //   0-3  the methods of krylov_solve (Jacobi PCG, block-Jacobi PCG, BiCGStab,
-//        mixed PCG + FP64 refinement)
+//        mixed PCG + FP64 refinement); 6 its restarted GMRES
 //   4    block-Jacobi flexible CG: the plain method the learned one is judged by
 //   5    flexible CG with block-Jacobi plus the learned coarse correction; if
 //        it stalls or needs more iterations than the plain solves did,
@@ -172,7 +172,7 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
   const int maxit = m->cmd.solve_maxit;
   const int bd = m->mesh.dim;
   Learned* L = m->learned;
-  if (method <= 3) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
+  if (method <= 3 || method == 6) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
   if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
   if (L->disabled) return plain_solve(m, b, x, nullptr, kr);
@@ -473,7 +473,7 @@ pdx_status pdx_newmark_init(pdx_model* m) {
 pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_info* info) {
   NEED_DEV(m);
   if (!m->newmark_ready) return set_error(PDX_ERR_INVALID, "pdx_newmark_init first");
-  if (method < 0 || method > 5) return set_error(PDX_ERR_INVALID, "method must be 0..5");
+  if (method < 0 || method > 6) return set_error(PDX_ERR_INVALID, "method must be 0..6");
   const int ne = m->setup.n_eq;
   double* u_all = m->d_u[0];
   double* upred = m->d_u[1];

@@ -149,7 +149,7 @@ def test_newmark_matrix_matches_reference(built):
     assert rel(f, gn["FN"]) < 1e-12
 
 
-@pytest.mark.parametrize("method", [0, 1, 2, 3])
+@pytest.mark.parametrize("method", [0, 1, 2, 3, 6])
 def test_krylov_solves_reference_system(built, method):
     gs = golden("b13_static")
     x, info = pdx.solve_csr(gs["K_ia"], gs["K_ja"], gs["K_a"], gs["F"], method=method, rtol=1e-12,
@@ -167,6 +167,49 @@ def test_krylov_solves_reference_system(built, method):
     else:
         # plain CG on the unsymmetric stiffness may stall; the drivers fall back to BiCGStab
         assert method in (0, 1, 3)
+
+
+def _indefinite_convection_system(nx=40, seed=0):
+    """A shifted, row-scaled 2D convection-diffusion matrix (unsymmetric and
+    indefinite, as the stiffness of a cracked plate can be) with two empty
+    rows and zero right-hand sides there (nodes with every bond broken)."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    eye = sp.identity(nx)
+    t = sp.diags([-1.0, 2.0, -1.0], [-1, 0, 1], (nx, nx))
+    c = sp.diags([-1.0, 0.0, 1.0], [-1, 0, 1], (nx, nx))
+    n = nx * nx
+    a = sp.kron(eye, t) + sp.kron(t, eye) + 4.0 * (sp.kron(eye, c) + sp.kron(c, eye)) - 0.3 * sp.identity(n)
+    a = (sp.diags(np.exp(rng.uniform(-2, 2, n))) @ a).tolil()
+    empty = [5, 777]
+    for i in empty:
+        a[i, :] = 0.0
+        a[:, i] = 0.0
+    a = a.tocsr()
+    a.sort_indices()
+    b = rng.standard_normal(n)
+    b[empty] = 0.0
+    return a, b, empty
+
+
+def test_gmres_solves_where_bicgstab_breaks_down(built):
+    """GMRES(30) (method 6, the drivers' last fallback) solves the indefinite
+    unsymmetric system on which Jacobi BiCGStab breaks down, and leaves the
+    empty rows at zero; checked against a direct solve."""
+    sps = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    a, b, empty = _indefinite_convection_system()
+    ia, ja = a.indptr.astype(np.int64), a.indices.astype(np.int64)
+    _, info2 = pdx.solve_csr(ia, ja, a.data, b, method=2, rtol=1e-10, max_iter=3000)
+    x, info6 = pdx.solve_csr(ia, ja, a.data, b, method=6, rtol=1e-10, max_iter=3000)
+    d = a.diagonal()
+    xd = spla.spsolve((a + sps.diags((d == 0).astype(float))).tocsc(), b)
+    print(f"\nBiCGStab: converged {info2.converged}, residual {info2.rel_residual:.2e}; "
+          f"GMRES: {info6.iterations} iterations, residual {info6.rel_residual:.2e}")
+    assert not info2.converged
+    assert info6.converged and info6.rel_residual <= 1e-10
+    assert np.all(x[empty] == 0.0)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-8
 
 
 def test_static_run_matches_reference_solution(built, tmp_path):
@@ -247,7 +290,7 @@ def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
     assert int((bs32 != bs_o).sum()) <= max(2, int(0.01 * (bs_o == 0).sum()))
 
 
-@pytest.mark.parametrize("method", [1, 2, 3])
+@pytest.mark.parametrize("method", [1, 2, 3, 6])
 def test_quasi_static_increments_match_reference(built, method):
     """Three quasi-static increments, one pdx_quasi_step each, against the
     reference's direct-solve trajectory: the Krylov solves stop at a 1e-8 true
@@ -267,7 +310,9 @@ def test_quasi_static_increments_match_reference(built, method):
             d = m.state()[0].reshape(-1)[free] - gq["u_traj"][i].reshape(-1)[free]
             errs.append(np.linalg.norm(d) / scale)
     print(f"\nmethod {method}: relative L2 error per increment {['%.1e' % e for e in errs]}")
-    assert max(errs) < 1e-6
+    # GMRES stops at the first iteration whose residual is below 1e-8; the
+    # other methods check every 10 iterations and end further below it
+    assert max(errs) < (5e-6 if method == 6 else 1e-6)
 
 
 @pytest.mark.parametrize("cmd", ["p21_fc2", "p21_fc2k"])

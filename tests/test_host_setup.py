@@ -93,9 +93,30 @@ def test_errors_are_returned_not_exit(built, tmp_path):
     with pytest.raises(pdx.PdxError) as e:
         pdx.Model(str(tmp_path / "p.in"), device=-1)
     assert e.value.code == 2
-    _write(tmp_path / "f.in", "MSHFILE m.lis\nSOLVER DYNAMIC\nFC 3\n")
+    _write(tmp_path / "f.in", "MSHFILE m.lis\nSOLVER DYNAMIC\nFC 3 -1\n")
     with pytest.raises(pdx.PdxError):
         pdx.Model(str(tmp_path / "f.in"), device=-1)
+    _write(tmp_path / "g.in", "MSHFILE m.lis\nSOLVER QUASI-STATIC\nSOLVE GMRES 1e-9 400\n")
+    pdx.Model(str(tmp_path / "g.in"), device=-1)
+    _write(tmp_path / "h.in", "MSHFILE m.lis\nSOLVER QUASI-STATIC\nSOLVE LU\n")
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.Model(str(tmp_path / "h.in"), device=-1)
+    assert e.value.code == 2
+    # an unknown Krylov method is refused before any device work
+    ia = np.array([0, 1], np.int64)
+    with pytest.raises(pdx.PdxError) as e:
+        pdx.solve_csr(ia, np.array([0], np.int64), np.array([2.0]), np.array([1.0]), method=5)
+    assert e.value.code == 4
+
+
+def test_bare_fc3_breaks_nothing_as_the_reference(built, tmp_path):
+    """The reference reads FC 3 without a value and breaks no bond with it
+    (its stretch criterion is never called); such decks still run."""
+    mesh = meshgen.plate_strip_crack(n=11, L=0.01)
+    meshgen.write_case(mesh, str(tmp_path), "b", solver="DYNAMIC", dt=1e-8, nsteps=2, save=2, factor=3.015, nlf=1.0,
+                       fc="3")
+    m = pdx.Model(str(tmp_path / "b.in"), device=-1)
+    assert m.info.fail_flag == 0
 
 
 def test_duplicate_dof_and_unsupported_elements(built, tmp_path):
