@@ -19,8 +19,20 @@ def main(inp: str, out: str) -> None:
     ja = np.frombuffer(raw, dtype=np.int64, count=nnz, offset=off); off += 8 * nnz
     a = np.frombuffer(raw, dtype=np.float64, count=nnz, offset=off); off += 8 * nnz
     b = np.frombuffer(raw, dtype=np.float64, count=n, offset=off)
-    A = sp.csr_matrix((a, ja, ia), shape=(n, n)).tocsc()
-    x = spla.splu(A, permc_spec="COLAMD").solve(b.copy())
+    A = sp.csr_matrix((a, ja, ia), shape=(n, n))
+    # PARDISO in the reference perturbs zero pivots (iparm[9] = 13,
+    # calMatrixOperations.cpp:292): an empty row (a node whose bonds are all
+    # broken) with a zero right-hand side then solves to 0.  SuperLU stops on
+    # an exactly singular factor instead, so such rows get a unit diagonal,
+    # which gives the same 0.
+    empty = np.diff(A.indptr) == 0
+    rowsum = np.asarray(abs(A).sum(axis=1)).ravel()
+    empty |= rowsum == 0
+    if empty.any():
+        if np.any(b[empty] != 0):
+            raise SystemExit("empty stiffness row with a nonzero load")
+        A = A + sp.diags(empty.astype(np.float64))
+    x = spla.splu(A.tocsc(), permc_spec="COLAMD").solve(b.copy())
     np.asarray(x, dtype=np.float64).tofile(out)
 
 
