@@ -13,6 +13,7 @@
 #include <iomanip>
 #include <string>
 #include <sys/stat.h>
+#include <thread>
 #include <vector>
 
 #include "model_impl.h"
@@ -39,6 +40,67 @@ pdx_status fetch(pdx_model* m, const double* d_u, HostState& h) {
 std::string out_name(const pdx_model* m, const std::string& dir, const std::string& tag) {
   return dir + "/" + m->mesh.title + "_" + tag + ".vtk";
 }
+
+// Result files written on a host thread while the GPU steps on.  The state of
+// a save step (u, the nodal stresses and damage already computed on the
+// device) is copied into pinned host buffers on the model's stream, so the
+// copy is ordered after that step and before the next one overwrites it; the
+// thread waits for the copy's event, then formats and writes the files.  Two
+// buffer sets alternate, and a set is reused only after its last write ends.
+class AsyncWriter {
+ public:
+  explicit AsyncWriter(pdx_model* m) : m_(m) {
+    const size_t N = (size_t)m->mesh.n_node;
+    nu_ = N * m->mesh.dim;
+    ns_ = N * 6;
+    np_ = N;
+    for (Slot& s : slot_) {
+      if (cudaMallocHost(&s.buf, (nu_ + ns_ + np_) * sizeof(double)) != cudaSuccess) s.buf = nullptr;
+      if (cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming) != cudaSuccess) s.ev = nullptr;
+    }
+  }
+  ~AsyncWriter() {
+    finish();
+    for (Slot& s : slot_) {
+      if (s.buf) cudaFreeHost(s.buf);
+      if (s.ev) cudaEventDestroy(s.ev);
+    }
+  }
+  pdx_status submit(const double* d_u, const std::string& path) {
+    Slot& s = slot_[next_];
+    next_ ^= 1;
+    if (s.th.joinable()) s.th.join();
+    if (!s.buf || !s.ev) return set_error(PDX_ERR_CUDA, "pinned result buffers");
+    cudaMemcpyAsync(s.buf, d_u, nu_ * 8, cudaMemcpyDeviceToHost, m_->stream);
+    cudaMemcpyAsync(s.buf + nu_, m_->d_sigma, ns_ * 8, cudaMemcpyDeviceToHost, m_->stream);
+    cudaMemcpyAsync(s.buf + nu_ + ns_, m_->d_phi, np_ * 8, cudaMemcpyDeviceToHost, m_->stream);
+    pdx_status st = cuda_check(cudaEventRecord(s.ev, m_->stream), "result copy");
+    if (st) return st;
+    const bool binary = m_->cmd.vtk_binary;
+    s.th = std::thread([this, &s, path, binary] {
+      if (cudaEventSynchronize(s.ev) != cudaSuccess) return;
+      const std::vector<double> u(s.buf, s.buf + nu_), sig(s.buf + nu_, s.buf + nu_ + ns_),
+          phi(s.buf + nu_ + ns_, s.buf + nu_ + ns_ + np_);
+      write_vtk(m_, path, u, sig, phi, binary);
+    });
+    return PDX_OK;
+  }
+  void finish() {
+    for (Slot& s : slot_)
+      if (s.th.joinable()) s.th.join();
+  }
+
+ private:
+  struct Slot {
+    double* buf = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::thread th;
+  };
+  pdx_model* m_;
+  size_t nu_ = 0, ns_ = 0, np_ = 0;
+  Slot slot_[2];
+  int next_ = 0;
+};
 
 pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int method, KrylovResult* kr) {
   DevCsr A;
@@ -106,18 +168,18 @@ pdx_status run_explicit(pdx_model* m, const std::string& dir) {
   if (st) return st;
   const int nsteps = m->cmd.nsteps, save = std::max(1, m->cmd.save_freq);
   int n = 0;
+  AsyncWriter writer(m);
   while (n < nsteps) {
     int next = std::min(nsteps, (n / save + 1) * save);
     st = pdx_explicit_advance(m, next - n);
     if (st) return st;
     n = next;
-    HostState h;
-    st = pdx_get_state(m, nullptr, nullptr, nullptr, nullptr);
+    st = pdx_get_state(m, nullptr, nullptr, nullptr, nullptr);   // stresses and damage on the device
     if (st) return st;
-    st = fetch(m, m->d_u[m->cur], h);
+    st = writer.submit(m->d_u[m->cur], out_name(m, dir, std::to_string(n)));
     if (st) return st;
-    write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
   }
+  writer.finish();
   return write_rf(m, dir, 0, false);
 }
 
@@ -223,22 +285,22 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
   double* u_all = m->d_u[0];
   m->cur = 0;
   m->quasi_load = 0;
+  AsyncWriter writer(m);
   for (int n = 1; n <= m->cmd.nsteps; n++) {
     KrylovResult kr;
     st = quasi_increment(m, n, m->cmd.solve_method, &kr, nullptr);
     if (!st) st = rf_record(m, n);
     if (st) return st;
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps || n == 1) {
-      HostState h;
-      st = fetch(m, u_all, h);
+      st = writer.submit(u_all, out_name(m, dir, std::to_string(n)));
       if (st) return st;
-      write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
     }
     st = quasi_advance(m);
     if (st) return st;
   }
   st = cuda_check(cudaStreamSynchronize(m->stream), "quasi-static");
   if (st) return st;
+  writer.finish();
   return write_rf(m, dir, 1, true);
 }
 
@@ -255,6 +317,7 @@ pdx_status run_newmark(pdx_model* m, const std::string& dir) {
   double* upred = m->d_u[1];
   cudaMemsetAsync(vel, 0, (size_t)ne * 8, m->stream);
   cudaMemsetAsync(acc, 0, (size_t)ne * 8, m->stream);
+  AsyncWriter writer(m);
   for (int n = 1; n <= m->cmd.nsteps; n++) {
     st = cuda_check(launch_newmark_predict(m->view, u_all, vel, acc, m->cmd.dt, m->cmd.beta, upred, m->stream),
                     "Newmark predictor");
@@ -277,14 +340,13 @@ pdx_status run_newmark(pdx_model* m, const std::string& dir) {
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps) {
       st = model_stress(m, u_all, true, true);
       if (st) return st;
-      HostState h;
-      st = fetch(m, u_all, h);
+      st = writer.submit(u_all, out_name(m, dir, std::to_string(n)));
       if (st) return st;
-      write_vtk(m, out_name(m, dir, std::to_string(n)), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
     }
   }
   st = cuda_check(cudaStreamSynchronize(m->stream), "Newmark");
   if (st) return st;
+  writer.finish();
   return write_rf(m, dir, 1, false);
 }
 

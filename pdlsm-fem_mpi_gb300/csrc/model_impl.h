@@ -186,6 +186,9 @@ pdx_status set_error(pdx_status code, const std::string& msg);
 pdx_status cuda_check(cudaError_t e, const char* what);
 void write_vtk(const pdx_model* m, const std::string& path, const std::vector<double>& u_all,
                const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);
+// <base>.sig and <base>.disp, the text files beside an ASCII VTK result
+void write_sig_disp(const pdx_model* m, const std::string& base, const std::vector<double>& u_all,
+                    const std::vector<double>& sigma);
 pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi);
 pdx_status rf_record(pdx_model* m, int64_t row);
 // FC 2 pass on the current state; with `report` it also reads back how many

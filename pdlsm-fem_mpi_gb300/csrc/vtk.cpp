@@ -120,6 +120,46 @@ void write_vtk(const pdx_model* m, const std::string& path, const std::vector<do
     f << float(phi[k]) << ' ';
     if (k % 20 == 0) f << std::endl;
   }
+  f.close();
+  // an ASCII result also writes <title>_<step>.sig and .disp beside it
+  const std::string base = path.size() > 4 ? path.substr(0, path.size() - 4) : path;
+  write_sig_disp(m, base, u_all, sigma);
+}
+
+// fioFiles::writeSigofNode and writeUofNode (fioFile.cpp:486-503, 528-547)
+// with the rows of pdNode::printStress and printFinalU (pdNode.cpp:92-103,
+// 120-130): one row per node, node id (1-based), coordinates, then the six
+// stresses (scientific, 5 digits) or the three displacements (scientific, 4
+// digits; the z entry of a 2D node is its unused third DOF, 0).
+void write_sig_disp(const pdx_model* m, const std::string& base, const std::vector<double>& u_all,
+                    const std::vector<double>& sigma) {
+  const Mesh& me = m->mesh;
+  const int N = me.n_node, D = me.dim;
+  {
+    std::ofstream f(base + ".sig");
+    f << "*****The stress of  point*****" << std::endl;
+    f << std::left;
+    f << "NID" << "\t" << "x" << "\t" << "y" << "\t" << "z" << "\t" << "Sxx" << "\t" << "Syy" << "\t" << "Szz" << "\t"
+      << "Sxy" << "\t" << "Syz" << "\t" << "Szx" << std::endl;
+    f << std::setiosflags(std::ios::scientific) << std::setprecision(5);
+    for (int k = 0; k < N; k++) {
+      f << k + 1 << "\t";
+      f << me.X[(size_t)k * 3] << "\t" << me.X[(size_t)k * 3 + 1] << "\t" << me.X[(size_t)k * 3 + 2];
+      for (int j = 0; j < 6; j++) f << "\t" << sigma[(size_t)k * 6 + j];
+      f << std::endl;
+    }
+  }
+  std::ofstream f(base + ".disp");
+  f << "*****The final displacement of  point*****" << std::endl;
+  f << std::left;
+  f << "ID" << "\t" << "x" << "\t" << "y" << "\t" << "z" << "\t" << "Ux" << "\t" << "Uy" << "\t" << "Uz" << std::endl;
+  f << std::setiosflags(std::ios::scientific) << std::setprecision(4);
+  for (int k = 0; k < N; k++) {
+    f << k + 1 << "\t" << me.X[(size_t)k * 3] << "\t" << me.X[(size_t)k * 3 + 1] << "\t" << me.X[(size_t)k * 3 + 2]
+      << "\t";
+    f << u_all[(size_t)k * D] << "\t" << u_all[(size_t)k * D + 1] << "\t" << (D == 3 ? u_all[(size_t)k * D + 2] : 0.0)
+      << std::endl;
+  }
 }
 
 }  // namespace pdx

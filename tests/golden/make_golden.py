@@ -8,7 +8,7 @@ The case inputs (.lis/.in) are copied here too, so the tests can rebuild the
 same models without the reference.
 
 Needs the reference tree (default /root/reference) and SciPy; it is run by
-hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only]
+hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
 """
 from __future__ import annotations
 
@@ -190,13 +190,56 @@ def rf_cases() -> None:
     shutil.rmtree(work)
 
 
+def solve_run(case_dir: str, cmd: str) -> None:
+    """The reference's own pdfemSolver on `cmd`; its build here stops with
+    SIGSEGV in about one run in eight (its output is identical whenever it
+    finishes), so a crashed run is repeated, up to five times."""
+    env = dict(os.environ, PDX_SPSOLVE_SCRIPT=os.path.join(REPO, "oracle", "ref", "spsolve.py"))
+    for attempt in range(5):
+        res = os.path.join(case_dir, "Results")
+        shutil.rmtree(res, ignore_errors=True)
+        os.makedirs(res)
+        rc = subprocess.run([DRIVER, "solve", cmd], cwd=case_dir, env=env, stdout=subprocess.DEVNULL).returncode
+        if rc == 0:
+            return
+        if rc != -11:
+            raise RuntimeError(f"reference solve of {cmd} failed ({rc})")
+    raise RuntimeError(f"reference solve of {cmd} crashed five times")
+
+
+def ascii_cases() -> None:
+    """VTKFORMAT ASCII: the reference's own pdfemSolver (explicit, FC 2 with
+    all candidates, 60 steps) writes an ASCII VTK file and the .sig and .disp
+    text files at every save step; the files of the last step are kept, and
+    the BINARY VTK file of the same run (p21_60_binary.vtk)."""
+    work = tempfile.mkdtemp(prefix="golden_ascii_")
+    d2 = os.path.join(work, "p21")
+    m = plate_case()
+    m.sigult = 3e7
+    meshgen.write_case(m, d2, "p21_ascii", solver="DYNAMIC", dt=5e-8, nsteps=60, save=20, factor=3.015, nlf=1.0,
+                       fc="2 0", vtk="ASCII")
+    copy_inputs(d2, "p21")
+    solve_run(d2, "p21_ascii.in")
+    dst = os.path.join(HERE, "p21_ascii")
+    os.makedirs(dst, exist_ok=True)
+    for ext in ("vtk", "sig", "disp"):
+        shutil.copy(os.path.join(d2, "Results", f"p21_60.{ext}"), dst)
+    meshgen.write_case(m, d2, "p21_ascii", solver="DYNAMIC", dt=5e-8, nsteps=60, save=20, factor=3.015, nlf=1.0,
+                       fc="2 0", vtk="BINARY")
+    solve_run(d2, "p21_ascii.in")
+    shutil.copy(os.path.join(d2, "Results", "p21_60.vtk"), os.path.join(dst, "p21_60_binary.vtk"))
+    shutil.rmtree(work)
+
+
 if __name__ == "__main__":
-    if "--fc2-only" in sys.argv or "--rf-only" in sys.argv:
+    if "--fc2-only" in sys.argv or "--rf-only" in sys.argv or "--ascii-only" in sys.argv:
         build_driver()
         if "--fc2-only" in sys.argv:
             fc2_cases()
         if "--rf-only" in sys.argv:
             rf_cases()
+        if "--ascii-only" in sys.argv:
+            ascii_cases()
     else:
         main()
         fc2_cases()

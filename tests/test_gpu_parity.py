@@ -3,6 +3,7 @@ C ABI.  Tolerances: FP64 path 1e-10 relative L2 for displacement and stress
 (the bar for the plain FP64 path), 1e-12 for single force/assembly
 evaluations; broken-bond sets identical.  Mixed precision states its error."""
 import os
+import shutil
 import tempfile
 
 import numpy as np
@@ -224,6 +225,74 @@ def test_static_run_matches_reference_solution(built, tmp_path):
     n = len(gs["u"])
     U = np.frombuffer(raw, ">f4", 3 * n, j + 1).reshape(n, 3).astype(np.float64)
     assert rel(U, gs["u"]) < 1e-6   # float32 file, Krylov solve to 1e-8
+
+
+def _text_lines_agree(mine: str, ref: str, rtol: float):
+    """Same lines and tokens; numbers equal up to the printed precision (a
+    last-digit difference where the FP64 states differ by ~1e-15 and the
+    rounding boundary falls between them), or within 1e-9 of the largest
+    number on the line (round-off noise such as 1e-23 beside 6e-6).
+    Returns the number of differing lines."""
+    a, b = mine.splitlines(), ref.splitlines()
+    assert len(a) == len(b)
+    differ = 0
+    for la, lb in zip(a, b):
+        if la == lb:
+            continue
+        differ += 1
+        ta, tb = la.split(), lb.split()
+        assert len(ta) == len(tb), (la, lb)
+        scale = max(abs(float(y)) for y in tb)
+        for x, y in zip(ta, tb):
+            if x != y:
+                fx, fy = float(x), float(y)
+                assert abs(fx - fy) <= rtol * max(abs(fx), abs(fy)) + 1e-9 * scale, (la, lb)
+    return differ
+
+
+def test_ascii_results_match_reference_files(built, tmp_path):
+    """VTKFORMAT ASCII: pdx_run writes the ASCII VTK file and the .sig and
+    .disp text files at each save step, as the reference's own solver does
+    (explicit, FC 2 with all candidates, 60 steps; the files of step 60 are
+    the reference's, written by its pdfemSolver)."""
+    gdir = os.path.join(os.path.dirname(__file__), "golden", "p21_ascii")
+    with pdx.Model(case_cmd("p21", "p21_ascii"), device=0, precision=0) as m:
+        m.run(str(tmp_path))
+    for ext, rtol in (("vtk", 2e-4), ("sig", 2e-5), ("disp", 2e-4)):
+        mine = open(os.path.join(tmp_path, f"p21_60.{ext}")).read()
+        ref = open(os.path.join(gdir, f"p21_60.{ext}")).read()
+        differ = _text_lines_agree(mine, ref, rtol)
+        print(f"\n{ext}: {differ} of {len(ref.splitlines())} lines differ in the last digit")
+        assert differ <= 0.01 * len(ref.splitlines())
+    for n in (20, 40):
+        for ext in ("vtk", "sig", "disp"):
+            assert os.path.exists(os.path.join(tmp_path, f"p21_{n}.{ext}"))
+
+
+def test_binary_vtk_matches_reference_file(built, tmp_path):
+    """VTKFORMAT BINARY, same run: header, points and cells byte for byte as
+    the reference's file; U, sigma and phi (big-endian float32) equal up to
+    the float32 rounding of FP64 states that agree to ~1e-15."""
+    src = os.path.join(os.path.dirname(__file__), "golden", "cases", "p21")
+    text = open(os.path.join(src, "p21_ascii.in")).read().replace("VTKFORMAT ASCII", "VTKFORMAT BINARY")
+    with open(os.path.join(tmp_path, "p21_bin.in"), "w") as f:
+        f.write(text)
+    shutil.copy(os.path.join(src, "p21_ascii.lis"), tmp_path)
+    out = tmp_path / "out"
+    out.mkdir()
+    with pdx.Model(str(tmp_path / "p21_bin.in"), device=0, precision=0) as m:
+        n = m.info.n_node
+        m.run(str(out))
+    mine = open(out / "p21_60.vtk", "rb").read()
+    ref = open(os.path.join(os.path.dirname(__file__), "golden", "p21_ascii", "p21_60_binary.vtk"), "rb").read()
+    assert len(mine) == len(ref)
+    cut = ref.index(b"VECTORS U")
+    assert mine[:cut] == ref[:cut]
+    for key, count in ((b"VECTORS U", 3 * n), (b"TENSORS sigma", 9 * n), (b"LOOKUP_TABLE", n)):
+        i, j = ref.index(key), mine.index(key)
+        a = np.frombuffer(mine, ">f4", count, mine.index(b"\n", j) + 1).astype(np.float64)
+        b = np.frombuffer(ref, ">f4", count, ref.index(b"\n", i) + 1).astype(np.float64)
+        assert np.all(np.abs(a - b) <= 2.4e-7 * np.abs(b) + 1e-9 * np.abs(b).max()), key
 
 
 def test_step_host_equals_device_resident(built):
