@@ -513,7 +513,11 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
   const auto t0 = clk::now();
   bool ok = read_command(cmd_path, m->cmd, m->mesh, m->base_dir, err);
   const auto t1 = clk::now();
-  ok = ok && build_setup(m->mesh, m->cmd, m->setup, err);
+  // with a device the family search runs on it; a host-only model (device
+  // -1) keeps the host search
+  int n_dev = 0;
+  const int fam_dev = o.device >= 0 && cudaGetDeviceCount(&n_dev) == cudaSuccess && o.device < n_dev ? o.device : -1;
+  ok = ok && build_setup(m->mesh, m->cmd, m->setup, err, fam_dev);
   const auto t2 = clk::now();
   ok = ok && prepare_model(m, err);
   const auto t3 = clk::now();
@@ -527,6 +531,7 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
     pdx_status code = err.code == 1 ? PDX_ERR_IO
                       : err.code == 3 ? PDX_ERR_UNSUPPORTED
                       : err.code == 6 ? PDX_ERR_SINGULAR
+                      : err.code == 7 ? PDX_ERR_CUDA
                                       : PDX_ERR_PARSE;
     return set_error(code, err.msg);
   }

@@ -141,7 +141,7 @@ bool update_pde_by_crack(Ctx& cx, const std::array<double, 9>& cr, Error& err) {
 
 }  // namespace
 
-bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err) {
+bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int device) {
   const int D = m.dim, N = m.n_node, E = m.n_elem;
   s = Setup();
   s.dim = D;
@@ -316,8 +316,12 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err) {
   std::vector<double> delta_node(N);
   for (int k = 0; k < N; k++) delta_node[k] = cmd.factor * std::pow(s.vol_node[k], 1.0 / D);
   const double md = s.min_delta;
-  s.fam_off.assign(1, 0);
-  for (int f = 0; f < nf; f++) {
+  if (device >= 0) {
+    // the same search, one warp per family, on the model's GPU (k_setup.cu)
+    if (!gpu_family_search(m, s, delta_node, md, device, err)) return false;
+  }
+  if (device < 0) s.fam_off.assign(1, 0);
+  for (int f = 0; f < nf && device < 0; f++) {
     const int k = s.fam_node[f];
     const double dk = s.fam_delta[f];
     const double* xk = &m.X[(size_t)k * 3];

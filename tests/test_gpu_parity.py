@@ -295,6 +295,37 @@ def test_binary_vtk_matches_reference_file(built, tmp_path):
         assert np.all(np.abs(a - b) <= 2.4e-7 * np.abs(b) + 1e-9 * np.abs(b).max()), key
 
 
+@pytest.mark.parametrize("case,cmd", [("p21", "p21_explicit"), ("b13", "b13_explicit")])
+def test_gpu_family_search_equals_host_and_reference(built, case, cmd):
+    """A model with a device builds its families on the GPU: the member lists
+    (order included), offsets, pre-crack bond states and CSR pattern equal the
+    host search's and the reference's set-up dump."""
+    g = golden(case + "_setup")
+    host = pdx.Model(case_cmd(case, cmd), device=-1)
+    with pdx.Model(case_cmd(case, cmd), device=0) as dev:
+        for name in ("fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja"):
+            np.testing.assert_array_equal(dev.array(name), host.array(name))
+        np.testing.assert_array_equal(dev.array("fam_members") + 1, g["fam_members"])
+        np.testing.assert_array_equal(dev.array("fam_off"), g["fam_off"])
+
+
+def test_gpu_family_search_full_size(built):
+    """C2 (151,284 nodes, 31,584 families, 3.53M bonds): GPU and host family
+    lists are identical; the set-up times are printed."""
+    import time
+    d = tempfile.mkdtemp()
+    mesh, kw = meshgen.config_c2(nsteps=2)
+    cmd = meshgen.write_case(mesh, d, "c2", **kw)
+    t0 = time.perf_counter()
+    host = pdx.Model(cmd, device=-1)
+    t1 = time.perf_counter()
+    with pdx.Model(cmd, device=0, verbose=2) as dev:
+        t2 = time.perf_counter()
+        for name in ("fam_off", "fam_members", "bond_state0"):
+            np.testing.assert_array_equal(dev.array(name), host.array(name))
+    print(f"\nC2 set-up: host-only model {t1 - t0:.2f} s, model with device {t2 - t1:.2f} s")
+
+
 def test_step_host_equals_device_resident(built):
     cmd = case_cmd("b13", "b13_explicit")
     with pdx.Model(cmd, device=0, precision=0) as a, pdx.Model(cmd, device=0, precision=0) as b:
