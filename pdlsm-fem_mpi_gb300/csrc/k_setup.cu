@@ -11,6 +11,7 @@
 // count pass gives the offsets, a fill pass writes the members.  Distances
 // use the host's operation order with explicit round-to-nearest products and
 // sums (no fused multiply-add), so every borderline decision is the host's.
+#include <climits>
 #include <cstdint>
 #include <vector>
 
@@ -81,6 +82,74 @@ __global__ void __launch_bounds__(256) k_family(FamArgs a) {
         }
       }
   if (!kFill && lane == 0) a.count[f] = (int)pos;
+}
+
+// CSR pattern (build_csr_pattern in setup.cpp): node k interacts with the
+// sorted, unique union of its family members and the nodes of its FE
+// elements; each active DOF row of k holds the active DOFs of those nodes.
+// One warp per node emits the union in increasing order by repeated warp
+// minima over the candidates above the last one emitted (a node has at most
+// a few hundred candidates), counting the row length in the count pass and
+// writing the columns of all of k's rows in the fill pass.
+struct PatArgs {
+  int n_node, dim;
+  const int* fam_of_node;
+  const int64_t* fam_off;
+  const int* fam_members;
+  const int* ne_ptr;    // FE elements of node k: ne_list[ne_ptr[k] .. ne_ptr[k+1])
+  const int* ne_list;
+  const int* conn;      // 8 per element
+  const int* elem_nn;
+  const int* eq;        // n_node x dim, -1 for prescribed DOFs
+  int64_t* rowlen;      // count pass: columns of each of node k's rows
+  const int64_t* ia;    // fill pass
+  int64_t* ja;
+};
+
+template <bool kFill>
+__global__ void __launch_bounds__(256) k_pattern(PatArgs a) {
+  const int k = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= a.n_node) return;   // whole warps leave together
+  const int D = a.dim;
+  const int f = a.fam_of_node[k];
+  const int64_t fb = f >= 0 ? a.fam_off[f] : 0;
+  const int nfam = f >= 0 ? (int)(a.fam_off[f + 1] - fb) : 0;
+  const int e0 = a.ne_ptr[k];
+  const int total = nfam + (a.ne_ptr[k + 1] - e0) * 8;
+  int64_t base = 0;   // fill pass: row start of lane's DOF (lanes < D)
+  bool row = false;
+  if (kFill && lane < D) {
+    const int r = a.eq[(size_t)k * D + lane];
+    row = r >= 0;
+    if (row) base = a.ia[r];
+  }
+  int64_t p = 0;
+  int last = -1;
+  while (true) {
+    int best = INT_MAX;
+    for (int t = lane; t < total; t += 32) {
+      int v;
+      if (t < nfam) {
+        v = a.fam_members[fb + t];
+      } else {
+        const int q = t - nfam;
+        const int e = a.ne_list[e0 + (q >> 3)];
+        v = (q & 7) < a.elem_nn[e] ? a.conn[(size_t)e * 8 + (q & 7)] : INT_MAX;
+      }
+      if (v > last && v < best) best = v;
+    }
+    best = __reduce_min_sync(0xffffffffu, best);
+    if (best == INT_MAX) break;
+    last = best;
+    for (int jj = 0; jj < D; jj++) {
+      const int c = a.eq[(size_t)best * D + jj];
+      if (c < 0) continue;
+      if (kFill && row) a.ja[base + p] = c;
+      p++;
+    }
+  }
+  if (!kFill && lane == 0) a.rowlen[k] = p;
 }
 
 struct DevArrays {
@@ -160,6 +229,86 @@ bool gpu_family_search(const Mesh& m, Setup& s, const std::vector<double>& delta
         if (nf) k_family<true><<<grid, threads, 0, st>>>(a);
         if (!s.fam_members.empty())
           cudaMemcpyAsync(s.fam_members.data(), dm, s.fam_members.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        ok = e == cudaSuccess;
+      } else {
+        e = cudaErrorMemoryAllocation;
+      }
+    }
+  }
+  cudaStreamDestroy(st);
+  if (!ok) return fail("kernel", e);
+  return true;
+}
+
+bool gpu_csr_pattern(const Mesh& m, Setup& s, int device, Error& err) {
+  auto fail = [&](const char* what, cudaError_t e) {
+    err.code = 7;
+    err.msg = std::string("CSR pattern on the GPU: ") + what + ": " + cudaGetErrorString(e);
+    return false;
+  };
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail("device", e);
+  const int N = m.n_node, D = m.dim;
+  // FE elements of every node
+  std::vector<int> ne_ptr((size_t)N + 1, 0), ne_list;
+  for (int el : s.fe)
+    for (int j = 0; j < m.elem_nn[el]; j++) ne_ptr[(size_t)m.conn[(size_t)el * 8 + j] + 1]++;
+  for (int k = 0; k < N; k++) ne_ptr[(size_t)k + 1] += ne_ptr[k];
+  ne_list.resize((size_t)ne_ptr[N]);
+  {
+    std::vector<int> at(ne_ptr.begin(), ne_ptr.end() - 1);
+    for (int el : s.fe)
+      for (int j = 0; j < m.elem_nn[el]; j++) ne_list[(size_t)at[m.conn[(size_t)el * 8 + j]]++] = el;
+  }
+  cudaStream_t st;
+  if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
+  bool ok = false;
+  {
+    DevArrays d;
+    PatArgs a{};
+    a.n_node = N;
+    a.dim = D;
+    a.fam_of_node = d.put(s.fam_of_node.data(), s.fam_of_node.size(), st);
+    a.fam_off = d.put(s.fam_off.data(), s.fam_off.size(), st);
+    a.fam_members = d.put(s.fam_members.data(), s.fam_members.size(), st);
+    a.ne_ptr = d.put(ne_ptr.data(), ne_ptr.size(), st);
+    a.ne_list = d.put(ne_list.data(), ne_list.size(), st);
+    a.conn = d.put(m.conn.data(), m.conn.size(), st);
+    a.elem_nn = d.put(m.elem_nn.data(), m.elem_nn.size(), st);
+    a.eq = d.put(s.eq.data(), s.eq.size(), st);
+    std::vector<int64_t> rowlen((size_t)N);
+    a.rowlen = d.put(rowlen.data(), rowlen.size(), st);
+    if (!a.fam_of_node || !a.fam_off || !a.fam_members || !a.ne_ptr || !a.ne_list || !a.conn || !a.elem_nn || !a.eq ||
+        !a.rowlen) {
+      cudaStreamDestroy(st);
+      return fail("allocation", cudaErrorMemoryAllocation);
+    }
+    const int threads = 256;
+    const int grid = (int)(((int64_t)N * 32 + threads - 1) / threads);
+    if (N) k_pattern<false><<<grid, threads, 0, st>>>(a);
+    if (N) cudaMemcpyAsync(rowlen.data(), a.rowlen, (size_t)N * 8, cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) {
+      // rows in equation order: node-major, DOF-minor
+      s.csr_ia.assign((size_t)s.n_eq + 1, 0);
+      for (int k = 0; k < N; k++)
+        for (int i = 0; i < D; i++) {
+          const int r = s.eq[(size_t)k * D + i];
+          if (r >= 0) s.csr_ia[(size_t)r + 1] = rowlen[k];
+        }
+      for (int r = 0; r < s.n_eq; r++) s.csr_ia[(size_t)r + 1] += s.csr_ia[r];
+      s.csr_ja.assign((size_t)s.csr_ia[s.n_eq], 0);
+      a.ia = d.put(s.csr_ia.data(), s.csr_ia.size(), st);
+      int64_t* dja = nullptr;
+      if (a.ia && cudaMalloc(&dja, (s.csr_ja.size() ? s.csr_ja.size() : 1) * 8) == cudaSuccess) {
+        d.ptrs.push_back(dja);
+        a.ja = dja;
+        if (N) k_pattern<true><<<grid, threads, 0, st>>>(a);
+        if (!s.csr_ja.empty())
+          cudaMemcpyAsync(s.csr_ja.data(), dja, s.csr_ja.size() * 8, cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e == cudaSuccess) e = cudaGetLastError();
         ok = e == cudaSuccess;

@@ -117,12 +117,15 @@ bool read_command(const std::string& path, Command& cmd, Mesh& mesh, std::string
 bool read_mesh(const std::string& path, Mesh& mesh, Error& err);
 
 // setup (pdsolve::setDatModel restated)
-// device >= 0: the family member search runs on that GPU (identical lists)
+// device >= 0: the family member search and the CSR pattern run on that GPU
+// (identical results)
 bool build_setup(const Mesh& mesh, const Command& cmd, Setup& s, Error& err, int device = -1);
 // family members and offsets of s.fam_node on the GPU, in the host loop's
 // order; err.code 7 on a CUDA failure (k_setup.cu)
 bool gpu_family_search(const Mesh& m, Setup& s, const std::vector<double>& delta_node, double md, int device,
                        Error& err);
+// csr_ia / csr_ja of build_csr_pattern on the GPU, identical (k_setup.cu)
+bool gpu_csr_pattern(const Mesh& m, Setup& s, int device, Error& err);
 void build_csr_pattern(const Mesh& mesh, Setup& s);
 
 // element utilities (fe_host.cpp)

@@ -367,6 +367,7 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int de
           }
         }
   }
+  if (device >= 0) return gpu_csr_pattern(m, s, device, err);   // k_setup.cu
   build_csr_pattern(m, s);
   return true;
 }

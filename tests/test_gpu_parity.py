@@ -297,7 +297,7 @@ def test_binary_vtk_matches_reference_file(built, tmp_path):
 
 @pytest.mark.parametrize("case,cmd", [("p21", "p21_explicit"), ("b13", "b13_explicit")])
 def test_gpu_family_search_equals_host_and_reference(built, case, cmd):
-    """A model with a device builds its families on the GPU: the member lists
+    """A model with a device builds its families and CSR pattern on the GPU: the member lists
     (order included), offsets, pre-crack bond states and CSR pattern equal the
     host search's and the reference's set-up dump."""
     g = golden(case + "_setup")
@@ -310,8 +310,9 @@ def test_gpu_family_search_equals_host_and_reference(built, case, cmd):
 
 
 def test_gpu_family_search_full_size(built):
-    """C2 (151,284 nodes, 31,584 families, 3.53M bonds): GPU and host family
-    lists are identical; the set-up times are printed."""
+    """C2 (151,284 nodes, 31,584 families, 3.53M bonds, 59.4M nonzeros): GPU
+    and host family lists and CSR pattern are identical; the set-up times are
+    printed."""
     import time
     d = tempfile.mkdtemp()
     mesh, kw = meshgen.config_c2(nsteps=2)
@@ -321,7 +322,7 @@ def test_gpu_family_search_full_size(built):
     t1 = time.perf_counter()
     with pdx.Model(cmd, device=0, verbose=2) as dev:
         t2 = time.perf_counter()
-        for name in ("fam_off", "fam_members", "bond_state0"):
+        for name in ("fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja"):
             np.testing.assert_array_equal(dev.array(name), host.array(name))
     print(f"\nC2 set-up: host-only model {t1 - t0:.2f} s, model with device {t2 - t1:.2f} s")
 
