@@ -361,6 +361,9 @@ class Model:
 
 def solve_csr(ia: np.ndarray, ja: np.ndarray, a: np.ndarray, b: np.ndarray, method: int = 2,
               rtol: float = 1e-8, max_iter: int = 20000, x0: Optional[np.ndarray] = None):
+    """Solve A x = b on the GPU (pdx_solve_csr).  method: 0 Jacobi PCG,
+    1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 FP32 PCG in FP64 refinement,
+    6 GMRES(30) (right Jacobi).  Returns (x, SolveInfo)."""
     n = len(ia) - 1
     ia = np.ascontiguousarray(ia, dtype=np.int64)
     ja = np.ascontiguousarray(ja, dtype=np.int64)
