@@ -261,7 +261,10 @@ def make_workload(tmp: str, nsteps: int, precision: str):
 
 
 def algorithmic_bytes(model) -> dict:
-    """Unique bytes one step must move (the design doc gives the per-unit figures)."""
+    """Unique bytes one step must move: per bond its member index, stored
+    coefficients and state bit; per bond of a PD-boundary family its
+    correction block; per node its displacements, velocity, mass and force
+    state; per FE element its node ids."""
     info = model.info
     mixed = info.precision == 1
     cs = 4 if mixed else 8

@@ -212,7 +212,7 @@ pdx_status pdx_learned_probe(pdx_model* m, int nprobe, uint64_t seed);
 pdx_status pdx_learned_options(pdx_model* m, int trunc, int stall_window);
 /* 1 while method 5 uses the learned correction: the network is trained and
  * has not been switched off.  Plain block-Jacobi flexible CG (method 4) is
- * the judge: a learned solve is cut at the mean iteration count of the plain
+ * the arbiter: a learned solve is cut at the mean iteration count of the plain
  * Newmark solves (plain FCG finishes it), and after two learned solves in a
  * row slower than the mean plain solve (by time where plain solves that
  * collected nothing were timed, else by iterations) method 5 runs the plain

@@ -13,7 +13,7 @@
 //   5    flexible CG with block-Jacobi plus the learned coarse correction; if
 //        it stalls or needs more iterations than the plain solves did,
 //        block-Jacobi flexible CG and then BiCGStab take over from the current
-//        iterate.  Plain block-Jacobi FCG is also the judge: after two learned
+//        iterate.  Plain block-Jacobi FCG is also the arbiter: after two learned
 //        solves in a row slower than the plain ones, method 5 runs the plain
 //        method until the network is retrained (pdx_learned_active tells).
 // With `collect`, a method-4 solve stores one training pair per iteration:

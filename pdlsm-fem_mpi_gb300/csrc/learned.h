@@ -86,7 +86,7 @@ struct Learned : CoarseCorrection {
   int trunc = 1;              // directions kept for A-orthogonalisation in the learned solve
   int stall_window = 60;      // the learned correction is dropped if the residual has not
                               // fallen 10x within this many iterations
-  // plain block-Jacobi FCG as the judge: mean iterations and seconds of the
+  // plain block-Jacobi FCG as the arbiter: mean iterations and seconds of the
   // method-4 Newmark solves, learned solves in a row that lost to them, and
   // whether the learned correction is switched off (until it is retrained)
   double plain_its = 0.0, plain_sec = 0.0;   // plain_sec: only solves that collected nothing

@@ -104,7 +104,7 @@ def test_learned_preconditioner_gains_over_plain_fcg(built):
 
 @pytest.mark.gpu
 def test_plain_solver_judges_and_replaces_a_bad_network(built):
-    """Plain block-Jacobi flexible CG is the judge: with a network that only
+    """Plain block-Jacobi flexible CG is the arbiter: with a network that only
     adds noise the learned solves are cut at the plain iteration count, and
     after two losses method 5 runs the plain method itself."""
     cmd = small_newmark_case()
