@@ -608,7 +608,7 @@ pdx_status pdx_batch_create(const char* const* cmd_paths, int n, const pdx_optio
           if (!cmd_paths[i]) { errs[i] = {4, "null command path"}; continue; }
           pdx_model* q = new pdx_model();
           if (!read_command(cmd_paths[i], q->cmd, q->mesh, q->base_dir, errs[i]) ||
-              !build_setup(q->mesh, q->cmd, q->setup, errs[i]) || !prepare_model(q, errs[i])) {
+              !build_setup(q->mesh, q->cmd, q->setup, errs[i], -1, false) || !prepare_model(q, errs[i])) {
             delete q;
             continue;
           }

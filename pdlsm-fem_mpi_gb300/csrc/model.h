@@ -119,7 +119,8 @@ bool read_mesh(const std::string& path, Mesh& mesh, Error& err);
 // setup (pdsolve::setDatModel restated)
 // device >= 0: the family member search and the CSR pattern run on that GPU
 // (identical results)
-bool build_setup(const Mesh& mesh, const Command& cmd, Setup& s, Error& err, int device = -1);
+// pattern = false skips the CSR pattern (and prepare_model its scatter map)
+bool build_setup(const Mesh& mesh, const Command& cmd, Setup& s, Error& err, int device = -1, bool pattern = true);
 // family members and offsets of s.fam_node on the GPU, in the host loop's
 // order; err.code 7 on a CUDA failure (k_setup.cu)
 bool gpu_family_search(const Mesh& m, Setup& s, const std::vector<double>& delta_node, double md, int device,

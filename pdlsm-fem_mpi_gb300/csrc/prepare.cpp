@@ -433,7 +433,8 @@ bool prepare_model(pdx_model* m, Error& err) {
     }
   }
   // scatter map: offset of every neighbour's first column inside a node's rows
-  {
+  // (none without a CSR pattern: batch specimens)
+  if (!s.csr_ia.empty()) {
     std::vector<std::vector<int>> inter(N);
     for (int f = 0; f < nf; f++)
       inter[s.fam_node[f]].assign(s.fam_members.begin() + s.fam_off[f], s.fam_members.begin() + s.fam_off[f + 1]);

@@ -141,7 +141,7 @@ bool update_pde_by_crack(Ctx& cx, const std::array<double, 9>& cr, Error& err) {
 
 }  // namespace
 
-bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int device) {
+bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int device, bool pattern) {
   const int D = m.dim, N = m.n_node, E = m.n_elem;
   s = Setup();
   s.dim = D;
@@ -367,6 +367,7 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int de
           }
         }
   }
+  if (!pattern) return true;   // batch specimens: no CSR pattern (not merged)
   if (device >= 0) return gpu_csr_pattern(m, s, device, err);   // k_setup.cu
   build_csr_pattern(m, s);
   return true;
