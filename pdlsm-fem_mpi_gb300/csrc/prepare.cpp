@@ -81,10 +81,14 @@ void build_stencils(const Mesh& me, Prepared& p) {
   p.n_st_cls = 0;
   std::unordered_map<std::vector<int64_t>, int, VecHash> classes;
   struct Ent { std::array<int64_t, 3> c; int fe, al; };
+  // per-node work space, reused (the loop runs once per FE-only node)
+  std::vector<Ent> ent;
+  std::vector<std::pair<std::array<int64_t, 3>, int>> nb;
+  std::vector<int64_t> key;
   for (int it = 0; it < nfo; it++) {
     const int k = p.feonly[it];
     const double* xk = &me.X[(size_t)k * 3];
-    std::vector<Ent> ent;
+    ent.clear();
     double Le = 0;
     for (int j = p.fe_adj_ptr[k]; j < p.fe_adj_ptr[k + 1]; j++) {
       const int i = p.fe_adj[j] >> 3;
@@ -108,7 +112,7 @@ void build_stencils(const Mesh& me, Prepared& p) {
     std::sort(ent.begin(), ent.end(), [](const Ent& x, const Ent& y) {
       return x.c != y.c ? x.c < y.c : x.fe < y.fe;
     });
-    std::vector<std::pair<std::array<int64_t, 3>, int>> nb;
+    nb.clear();
     for (const Ent& e : ent)
       for (int a = 0; a < nen; a++) {
         const int n = p.fe_conn[(size_t)e.fe * 8 + a];
@@ -117,14 +121,18 @@ void build_stencils(const Mesh& me, Prepared& p) {
     std::sort(nb.begin(), nb.end());
     nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
     if ((int)nb.size() > S) continue;
-    std::map<int, int> slot;
-    for (size_t i = 0; i < nb.size(); i++) slot[nb[i].second] = (int)i;
-    std::vector<int64_t> key;
+    // slot of a neighbour node in nb (every node of ent's elements is there)
+    auto slot_of = [&](int n) {
+      int i = 0;
+      while (nb[(size_t)i].second != n) i++;
+      return i;
+    };
+    key.clear();
     key.push_back((int64_t)nb.size());
     for (const Ent& e : ent) {
       key.push_back(p.fe_cls[e.fe]);
       key.push_back(e.al);
-      for (int a = 0; a < nen; a++) key.push_back(slot[p.fe_conn[(size_t)e.fe * 8 + a]]);
+      for (int a = 0; a < nen; a++) key.push_back(slot_of(p.fe_conn[(size_t)e.fe * 8 + a]));
     }
     auto f = classes.find(key);
     int cls;
@@ -135,7 +143,7 @@ void build_stencils(const Mesh& me, Prepared& p) {
       for (const Ent& e : ent) {
         const double* K = &p.ke[(size_t)p.fe_cls[e.fe] * nd * nd];
         for (int a = 0; a < nen; a++) {
-          const int sl = slot[p.fe_conn[(size_t)e.fe * 8 + a]];
+          const int sl = slot_of(p.fe_conn[(size_t)e.fe * 8 + a]);
           for (int r = 0; r < D; r++)
             for (int c = 0; c < D; c++) blk[(size_t)sl * D * D + r * D + c] += K[(e.al * D + r) * nd + a * D + c];
         }
