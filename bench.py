@@ -77,12 +77,29 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        if not self.rows:
+            # the timed region ended before nvidia-smi's first row: nothing is known
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
         mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+def hold_clocks(index: int, advance, min_s: float = 1.0):
+    """Clocks under the same step loop, run untimed right after the timed
+    region for at least min_s seconds; used when the timed region was too short
+    for nvidia-smi to sample it."""
+    c = ClockSampler(index)
+    c.start()
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < min_s:
+        advance()
+    out = c.stop()
+    out["when"] = f"untimed hold of the same step loop for {time.perf_counter() - t0:.1f} s after the timed region"
+    return out
 
 
 def profile_traffic():
@@ -405,6 +422,8 @@ def main():
     clocks.start()
     ms = model.explicit_advance_timed(args.steps)
     clk = clocks.stop()
+    if clk.get("samples", 0) < 3:
+        clk["hold"] = hold_clocks(local, lambda: model.explicit_advance(200))
     t_s = ms * 1e-3
     if dist:
         import torch

@@ -144,16 +144,20 @@ pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi
  * pdfemAssembleKNFR_CSRformat :6327-6397).  mode 1 static: F = f_ext - K_pp u_p;
  * mode 2 quasi-static: F = f_ext - K u_all; mode 3 Newmark: a = beta dt^2 K + M,
  * F = f_ext - K v.  v_all: N*d DOF values (NULL = model state).  Outputs: ia
- * (n_eq+1), ja (nnz), a (nnz), f (n_eq); any may be NULL. */
-pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t* ia, int64_t* ja,
+ * (n_eq+1), ja (nnz), a (nnz), f (n_eq); any may be NULL.  ia and ja are
+ * `long long`, the type of pdsolve::cip_ia / cip_ja (HeaderFiles/Solver/
+ * pdsolve.h:254-255), so the reference's own arrays are passed without casts. */
+pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, long long* ia, long long* ja,
                             double* a, double* f);
 
 /* Sparse solve replacing calMatrixOperations::cluster_PARDISO_64Solver
- * (calMatrixOperations.cpp:378-498): zero-based CSR, real unsymmetric, one
- * right-hand side, caller-owned host arrays.  The reference factorises with
- * MKL PARDISO; this is a Krylov solve on the GPU judged by the true FP64
- * residual. */
-pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const double* a,
+ * (calMatrixOperations.h:47-48, calMatrixOperations.cpp:378-498): zero-based
+ * CSR, real unsymmetric, one right-hand side, caller-owned host arrays.  The
+ * first six arguments take the reference's own (long long& n, long long* ia,
+ * long long* ja, double* a, double* rhs, double* x) without casts.  The
+ * reference factorises with MKL PARDISO; this is a Krylov solve on the GPU
+ * judged by the true FP64 residual. */
+pdx_status pdx_solve_csr(long long n, const long long* ia, const long long* ja, const double* a,
                          const double* rhs, double* x, const pdx_solve_opts* opts, pdx_solve_info* info);
 
 /* Allocation-free Jacobi PCG (no counterpart in the reference).  The same

@@ -1065,7 +1065,11 @@ pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi
   return PDX_OK;
 }
 
-pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t* ia, int64_t* ja, double* a,
+// The CSR index arrays of the seams are the reference's `long long` (64-bit
+// here, like the int64_t arrays the library keeps).
+static_assert(sizeof(long long) == sizeof(int64_t), "CSR indices are 64-bit");
+
+pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, long long* ia, long long* ja, double* a,
                             double* f) {
   NEED_DEVICE(m);
   if (mode < 1 || mode > 3) return set_error(PDX_ERR_INVALID, "mode must be 1, 2 or 3");
@@ -1089,7 +1093,7 @@ pdx_status pdx_assemble_csr(pdx_model* m, int mode, const double* v_all, int64_t
   return cuda_check(cudaStreamSynchronize(m->stream), "assembly");
 }
 
-pdx_status pdx_solve_csr(int64_t n, const int64_t* ia, const int64_t* ja, const double* a, const double* rhs,
+pdx_status pdx_solve_csr(long long n, const long long* ia, const long long* ja, const double* a, const double* rhs,
                          double* x, const pdx_solve_opts* opts, pdx_solve_info* info) {
   if (n <= 0 || !ia || !ja || !a || !rhs || !x) return set_error(PDX_ERR_INVALID, "bad argument");
   pdx_solve_opts o{2, 1e-8, 20000, 0};

@@ -13,6 +13,19 @@ for p in (PKG, os.path.join(REPO, "oracle"), REPO):
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
 
+def reference_tree():
+    """The reference checkout: PDX_REFERENCE, else the one __graft_entry__.build()
+    recorded when it built the oracle's reference build; None when neither exists
+    (the GPU machine has no copy)."""
+    ref = os.environ.get("PDX_REFERENCE")
+    rec = os.path.join(REPO, "oracle", "_ref", "reference_path.txt")
+    if not ref and os.path.exists(rec):
+        ref = open(rec).read().strip()
+    if ref and os.path.isdir(os.path.join(ref, "HeaderFiles", "Solver")):
+        return ref
+    return None
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
 

@@ -7,7 +7,8 @@ full-precision (FP64) dumps into ``<case>_<mode>.npz`` next to this script.
 The case inputs (.lis/.in) are copied here too, so the tests can rebuild the
 same models without the reference.
 
-Needs the reference tree (default /root/reference) and SciPy; it is run by
+Needs the reference tree (PDX_REFERENCE, or the checkout that
+__graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
 """
 from __future__ import annotations
@@ -25,7 +26,19 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "pdlsm-fem_mpi_gb300"))
 import meshgen  # noqa: E402
 
-REF = os.environ.get("PDX_REFERENCE", "/root/reference")
+
+def _reference_tree() -> str:
+    """PDX_REFERENCE, else the checkout __graft_entry__.build() recorded."""
+    ref = os.environ.get("PDX_REFERENCE")
+    rec = os.path.join(REPO, "oracle", "_ref", "reference_path.txt")
+    if not ref and os.path.exists(rec):
+        ref = open(rec).read().strip()
+    if not ref or not os.path.isdir(os.path.join(ref, "SourceFiles")):
+        sys.exit("make_golden.py needs the reference tree: set PDX_REFERENCE or run __graft_entry__.build() first")
+    return ref
+
+
+REF = _reference_tree()
 DRIVER = os.path.join(REPO, "oracle", "_ref", "ref_driver")
 
 

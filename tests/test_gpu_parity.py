@@ -100,7 +100,6 @@ def test_mixed_precision_error_is_stated(built, case, cmd):
 
 @pytest.mark.parametrize("case,cmd", CASES)
 def test_stress_and_damage_match_oracle(built, case, cmd):
-    rng = np.random.default_rng(3)
     host = pdx.Model(case_cmd(case, cmd), device=-1)
     o = orc.Oracle(host)
     u, bs, _, _ = o.explicit(nsteps=15)
@@ -112,7 +111,7 @@ def test_stress_and_damage_match_oracle(built, case, cmd):
     np.testing.assert_array_equal(bsg, bs)
     assert rel(ug, u) < FP64_TOL
     assert rel(phg, phi_o) < 1e-14
-    assert rng is not None
+    assert rel(sg, sig_o) < FP64_TOL
 
 
 @pytest.mark.parametrize("case,cmd,mode", [("p21", "p21s", 1), ("b13", "b13s", 1), ("p21", "p21_quasi", 2)])
@@ -163,8 +162,13 @@ def test_krylov_solves_reference_system(built, method):
     print(f"\nmethod {method}: {info.iterations} iterations, reported {info.rel_residual:.2e}, true {true_res:.2e}")
     if info.converged:
         assert true_res <= 1.01e-12
-        eq_u = golden("b13_static")["u"]
-        assert true_res < 1e-11 and eq_u is not None
+        # the reference's direct solve, in equation order; the system's 2-norm
+        # condition number is 6.4e3, so a 1e-12 residual bounds the relative
+        # error by 6.4e-9
+        eq = pdx.Model(case_cmd("b13", "b13s"), device=-1).array("eq").reshape(-1)
+        u_ref = np.zeros_like(x)
+        u_ref[eq[eq >= 0]] = gs["u"].reshape(-1)[eq >= 0]
+        assert rel(x, u_ref) < 1e-8
     else:
         # plain CG on the unsymmetric stiffness may stall; the drivers fall back to BiCGStab
         assert method in (0, 1, 3)

@@ -60,9 +60,8 @@ def test_noalloc_pcg_matches_pcg_twice(built):
 
 
 def test_noalloc_rejects_oversize_before_any_launch(built):
-    torch = pytest.importorskip("torch")
-    if torch.cuda.is_available():
-        pytest.skip("size check is exercised without a device only")
+    """The size check returns before any CUDA call, so the dummy device
+    pointers are never touched; runs with and without a device."""
     big = 262144 + 1
     with pytest.raises(pdx.PdxError) as e:
         pdx.pcg_solve_noalloc(big, 10, 256, 256, 256, 256, 256)
