@@ -10,6 +10,7 @@ same models without the reference.
 Needs the reference tree (PDX_REFERENCE, or the checkout that
 __graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
+[--size-only]
 """
 from __future__ import annotations
 
@@ -244,7 +245,71 @@ def ascii_cases() -> None:
     shutil.rmtree(work)
 
 
+SETUP_ARRAYS = ("eq", "fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja")
+
+
+def setup_digests(d: dict) -> dict:
+    """SHA-256 of the reference's set-up arrays in a canonical form (little-endian
+    int64, family members 0-based), with their lengths."""
+    import hashlib
+    out = {}
+    for name in SETUP_ARRAYS:
+        a = np.asarray(d[name], dtype=np.int64).reshape(-1)
+        if name == "fam_members":
+            a = a - 1
+        out[name + "_sha256"] = np.array(hashlib.sha256(a.astype("<i8").tobytes()).hexdigest())
+        out[name + "_len"] = np.array(a.size)
+    return out
+
+
+def input_digest(case_dir: str, name: str) -> np.ndarray:
+    import hashlib
+    h = hashlib.sha256()
+    for ext in (".in", ".lis"):
+        h.update(open(os.path.join(case_dir, name + ext), "rb").read())
+    return np.array(h.hexdigest())
+
+
+def size_cases() -> None:
+    """The benchmark configurations at their own sizes.  C1 (101x101 plate,
+    FP64, FC 3 s0 = 1e-3): the reference's explicit loop over all 1,000 steps,
+    u every 250 steps, final damage and broken bonds, and its set-up as
+    digests.  C2 (121x61x21 box with hole): the reference's set-up as digests
+    (its per-bond +-5 % critical stretch is not in the reference, so its
+    trajectory is pinned against the C restatement instead).  Inputs come from
+    meshgen.config_c1 / config_c2; their digests are stored so a changed
+    generator shows up as a failed input check, not as a parity failure."""
+    work = tempfile.mkdtemp(prefix="golden_size_")
+    d1 = os.path.join(work, "c1")
+    mesh, kw = meshgen.config_c1()
+    meshgen.write_case(mesh, d1, "c1", **kw)
+    st = run(d1, "c1.in", "setup")
+    c1 = setup_digests(st)
+    c1["input_sha256"] = input_digest(d1, "c1")
+    ex = run(d1, "c1.in", "explicit", "1e-3", "250")
+    keep = [i for i, s in enumerate(ex["u_traj_steps"]) if s > 0]
+    c1["u_steps"] = ex["u_traj_steps"][keep]
+    c1["u"] = ex["u_traj"][keep]
+    bsf = np.asarray(ex["bond_state_final"]).reshape(-1)
+    c1["broken_final"] = np.flatnonzero(bsf == 0).astype(np.int32)
+    c1["n_member"] = np.array(bsf.size)
+    c1["phi_final"] = ex["phi_final"]
+    c1["sigma_final"] = ex["sigma_final"]
+    save("c1_size", c1)
+    d2 = os.path.join(work, "c2")
+    mesh, kw = meshgen.config_c2(nsteps=5000)
+    meshgen.write_case(mesh, d2, "c2", **kw)
+    c2 = setup_digests(run(d2, "c2.in", "setup"))
+    c2["input_sha256"] = input_digest(d2, "c2")
+    save("c2_setup", c2)
+    shutil.rmtree(work)
+
+
 if __name__ == "__main__":
+    if "--size-only" in sys.argv:
+        build_driver()
+        size_cases()
+        sys.exit(0)
     if "--fc2-only" in sys.argv or "--rf-only" in sys.argv or "--ascii-only" in sys.argv:
         build_driver()
         if "--fc2-only" in sys.argv:

@@ -1,0 +1,242 @@
+"""Parity at the benchmark configurations' own sizes.
+
+- C1 (101x101 plate, FP64, FC 3 s0 = 1e-3): the reference's own explicit loop
+  over all 1,000 steps (tests/golden/c1_size.npz, written by
+  tests/golden/make_golden.py --size-only) against the FP64 GPU path: u every
+  250 steps, final stress and damage to 1e-10, identical broken bonds.
+- C1 and C2 set-up: DOF numbers, family offsets and members, pre-crack bond
+  states and the CSR pattern equal the reference's set-up dump, compared by
+  SHA-256 digests (host set-up on the CPU, device set-up on the GPU).
+- C2 (121x61x21 box with hole, s0 = 2e-3 +-5 % per bond): the FP64 GPU path
+  against the C restatement over 50 steps; the mixed path against the FP64
+  GPU run over all 5,000 steps, error and bond-set difference stated.
+- C3 (401x401 plate, quasi-static): all 50 increments through pdx_quasi_step;
+  the loaded increment solved to 1e-12 closes its gap to a direct solve.
+- C4 (256 plates of the seeded draw): eight specimens of the full batch run,
+  the smallest and the largest among them, equal their single runs bitwise
+  over 2,000 steps.
+"""
+import hashlib
+import os
+import tempfile
+import time
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel
+
+import meshgen
+import pdx
+
+FP64_TOL = 1e-10
+SETUP_ARRAYS = ("eq", "fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja")
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.asarray(a, dtype=np.int64).reshape(-1).astype("<i8").tobytes()).hexdigest()
+
+
+def write_config(name: str, **kw) -> str:
+    """The configuration's case from the seeded generator, checked against the
+    digest of the inputs the reference ran on."""
+    d = tempfile.mkdtemp(prefix=f"pdx_{name}_")
+    mesh, cmdkw = {"c1": meshgen.config_c1, "c2": meshgen.config_c2, "c3": meshgen.config_c3}[name](**kw)
+    return meshgen.write_case(mesh, d, name, **cmdkw)
+
+
+def input_sha(cmd: str) -> str:
+    h = hashlib.sha256()
+    base = os.path.splitext(cmd)[0]
+    for ext in (".in", ".lis"):
+        h.update(open(base + ext, "rb").read())
+    return h.hexdigest()
+
+
+def check_setup(model, g):
+    for name in SETUP_ARRAYS:
+        a = model.array(name)
+        assert a.size == int(g[name + "_len"]), name
+        assert sha(a) == str(g[name + "_sha256"]), name
+
+
+C1_GOLDEN, C2_GOLDEN = "c1_size", "c2_setup"
+
+
+def c1_cmd():
+    cmd = write_config("c1")
+    assert input_sha(cmd) == str(golden(C1_GOLDEN)["input_sha256"]), "meshgen.config_c1 changed"
+    return cmd
+
+
+def c2_cmd(nsteps=5000, precision="MIXED"):
+    cmd = write_config("c2", nsteps=nsteps, precision=precision)
+    return cmd
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_host_setup_matches_reference_at_size(built, name):
+    g = golden(C1_GOLDEN if name == "c1" else C2_GOLDEN)
+    cmd = c1_cmd() if name == "c1" else c2_cmd()
+    if name == "c2":
+        assert input_sha(cmd) == str(g["input_sha256"]), "meshgen.config_c2 changed"
+    check_setup(pdx.Model(cmd, device=-1), g)
+
+
+def test_oracle_matches_reference_c1_over_1000_steps(built):
+    """The C restatement (the checker of the larger GPU cases) against the
+    reference's own 1,000-step C1 run."""
+    import orc
+    g = golden(C1_GOLDEN)
+    o = orc.Oracle(pdx.Model(c1_cmd(), device=-1))
+    u, bs, _, _ = o.explicit(nsteps=1000)
+    assert rel(u, g["u"][-1]) < 1e-12
+    np.testing.assert_array_equal(np.flatnonzero(bs == 0), g["broken_final"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1", "c2"])
+def test_device_setup_matches_reference_at_size(built, name):
+    g = golden(C1_GOLDEN if name == "c1" else C2_GOLDEN)
+    cmd = c1_cmd() if name == "c1" else c2_cmd()
+    with pdx.Model(cmd, device=0) as m:
+        check_setup(m, g)
+
+
+@pytest.mark.gpu
+def test_c1_fp64_matches_reference_over_1000_steps(built):
+    g = golden(C1_GOLDEN)
+    steps = [int(s) for s in g["u_steps"]]
+    with pdx.Model(c1_cmd(), device=0, precision=0) as m:
+        m.explicit_init()
+        done, errs = 0, []
+        for i, s in enumerate(steps):
+            m.explicit_advance(s + 1 - done)
+            done = s + 1
+            u, sig, phi, bs = m.state()
+            errs.append(rel(u, g["u"][i]))
+    broken = np.flatnonzero(bs == 0)
+    print(f"\nC1 FP64 vs reference: u rel L2 at steps {steps}: {['%.1e' % e for e in errs]}; "
+          f"sigma {rel(sig, g['sigma_final']):.1e}; broken bonds {broken.size} (reference "
+          f"{g['broken_final'].size})")
+    assert bs.size == int(g["n_member"])
+    assert max(errs) < FP64_TOL
+    np.testing.assert_array_equal(broken, g["broken_final"])
+    assert rel(sig, g["sigma_final"]) < FP64_TOL
+    np.testing.assert_allclose(phi, g["phi_final"], rtol=0, atol=1e-14)
+
+
+@pytest.mark.gpu
+def test_c2_fp64_matches_oracle_over_50_steps(built):
+    import orc
+    cmd = c2_cmd(nsteps=50, precision="FP64")
+    host = pdx.Model(cmd, device=-1)
+    o = orc.Oracle(host)
+    t0 = time.perf_counter()
+    u_o, bs_o, _, nb = o.explicit(nsteps=49)
+    t_o = time.perf_counter() - t0
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        m.explicit_init()
+        m.explicit_advance(50)
+        u, _, _, bs = m.state()
+    print(f"\nC2 FP64 vs oracle, 50 steps: u rel L2 {rel(u, u_o):.2e}, broken {int((bs == 0).sum())} "
+          f"(oracle {int((bs_o == 0).sum())}), oracle {t_o:.1f} s")
+    assert rel(u, u_o) < FP64_TOL
+    np.testing.assert_array_equal(bs, bs_o)
+
+
+@pytest.mark.gpu
+def test_c2_mixed_against_fp64_over_5000_steps(built):
+    """The benchmarked configuration: mixed precision (FP32 forces, FP64 state)
+    against the FP64 GPU path over all 5,000 steps."""
+    cmd = c2_cmd(nsteps=5000)
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        m.explicit_init()
+        m.explicit_advance(5000)
+        u64, s64, _, b64 = m.state()
+    with pdx.Model(cmd, device=0, precision=1) as m:
+        m.explicit_init()
+        m.explicit_advance(5000)
+        u32, s32, _, b32 = m.state()
+    err_u, err_s = rel(u32, u64), rel(s32, s64)
+    nbroken = int((b64 == 0).sum())
+    ndiff = int((b32 != b64).sum())
+    print(f"\nC2 mixed vs FP64 after 5000 steps: u rel L2 {err_u:.2e}, sigma rel L2 {err_s:.2e}, "
+          f"{ndiff} bond-state differences of {nbroken} broken bonds")
+    assert nbroken > 0
+    assert err_u < 1e-5
+    assert ndiff <= max(2, nbroken // 100)
+
+
+@pytest.mark.gpu
+def test_c3_fifty_increments_and_direct_solve(built):
+    """All 50 quasi-static increments (reassembly of K and f_ext - K u each
+    time, FC 3 failure pass after each solve); then the loaded increment's
+    system solved to 1e-8 and to 1e-12 against SciPy's direct solve: the gap
+    shrinks with the residual, so it is the conditioning of the plate and not
+    an error of the solve."""
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    import scipy.sparse as sp
+    cmd = write_config("c3")
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        free = m.array("eq").reshape(-1) >= 0
+        m_bs0 = m.array("bond_state0")
+        m.quasi_init()
+        m.quasi_step(2)
+        u1 = m.state()[0].reshape(-1).copy()
+        ia, ja, a, f = m.assemble(2, u1)
+        t0 = time.perf_counter()
+        its = []
+        for k in range(49):
+            info = m.quasi_step(2)
+            assert info.converged and info.rel_residual <= 1e-8
+            its.append(info.iterations)
+            if k == 0:
+                u2 = m.state()[0].reshape(-1).copy()
+        t_run = time.perf_counter() - t0
+        u, _, _, bs = m.state()
+    n = len(ia) - 1
+    x8, i8 = pdx.solve_csr(ia, ja, a, f, method=2, rtol=1e-8, max_iter=40000)
+    x12, i12 = pdx.solve_csr(ia, ja, a, f, method=2, rtol=1e-12, max_iter=40000)
+    K = sp.csr_matrix((a, ja, ia), shape=(n, n)).tocsc()
+    xd = spla.spsolve(K, f)
+    g8, g12 = rel(x8, xd), rel(x12, xd)
+    print(f"\nC3: 50 increments in {t_run:.1f} s after the first ({sum(its)} BiCGStab iterations), "
+          f"{int((bs == 0).sum())} broken bonds; loaded increment vs direct solve: "
+          f"{g8:.2e} at 1e-8 ({i8.iterations} its), {g12:.2e} at 1e-12 ({i12.iterations} its)")
+    assert i12.converged and i12.rel_residual <= 1e-12
+    assert g12 < 1e-6 and g12 < g8 / 100
+    # no bond reaches s0 = 1e-3 at this load, and the increments after the
+    # loaded one hold it (the reference's rule with load ratio 1): the state
+    # stays the loaded solution up to the solves' tolerance
+    assert int((bs == 0).sum()) == int((m_bs0 == 0).sum())
+    assert rel(u.reshape(-1)[free], u2[free]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_c4_batch_specimens_equal_single_runs(built):
+    """The seeded 256-plate draw run as one batch for 2,000 steps; eight of its
+    specimens (the smallest, the largest and six spread over the draw) run alone
+    give the same fields and broken bonds bit for bit."""
+    nsteps = 2000
+    d = tempfile.mkdtemp(prefix="pdx_c4_")
+    specs = meshgen.config_c4(n_spec=256, nsteps=nsteps, precision="MIXED")
+    paths = [meshgen.write_case(mm, d, f"c4_{i:03d}", **kw) for i, (mm, kw) in enumerate(specs)]
+    sizes = np.array([mm.n_node for mm, _ in specs])
+    pick = sorted({int(np.argmin(sizes)), int(np.argmax(sizes)), 1, 37, 90, 128, 201, 254})
+    with pdx.Model.batch(paths, device=0, precision=1) as b:
+        b.explicit_init()
+        b.explicit_advance(nsteps)
+        u, _, phi, bs = b.state()
+        no, mo, eo = b.batch_offsets()
+    nbroken = 0
+    for i in pick:
+        with pdx.Model(paths[i], device=0, precision=1) as m:
+            m.explicit_init()
+            m.explicit_advance(nsteps)
+            ui, _, pi, bi = m.state()
+        np.testing.assert_array_equal(u[no[i]:no[i + 1]], ui, err_msg=f"specimen {i}")
+        np.testing.assert_array_equal(bs[mo[i]:mo[i + 1]], bi, err_msg=f"specimen {i}")
+        np.testing.assert_array_equal(phi[no[i]:no[i + 1]], pi, err_msg=f"specimen {i}")
+        nbroken += int((bi == 0).sum())
+    print(f"\nC4: specimens {pick} (nodes {sizes[pick].tolist()}) equal their single runs; {nbroken} broken bonds")
