@@ -863,6 +863,7 @@ static pdx_status explicit_reset(pdx_model* m) {
   m->cur = 0;
   m->steps_done = 0;
   m->rf_rows = 0;
+  m->explicit_run = true;
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit init");
 }
 
@@ -1040,7 +1041,7 @@ pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi
   // (with FC 2 the last pass computed the stresses before its cuts)
   pdx_status st = m->fc2 && m->steps_done > 0 ? PDX_OK : model_stress(m, m->d_u[m->cur], true, false);
   if (st) return st;
-  if (m->steps_done > 0 && m->view.fail3) st = explicit_step_launch(m, 2, m->steps_done);
+  if (m->explicit_run && m->steps_done > 0 && m->view.fail3) st = explicit_step_launch(m, 2, m->steps_done);
   if (st) return st;
   st = model_stress(m, m->d_u[m->cur], false, true);
   if (st) return st;

@@ -281,6 +281,7 @@ pdx_status quasi_advance(pdx_model* m) {
 
 pdx_status run_quasi(pdx_model* m, const std::string& dir) {
   pdx_status st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
+  m->explicit_run = false;
   if (st) return st;
   double* u_all = m->d_u[0];
   m->cur = 0;
@@ -307,6 +308,7 @@ pdx_status run_quasi(pdx_model* m, const std::string& dir) {
 pdx_status run_newmark(pdx_model* m, const std::string& dir) {
   pdx_status st = pdx_explicit_init(m);
   if (st) return st;
+  m->explicit_run = false;
   double* u_all = m->d_u[0];
   m->cur = 0;
   const int ne = m->setup.n_eq;
@@ -387,6 +389,7 @@ extern "C" pdx_status pdx_quasi_init(pdx_model* m) {
   m->cur = 0;
   m->steps_done = 0;
   m->quasi_load = 0;
+  m->explicit_run = false;
   return PDX_OK;
 }
 

@@ -466,6 +466,7 @@ pdx_status pdx_newmark_init(pdx_model* m) {
   m->cur = 0;
   m->steps_done = 0;
   m->rf_rows = 0;
+  m->explicit_run = false;
   m->newmark_ready = true;
   return cuda_check(cudaStreamSynchronize(m->stream), "Newmark init");
 }

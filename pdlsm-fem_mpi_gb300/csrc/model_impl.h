@@ -176,6 +176,10 @@ struct pdx_model {
   pdx::Learned* learned = nullptr;
   int cur = 0;                       // index of the buffer holding u_n
   int64_t steps_done = 0;
+  // explicit runs apply a step's FC 3 failure pass at the start of the next
+  // step; pdx_get_state applies it when the state is read.  Quasi-static
+  // increments and Newmark steps finish their own passes.
+  bool explicit_run = true;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   int graph_parity = 0;

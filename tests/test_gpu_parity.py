@@ -100,10 +100,15 @@ def test_mixed_precision_error_is_stated(built, case, cmd):
 
 @pytest.mark.parametrize("case,cmd", CASES)
 def test_stress_and_damage_match_oracle(built, case, cmd):
+    """Nodal stress after step 15: the reference computes it before that
+    step's failure pass (pdsolve.cpp:6062 before :6064), i.e. with the bond
+    states left by step 14; damage uses the states after the pass."""
     host = pdx.Model(case_cmd(case, cmd), device=-1)
     o = orc.Oracle(host)
+    _, bs14, _, _ = o.explicit(nsteps=14)
     u, bs, _, _ = o.explicit(nsteps=15)
-    sig_o, phi_o = o.stress(u, bs)
+    sig_o, _ = o.stress(u, bs14)
+    _, phi_o = o.stress(u, bs)
     with pdx.Model(case_cmd(case, cmd), device=0, precision=0) as m:
         m.explicit_init()
         m.explicit_advance(16)
@@ -518,3 +523,24 @@ def test_fc2_quasi_static_load_control_matches_reference(built):
     assert worst < 1e-9
     assert rows.shape == (21, 4)
     assert np.abs(rows[1:, 1:4] - rf[:, 2:5]).max() <= 1e-8 * np.abs(rf[:, 2:5]).max()
+
+
+def test_reading_the_state_between_quasi_increments_changes_nothing(built, tmp_path):
+    """pdx_get_state applies the pending failure pass of an explicit run only:
+    a quasi-static increment finishes its own pass, and its state (with the
+    prescribed values already advanced for the next increment) must not be
+    tested again.  Plate of 41 x 41 nodes, FC 3, three increments."""
+    mesh, kw = meshgen.config_c3(n=41)
+    cmd = meshgen.write_case(mesh, str(tmp_path), "q41", **kw)
+    out = []
+    for read_between in (False, True):
+        with pdx.Model(cmd, device=0, precision=0) as m:
+            m.quasi_init()
+            for _ in range(3):
+                m.quasi_step(2)
+                if read_between:
+                    m.state()
+            out.append(m.state())
+    np.testing.assert_array_equal(out[0][3], out[1][3])
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert int((out[1][3] == 0).sum()) == int((pdx.Model(cmd, device=-1).array("bond_state0") == 0).sum())

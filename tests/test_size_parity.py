@@ -179,8 +179,9 @@ def test_c3_fifty_increments_and_direct_solve(built):
     import scipy.sparse as sp
     cmd = write_config("c3")
     with pdx.Model(cmd, device=0, precision=0) as m:
-        free = m.array("eq").reshape(-1) >= 0
-        m_bs0 = m.array("bond_state0")
+        eq = m.array("eq").reshape(-1)
+        free = eq >= 0
+        n_pre = int((m.array("bond_state0") == 0).sum())
         m.quasi_init()
         m.quasi_step(2)
         u1 = m.state()[0].reshape(-1).copy()
@@ -202,15 +203,23 @@ def test_c3_fifty_increments_and_direct_solve(built):
     xd = spla.spsolve(K, f)
     g8, g12 = rel(x8, xd), rel(x12, xd)
     print(f"\nC3: 50 increments in {t_run:.1f} s after the first ({sum(its)} BiCGStab iterations), "
-          f"{int((bs == 0).sum())} broken bonds; loaded increment vs direct solve: "
+          f"{int((bs == 0).sum()) - n_pre} bonds cut by the failure passes; loaded increment vs direct solve: "
           f"{g8:.2e} at 1e-8 ({i8.iterations} its), {g12:.2e} at 1e-12 ({i12.iterations} its)")
     assert i12.converged and i12.rel_residual <= 1e-12
     assert g12 < 1e-6 and g12 < g8 / 100
-    # no bond reaches s0 = 1e-3 at this load, and the increments after the
-    # loaded one hold it (the reference's rule with load ratio 1): the state
-    # stays the loaded solution up to the solves' tolerance
-    assert int((bs == 0).sum()) == int((m_bs0 == 0).sum())
-    assert rel(u.reshape(-1)[free], u2[free]) < 1e-6
+    # at this load no bond comes near s0 = 1e-3 (largest stretch 4.2e-5 in a
+    # direct solve of the loaded increment), so the failure passes cut nothing
+    assert int((bs == 0).sum()) == n_pre
+    # the increments after the loaded one hold the load (the reference's rule
+    # with load ratio 1) and only correct the residual left by the solves: the
+    # final state is no further from the direct solution than increment 2's
+    def du_eq(uu):
+        d = np.zeros(n)
+        d[eq[free]] = (uu - u1)[free]
+        return d
+    e2, e50 = rel(du_eq(u2), xd), rel(du_eq(u.reshape(-1)), xd)
+    print(f"    increment 2 vs direct {e2:.2e}, after 50 increments {e50:.2e}")
+    assert e50 <= e2 * 1.01
 
 
 @pytest.mark.gpu
