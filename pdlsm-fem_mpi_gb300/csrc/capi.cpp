@@ -139,6 +139,7 @@ static pdx_status upload_model(pdx_model* m) {
   v.fam_s0 = upload(m, p.fam_s0);
   v.fam_s0f = upload(m, to_f32(p.fam_s0));
   v.dt2m = upload(m, p.dt2m);
+  v.dt2m_f = upload(m, to_f32(p.dt2m));
   v.fail3 = m->cmd.fail_flag == 3 ? 1 : 0;
   if (m->batch.empty()) {
     m->d_D = upload(m, p.D);

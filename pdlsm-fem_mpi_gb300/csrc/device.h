@@ -70,6 +70,7 @@ struct DevView {
   const double* fam_s0;     // critical stretch of each family (before the per-bond draw)
   const float* fam_s0f;
   const double* dt2m;       // dt^2 / lumped mass per node (0 without active DOFs)
+  const float* dt2m_f;      // the same in FP32 (mixed-precision update)
 };
 
 struct StepArgs {

@@ -62,6 +62,36 @@ __device__ __forceinline__ bool stretch_over_fp64(const DevView& v, const double
   return s > sc;
 }
 
+// Conversions between float and double on the integer pipe.  GB300 issues
+// FP64 arithmetic and FP64 conversions at 2 lanes per clock per SM (FP32
+// FMA: 128; both measured on the GB300), so the mixed kernels keep them off
+// the per-DOF update: only the FP64 accumulation
+// u_{n+1} = (2 u_n - u_{n-1}) + dt^2 F / m runs on the FP64 pipe.  Both
+// conversions give the bits of cvt.f64.f32 / cvt.rn.f32.f64; the rare inputs
+// outside the plain normal range (float subnormals, infinities, NaN) take
+// the hardware conversion.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t em = b & 0x7fffffffu;
+  if (em == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+  if (em < 0x00800000u || em >= 0x7f800000u) return (double)f;
+  // exponent bias 127 -> 1023 (+896 << 20 in the high word); 23 -> 52 mantissa bits
+  const uint32_t hi = (b & 0x80000000u) | ((em >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(em << 29));
+}
+
+__device__ __forceinline__ float d2f_bits(double d) {
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  const uint32_t sgn = hi & 0x80000000u;
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e == 0u && (hi & 0xfffffu) == 0u && lo == 0u) return __uint_as_float(sgn);
+  if (e <= 896u || e >= 1151u) return (float)d;
+  uint32_t r = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t rest = lo & 0x1fffffffu;   // the 29 bits rounded away
+  if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;   // nearest, ties to even
+  return __uint_as_float(sgn | r);
+}
+
 template <int D, int L, typename T>
 __device__ __forceinline__ void warp_sum(T* acc) {
 #pragma unroll
@@ -143,11 +173,12 @@ struct UpdateOperands {
   int n[ROUNDS];                              // node of this lane's (item, DOF) pair, -1 none
   unsigned flag[ROUNDS];                      // bcflag: bit i varying prescribed, bit 4 + i prescribed
   double un[ROUNDS], prev[ROUNDS], dt2m[ROUNDS];
+  float dt2mf[ROUNDS];                        // mixed kernels: dt^2 / m in FP32
 };
 
 // Loads what the update of this lane's (item, DOF) pairs needs; it depends
 // only on the items' nodes, so it can be issued before the force is known.
-template <int D, int L>
+template <int D, int L, bool MIXED = false>
 __device__ __forceinline__ void update_prefetch(const StepArgs& a, int node_or_neg, UpdateOperands<D, L>& o) {
   using O = UpdateOperands<D, L>;
   const DevView& v = a.v;
@@ -161,11 +192,13 @@ __device__ __forceinline__ void update_prefetch(const StepArgs& a, int node_or_n
     o.n[r] = act ? n : -1;
     o.flag[r] = 0;
     o.un[r] = o.prev[r] = o.dt2m[r] = 0.0;
+    o.dt2mf[r] = 0.f;
     if (o.n[r] >= 0) {
       const int64_t idx = (int64_t)n * D + i;
       o.un[r] = a.u_n[idx];
       o.prev[r] = a.u_next[idx];
-      o.dt2m[r] = v.dt2m[n];
+      if (MIXED) o.dt2mf[r] = v.dt2m_f[n];
+      else o.dt2m[r] = v.dt2m[n];
       o.flag[r] = v.bcflag[n];
     }
   }
@@ -173,8 +206,11 @@ __device__ __forceinline__ void update_prefetch(const StepArgs& a, int node_or_n
 
 // Central-difference update of the active DOFs and the next value of the
 // varying prescribed ones; the mixed kernel also writes the node record.
-template <int D, int L, bool MIXED>
-__device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOperands<D, L>& o, const double* F) {
+// F: FP64 forces (FP64 kernels) or FP32 forces (mixed kernels).  The mixed
+// update forms dt^2 F / m in FP32 (the force is FP32 already) and accumulates
+// it into the FP64 state as (2 u_n - u_{n-1}) + dt^2 F / m.
+template <int D, int L, bool MIXED, typename FT>
+__device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOperands<D, L>& o, const FT* F) {
   using O = UpdateOperands<D, L>;
   const int t = threadIdx.x & 31;
   const int jr = t / D, i = t % D;
@@ -182,10 +218,10 @@ __device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOper
   for (int r = 0; r < O::ROUNDS; r++) {
     const int j = r * O::IPR + jr;
     const int src = (jr < O::IPR && j < O::IPW ? j : 0) * L;
-    double Fi = 0.0;
+    FT Fi = FT(0);
 #pragma unroll
     for (int c = 0; c < D; c++) {
-      const double x = __shfl_sync(kFull, F[c], src);
+      const FT x = __shfl_sync(kFull, F[c], src);
       if (c == i) Fi = x;
     }
     const int n = o.n[r];
@@ -193,13 +229,18 @@ __device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOper
     if (n >= 0) {
       double unew;
       if (!((o.flag[r] >> (4 + i)) & 1u)) {
-        const double tempA = Fi * o.dt2m[r];
-        unew = a.mode == 0 ? o.un[r] + 0.5 * tempA : fma(2.0, o.un[r], tempA) - o.prev[r];
+        if constexpr (MIXED) {
+          const float tA = (float)Fi * o.dt2mf[r];
+          unew = a.mode == 0 ? o.un[r] + f2d_bits(0.5f * tA) : fma(2.0, o.un[r], -o.prev[r]) + f2d_bits(tA);
+        } else {
+          const double tempA = (double)Fi * o.dt2m[r];
+          unew = a.mode == 0 ? o.un[r] + 0.5 * tempA : fma(2.0, o.un[r], tempA) - o.prev[r];
+        }
       } else {
         unew = (o.flag[r] >> i) & 1u ? o.un[r] + a.v.dtv[3 * n + i] : o.un[r];
       }
       a.u_next[(int64_t)n * D + i] = unew;
-      uf = (float)unew;
+      uf = MIXED ? d2f_bits(unew) : (float)unew;
     }
     if (MIXED) {
       const float c1 = __shfl_down_sync(kFull, uf, 1);
@@ -210,21 +251,21 @@ __device__ __forceinline__ void update_apply(const StepArgs& a, const UpdateOper
   }
 }
 
-template <int D, int L, bool MIXED>
-__device__ __forceinline__ void warp_update(const StepArgs& a, const double* F, int node_or_neg) {
+template <int D, int L, bool MIXED, typename FT>
+__device__ __forceinline__ void warp_update(const StepArgs& a, const FT* F, int node_or_neg) {
   UpdateOperands<D, L> o;
-  update_prefetch<D, L>(a, node_or_neg, o);
+  update_prefetch<D, L, MIXED>(a, node_or_neg, o);
   update_apply<D, L, MIXED>(a, o, F);
 }
 
-template <int D>
-__device__ __forceinline__ void external_force(const StepArgs& a, int node, double* fext) {
+template <int D, typename FT>
+__device__ __forceinline__ void external_force(const StepArgs& a, int node, FT* fext) {
   const DevView& v = a.v;
   if (v.ext_ptr && a.nbc_val) {
     for (int j = v.ext_ptr[node]; j < v.ext_ptr[node + 1]; j++) {
       const double t = a.nbc_val[v.ext_nbc[j]];
 #pragma unroll
-      for (int i = 0; i < D; i++) fext[i] += t * v.ext_f[3 * j + i];
+      for (int i = 0; i < D; i++) fext[i] += (FT)(t * v.ext_f[3 * j + i]);
     }
   }
 }
@@ -296,7 +337,7 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
   const int cls = valid && v.st_cls ? v.st_cls[item] : -1;
   const int dcls = valid && v.st_delta ? v.st_dcls[item] : 0;
   UpdateOperands<D, L> o;
-  update_prefetch<D, L>(a, valid ? node : -1, o);
+  update_prefetch<D, L, MIXED>(a, valid ? node : -1, o);
   T acc[D];
 #pragma unroll
   for (int i = 0; i < D; i++) acc[i] = T(0);
@@ -312,9 +353,10 @@ __device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int6
     }
   }
   warp_sum<D, L>(acc);
-  double F[D];
+  using FT = typename std::conditional<MIXED, float, double>::type;
+  FT F[D];
 #pragma unroll
-  for (int i = 0; i < D; i++) F[i] = (double)acc[i];
+  for (int i = 0; i < D; i++) F[i] = (FT)acc[i];
   if (lane == 0 && valid) external_force<D>(a, node, F);
   update_apply<D, L, MIXED>(a, o, F);
 }

@@ -249,11 +249,8 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
   for (int o = L / 2; o > 0; o >>= 1) nbroken += __shfl_xor_sync(kFull, nbroken, o);
   if (lane == 0 && valid && nbroken) v.fam_intact[f] -= nbroken;
   if (a.mode == 2) return;
-  double F[D];
-#pragma unroll
-  for (int i = 0; i < D; i++) F[i] = (double)acc[i];
-  if (lane == 0 && valid) external_force<D>(a, node, F);
-  warp_update<D, L, true>(a, F, valid ? node : -1);
+  if (lane == 0 && valid) external_force<D>(a, node, acc);
+  warp_update<D, L, true>(a, acc, valid ? node : -1);
 }
 
 // Blocks per SM: 4 in 3D (64 registers: the two-stage family pipeline holds
