@@ -89,7 +89,13 @@ pdx_status pdx_model_get_info(const pdx_model* m, pdx_model_info* info);
  * "fam_cdv" (f64), "bond_state0" (uint8, member layout), "pdbe" (int32, n*4),
  * "pde_idx", "fe_idx" (int32), "csr_ia", "csr_ja" (int64), "mass" (f64, lumped
  * per equation), "u0" (f64, N*d initial DOF values), "geom" (f64: min delta,
- * max delta, block size, lbc[3], rtc[3]). */
+ * max delta, block size, lbc[3], rtc[3]); the mixed step kernel's lattice
+ * tiles of 2D FE-only nodes: "tile_rows" (int32, per tile and staged row:
+ * first node id, presence bits), "tile_cls" (int16, per tile site: stencil
+ * class | 1 << 14 when the PD part reads the node's FP32 record, -1 none),
+ * "lat_blk" (f32, per class 9 blocks of 2 x 2 by lattice offset
+ * (dx + 1) + 3 (dy + 1)), "fe_rest" (int32: the FE-only items, in "feonly"
+ * order, that no tile covers). */
 pdx_status pdx_model_array_len(const pdx_model* m, const char* name, int64_t* count);
 pdx_status pdx_model_array(const pdx_model* m, const char* name, void* dst, int64_t count);
 

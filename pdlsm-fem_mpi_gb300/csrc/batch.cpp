@@ -79,6 +79,7 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
   int64_t node_off = 0, elem_off = 0, fam_off = 0, bond_off = 0, eq_off = 0, member_off = 0, fe_off = 0;
   int64_t cls_off = 0, st_off = 0, corr_off = 0, wd_off = 0, adj_off = 0, dcls_off = 0;
   bool all_delta = true;
+  int64_t feonly_off = 0;
   const int NV = D == 2 ? 3 : 6;
   for (size_t i = 0; i < parts.size(); i++) {
     const pdx_model* q = parts[i];
@@ -177,6 +178,23 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
       P.st_dcls.insert(P.st_dcls.end(), p.feonly.size(), -1);
       if (p.n_st_cls > 0) all_delta = false;
     }
+    // lattice tiles: node ids and classes shifted; a specimen without tiles
+    // lists its FE-only items for the per-node path
+    if (p.n_tiles > 0) {
+      const size_t r0 = P.tile_rows.size();
+      P.tile_rows.insert(P.tile_rows.end(), p.tile_rows.begin(), p.tile_rows.end());
+      for (size_t r = r0; r < P.tile_rows.size(); r += 2)
+        if (P.tile_rows[r + 1] != 0) P.tile_rows[r] += (int)node_off;
+      for (int16_t c : p.tile_cls)
+        P.tile_cls.push_back(c < 0 ? c : (int16_t)(((c & kTileClsMask) + st_off) | (c & kTileShadowBit)));
+      append(P.lat_blk, p.lat_blk);
+      P.n_tiles += p.n_tiles;
+    } else {
+      for (size_t it = 0; it < p.feonly.size(); it++) P.fe_rest.push_back((int)(feonly_off + (int64_t)it));
+      // keep the class numbering of lat_blk aligned with st_cls
+      P.lat_blk.insert(P.lat_blk.end(), (size_t)p.n_st_cls * Tile2::SLOTS * Tile2::BW, 0.f);
+    }
+    feonly_off += (int64_t)p.feonly.size();
     if (i == 0) { P.D = p.D; P.lambda = p.lambda; P.mu = p.mu; }
     // offsets
     node_off += m.n_node;
@@ -195,6 +213,13 @@ bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& er
       err = {3, "batch too large for 32-bit node, bond or element indices"};
       return false;
     }
+  }
+  if (P.n_tiles == 0 || st_off > kTileClsMask) {
+    P.tile_rows.clear();
+    P.tile_cls.clear();
+    P.lat_blk.clear();
+    P.n_tiles = 0;
+    P.fe_rest.clear();
   }
   P.n_st_dcls = (int)dcls_off;
   P.st_use_delta = P.n_st_cls > 0 && all_delta;

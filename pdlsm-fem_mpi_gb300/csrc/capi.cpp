@@ -124,6 +124,14 @@ static pdx_status upload_model(pdx_model* m) {
       for (int e = 0; e < dd; e++) b32[i * w + e] = (float)p.st_blk[i * dd + e];
     v.st_blk32 = upload(m, b32);
   }
+  v.n_tiles = p.n_tiles;
+  if (p.n_tiles > 0) {
+    v.tile_rows = reinterpret_cast<const int2*>(upload(m, p.tile_rows));
+    v.tile_cls = upload(m, p.tile_cls);
+    v.lat_blk = upload(m, p.lat_blk);
+    v.n_rest = (int)p.fe_rest.size();
+    if (v.n_rest) v.fe_rest = upload(m, p.fe_rest);
+  }
   v.n_nbc = (int)me.nbcs.size();
   if (v.n_nbc) {
     v.ext_ptr = upload(m, p.ext_ptr);
@@ -740,6 +748,10 @@ static bool array_ref(const pdx_model* m, const std::string& n, const void** ptr
   if (n == "st_cls") return set(p.st_cls.data(), p.st_cls.size(), 4);
   if (n == "st_nbr") return set(p.st_nbr.data(), p.st_nbr.size(), 4);
   if (n == "st_blk") return set(p.st_blk.data(), p.st_blk.size(), 8);
+  if (n == "tile_rows") return set(p.tile_rows.data(), p.tile_rows.size(), 4);
+  if (n == "tile_cls") return set(p.tile_cls.data(), p.tile_cls.size(), 2);
+  if (n == "lat_blk") return set(p.lat_blk.data(), p.lat_blk.size(), 4);
+  if (n == "fe_rest") return set(p.fe_rest.data(), p.fe_rest.size(), 4);
   if (n == "bcflag") return set(p.bcflag.data(), p.bcflag.size(), 1);
   if (n == "dtv") return set(p.dtv.data(), p.dtv.size(), 8);
   if (n == "material") {

@@ -14,6 +14,21 @@ constexpr int kMaxFeAdj = 8;      // FE elements around a node (Q4: 4, Hex8: 8)
 constexpr int kStencil2 = 9;      // neighbour slots of an FE-only node's stencil (Q4)
 constexpr int kStencil3 = 27;     // (Hex8)
 
+// Lattice tiles of 2D FE-only nodes (mixed step kernel): one block of 256
+// threads per tile of 16 x 16 lattice sites, one node per thread; the tile's
+// nodes and a one-site halo (18 x 18 sites) are staged in shared memory.
+struct Tile2 {
+  static constexpr int X = 16, Y = 16;
+  static constexpr int WX = X + 2, WY = Y + 2;
+  static constexpr int ROWS = WY;               // staged rows (x runs)
+  static constexpr int SITES = WX * WY;         // staged sites
+  static constexpr int NODES = X * Y;           // tile sites (= threads)
+  static constexpr int SLOTS = 9;               // lattice offsets {-1,0,1}^2
+  static constexpr int BW = 4;                  // floats per 2 x 2 block
+};
+constexpr int kTileShadowBit = 1 << 14;
+constexpr int kTileClsMask = kTileShadowBit - 1;
+
 // Everything a kernel needs, as raw device pointers (passed by value).
 struct DevView {
   int dim, n_node, n_fam, n_feonly, n_eq;
@@ -56,6 +71,13 @@ struct DevView {
   const int* st_delta;      // per delta class: kStencil2|3 offsets neighbour - node, INT32_MIN empty; or null
   const float* st_blk32;    // per class and slot: 3D 12 floats (3x3 row-major + pad), 2D 4 floats
   const double* st_blk64;   // per class and slot: D*D doubles
+  // lattice tiles of 2D FE-only nodes (n_tiles = 0: none)
+  int n_tiles;
+  const int2* tile_rows;    // per tile Tile2::ROWS (first node id, presence bits of the row's WX sites)
+  const int16_t* tile_cls;  // per tile Tile2::NODES: class | kTileShadowBit, -1 no FE-only node
+  const float* lat_blk;     // per class Tile2::SLOTS 2 x 2 blocks by lattice offset (dx + 1) + 3 (dy + 1)
+  const int* fe_rest;       // with tiles: FE-only items outside every tile (per-node path)
+  int n_rest;
   // external force (traction BCs): per node list of (nbc id, unit force)
   const int* ext_ptr;       // n_node+1 or null
   const int* ext_nbc;

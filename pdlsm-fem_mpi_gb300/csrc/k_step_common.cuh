@@ -327,12 +327,16 @@ __device__ __forceinline__ void stencil_rows(const DevView& v, int item, int nod
 // FE-only node item: stencil (or element) rows, then the update, whose
 // operands are requested before the force.  t = thread index within the FE
 // part of the grid.
+// rest: optional list of the FE-only items to take (n_items entries), else
+// items 0 .. n_feonly - 1.
 template <int D, int L, typename T, bool MIXED, typename ULoad>
-__device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int64_t t, const ULoad& uload) {
+__device__ __forceinline__ void feonly_item(const StepArgs& a, const T* ke, int64_t t, const ULoad& uload,
+                                            const int* rest = nullptr, int n_items = -1) {
   const DevView& v = a.v;
-  const int item = (int)(t / L);
+  const int pick = (int)(t / L);
   const int lane = (int)(t % L);
-  const bool valid = item < v.n_feonly;
+  const bool valid = pick < (rest ? n_items : v.n_feonly);
+  const int item = rest ? (valid ? rest[pick] : 0) : pick;
   const int node = valid ? v.feonly_node[item] : 0;
   const int cls = valid && v.st_cls ? v.st_cls[item] : -1;
   const int dcls = valid && v.st_delta ? v.st_dcls[item] : 0;

@@ -253,6 +253,80 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
   warp_update<D, L, true>(a, acc, valid ? node : -1);
 }
 
+// 2D FE-only nodes of one lattice tile, one node per thread.  The tile's
+// sites and a one-site halo are staged in shared memory as FP32
+// displacements (the FP64 state rounded on the integer pipe, plus this
+// step's increment for varying prescribed DOFs), so each staged value is
+// read from HBM once per tile (1.27 times per node) instead of once per
+// stencil neighbour; a site's node is the row's first node id plus the
+// number of present sites before it.  The stencil runs over the 9 lattice
+// offsets with the class's blocks (zero blocks where the class has no
+// neighbour); the node is then updated in FP64 and its FP32 record is
+// written only if the PD part of the step reads it.
+__device__ __forceinline__ void tile_item2(const StepArgs& a, int tile, float2* su) {
+  using T = Tile2;
+  const DevView& v = a.v;
+  const int2* rows = v.tile_rows + (int64_t)tile * T::ROWS;
+  for (int q = threadIdx.x; q < T::SITES; q += blockDim.x) {
+    const int r = q / T::WX, x = q - r * T::WX;
+    const int2 ri = __ldg(rows + r);
+    float2 w = make_float2(0.f, 0.f);
+    if (((unsigned)ri.y >> x) & 1u) {
+      const int n = ri.x + __popc((unsigned)ri.y & ((1u << x) - 1u));
+      const unsigned fl = v.bcflag[n];
+      double2 c = *reinterpret_cast<const double2*>(a.u_n + 2 * (int64_t)n);
+      if (fl & 1u) c.x += v.dtv[3 * n];
+      if (fl & 2u) c.y += v.dtv[3 * n + 1];
+      w = make_float2(d2f_bits(c.x), d2f_bits(c.y));
+    }
+    su[q] = w;
+  }
+  const int x = threadIdx.x % T::X, y = threadIdx.x / T::X;
+  const int ctr = (x + 1) + T::WX * (y + 1);
+  const int cc = v.tile_cls[(int64_t)tile * T::NODES + threadIdx.x];
+  int node = -1;
+  if (cc >= 0) {
+    const int2 ri = __ldg(rows + y + 1);
+    node = ri.x + __popc((unsigned)ri.y & ((1u << (x + 1)) - 1u));
+  }
+  // update operands, requested before the barrier so their loads overlap the staging
+  double2 un = make_double2(0.0, 0.0), prev = make_double2(0.0, 0.0);
+  float dt2m = 0.f;
+  unsigned fl = 0;
+  if (node >= 0) {
+    un = *reinterpret_cast<const double2*>(a.u_n + 2 * (int64_t)node);
+    prev = *reinterpret_cast<const double2*>(a.u_next + 2 * (int64_t)node);
+    dt2m = v.dt2m_f[node];
+    fl = v.bcflag[node];
+  }
+  __syncthreads();
+  if (node < 0) return;
+  float acc[2] = {0.f, 0.f};
+  const float4* B = reinterpret_cast<const float4*>(v.lat_blk) + (int64_t)(cc & kTileClsMask) * T::SLOTS;
+#pragma unroll
+  for (int o = 0; o < T::SLOTS; o++) {
+    const float4 b = __ldg(B + o);
+    const float2 u = su[ctr + (o % 3 - 1) + T::WX * (o / 3 - 1)];
+    acc[0] -= b.x * u.x + b.y * u.y;
+    acc[1] -= b.z * u.x + b.w * u.y;
+  }
+  external_force<2>(a, node, acc);
+  const double uo[2] = {un.x, un.y}, up[2] = {prev.x, prev.y};
+  double unew[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    if (!((fl >> (4 + i)) & 1u)) {
+      const float tA = acc[i] * dt2m;
+      unew[i] = a.mode == 0 ? uo[i] + f2d_bits(0.5f * tA) : fma(2.0, uo[i], -up[i]) + f2d_bits(tA);
+    } else {
+      unew[i] = (fl >> i) & 1u ? uo[i] + v.dtv[3 * node + i] : uo[i];
+    }
+  }
+  *reinterpret_cast<double2*>(a.u_next + 2 * (int64_t)node) = make_double2(unew[0], unew[1]);
+  if (cc & kTileShadowBit)
+    a.uf_next[2 * (int64_t)node + 1] = make_float4(d2f_bits(unew[0]), d2f_bits(unew[1]), 0.f, __uint_as_float(fl));
+}
+
 // Blocks per SM: 4 in 3D (64 registers: the two-stage family pipeline holds
 // two bond records and a node record per lane; C2 47.0 us per step against
 // 48.5 with 5 blocks); 6 in 2D (40 registers, a few spills to L1), which took
@@ -269,6 +343,15 @@ __global__ void __launch_bounds__(256, D == 3 ? 4 : 6) k_step_mixed(StepArgs a) 
   }
   if ((int)blockIdx.x < a.pd_blocks) {
     mixed_family_item<D, LP>(a, ke, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  } else if (D == 2 && a.v.n_tiles > 0) {
+    const int tb = (int)blockIdx.x - a.pd_blocks;
+    if (tb < a.v.n_tiles) {
+      __shared__ float2 s_tile[Tile2::SITES];
+      tile_item2(a, tb, s_tile);
+    } else {
+      const int64_t t = (int64_t)(tb - a.v.n_tiles) * blockDim.x + threadIdx.x;
+      feonly_item<D, LF, float, true>(a, ke, t, LoadMixed<D>{a.uf_n, a.v.dtv}, a.v.fe_rest, a.v.n_rest);
+    }
   } else {
     const int64_t t = (int64_t)(blockIdx.x - a.pd_blocks) * blockDim.x + threadIdx.x;
     feonly_item<D, LF, float, true>(a, ke, t, LoadMixed<D>{a.uf_n, a.v.dtv});
@@ -316,7 +399,9 @@ cudaError_t mixed_dispatch_lf(const StepArgs& a, int lf, int blocks, size_t smem
 template <int D>
 cudaError_t mixed_dispatch(StepArgs a, int lp, int lf, cudaStream_t s) {
   const int pd_blocks = (int)(((int64_t)a.v.n_fam * lp + 255) / 256);
-  const int fe_blocks = a.mode == 2 ? 0 : (int)(((int64_t)a.v.n_feonly * lf + 255) / 256);
+  const int fe_blocks = a.mode == 2 ? 0
+                        : D == 2 && a.v.n_tiles > 0 ? a.v.n_tiles + (int)(((int64_t)a.v.n_rest * lf + 255) / 256)
+                                                    : (int)(((int64_t)a.v.n_feonly * lf + 255) / 256);
   a.pd_blocks = pd_blocks;
   const int blocks = pd_blocks + fe_blocks;
   if (blocks == 0) return cudaSuccess;

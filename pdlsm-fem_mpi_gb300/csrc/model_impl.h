@@ -50,6 +50,16 @@ struct Prepared {
   std::vector<int> st_delta;         // per delta class: slots of (neighbour - node), INT32_MIN empty
   int n_st_dcls = 0;
   bool st_use_delta = false;         // kernels read delta classes instead of st_nbr
+  // 2D FE-only nodes by lattice tile (mixed step kernel; structured meshes
+  // whose lattice rows are numbered consecutively): per tile, the staged
+  // box's rows as (first node id, presence bits) and the stencil class of
+  // each tile site (-1 none; bit 14: the PD part of the step reads the node's
+  // FP32 record); per class the 2 x 2 blocks by lattice offset
+  std::vector<int> tile_rows;
+  std::vector<int16_t> tile_cls;
+  std::vector<float> lat_blk;
+  int n_tiles = 0;
+  std::vector<int> fe_rest;          // with tiles: FE-only items (feonly order) outside every tile
   // traction BCs
   std::vector<int> ext_ptr, ext_nbc;
   std::vector<double> ext_f;

@@ -143,7 +143,8 @@ _ARRAY_DTYPES = {"eq": np.int32, "vol_node": np.float64, "vol_elem": np.float64,
                  "csr_ia": np.int64, "csr_ja": np.int64, "mass": np.float64, "u0": np.float64, "geom": np.float64,
                  "X": np.float64, "conn": np.int32, "elem_nn": np.int32, "bcflag": np.uint8, "dtv": np.float64,
                  "material": np.float64, "feonly": np.int32, "st_cls": np.int32, "st_nbr": np.int32,
-                 "st_blk": np.float64}
+                 "st_blk": np.float64, "tile_rows": np.int32, "tile_cls": np.int16, "lat_blk": np.float32,
+                 "fe_rest": np.int32}
 
 
 class Model:
