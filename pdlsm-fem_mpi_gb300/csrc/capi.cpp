@@ -870,7 +870,7 @@ static pdx_status explicit_reset(pdx_model* m) {
                   m->stream);
   if (m->mixed) {
     pdx_status st = cuda_check(
-        launch_pack_bonds(m->view, (float)m->cmd.s0_pert, m->d_brec, m->stream), "pack bonds");
+        launch_pack_bonds(m->view, (float)m->cmd.s0_pert, m->lanes, m->d_brec, m->stream), "pack bonds");
     if (st) return st;
   }
   m->cur = 0;
@@ -898,6 +898,10 @@ static pdx_status autotune_lanes(pdx_model* m) {
     for (int j = 0; j < nlf && !st; j++) {
       m->lanes = m->tune_lanes ? kLp[i] : lp0;
       m->fe_lanes = m->tune_fe_lanes ? kLf[j] : lf0;
+      // 3D records are laid out for the lane count that reads them
+      if (m->mixed)
+        st = cuda_check(launch_pack_bonds(m->view, (float)m->cmd.s0_pert, m->lanes, m->d_brec, m->stream),
+                        "pack bonds");
       for (int w = 0; w < 2 && !st; w++) st = explicit_step_launch(m, 1, 0);
       if (!st) st = cuda_check(cudaEventRecord(e0, m->stream), "event record");
       for (int w = 0; w < 5 && !st; w++) st = explicit_step_launch(m, 1, 0);

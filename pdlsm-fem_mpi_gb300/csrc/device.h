@@ -179,7 +179,9 @@ bool step_lanes_valid(int lp, int lf);
 cudaError_t launch_step(const StepArgs& a, int mixed, int lp, int lf, cudaStream_t s);
 cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s);
 cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
-cudaError_t launch_pack_bonds(const DevView& v, float pertf, float4* rec, cudaStream_t s);
+// lanes: lanes per PD family of the step kernel that will read the records
+// (3D records name the neighbour of the bond 2 * lanes further on)
+cudaError_t launch_pack_bonds(const DevView& v, float pertf, int lanes, float4* rec, cudaStream_t s);
 cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
 cudaError_t launch_assemble(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_newmark_predict(const DevView& v, const double* u, const double* vel, const double* acc,

@@ -2,11 +2,16 @@
 // FP64.  Same work split, failure order and update as the FP64 kernel
 // (k_step.cu, k_step_common.cuh); the data it streams differ:
 //
-// Bond records (one per bond; 3D: 32 B = 6 FP32 coefficients, the neighbour
-// index whose sign carries the bond state, the bond's FP32 threshold; 2D:
-// 16 B = 3 coefficients + neighbour) are the only per-bond stream.  They are
-// prefetched one iteration ahead in registers.  Breaking a bond flips the
-// record's sign and clears the bit of the FP64 state array as well.
+// Bond records (one per bond) are the only per-bond stream.  3D: 32 B = 6
+// FP32 coefficients, the neighbour of the bond two places further in the
+// lane's bond sequence (b + 2L: a family's lanes take bonds lane, lane + L,
+// ...), and the bond's FP32 threshold, whose sign carries the bond state.
+// Carrying the later bond's neighbour means a lane knows whom to gather
+// next from a record that arrived an iteration ago, instead of waiting on
+// the record it has just requested.  2D: 16 B = 3 coefficients + the bond's
+// own neighbour, whose sign carries the state.  Records are prefetched two
+// bonds ahead in registers.  Breaking a bond flips the sign in its record
+// and clears the bit of the FP64 state array as well.
 //
 // Node records (2 float4 per node): [2n] = position (x, y, z, 0),
 // [2n+1] = stored displacement (ux, uy, uz, varying-prescribed bits), so one
@@ -85,6 +90,14 @@ __device__ __forceinline__ void load_record(const float4* R, int64_t b, float4& 
   }
 }
 
+// Marks bond b broken in its record: 3D negates the threshold (positive for
+// every intact bond), 2D stores the complement of the neighbour index.
+template <int D>
+__device__ __forceinline__ void mark_broken(float4* R, int64_t b, int m, float thr) {
+  if (D == 3) reinterpret_cast<float*>(R + 2 * b + 1)[3] = -thr;
+  else reinterpret_cast<int*>(R + b)[3] = ~m;
+}
+
 template <int D>
 __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, const float* du, float* acc) {
   if (D == 2) {
@@ -94,6 +107,93 @@ __device__ __forceinline__ void bond_force(const float4& ra, const float4& rb, c
     acc[0] += ra.x * du[0] + ra.y * du[1] + ra.z * du[2];
     acc[1] += ra.y * du[0] + ra.w * du[1] + rb.x * du[2];
     acc[D - 1] += ra.z * du[0] + rb.x * du[1] + rb.y * du[2];
+  }
+}
+
+// One 3D bond: FP32 stretch test (bonds within 2e-4 of the threshold are
+// left to the FP64 pass after the loop) and, if it stays intact, its force.
+struct Bond3Ctx {
+  float4 xk, qk;
+  float uk[3];
+  float acc[3];
+  int b0, corr0, nbroken;
+  bool brk, force, deferred;
+};
+
+__device__ __forceinline__ void bond3(const DevView& v, float4* R, int b, const Rec32& r, const Rec32& g,
+                                      Bond3Ctx& c) {
+  if (!(r.b.w > 0.f)) return;               // broken
+  const float4 um = g.b;
+  if (c.brk) {
+    const float4 xm = g.a;
+    const float x0 = xm.x - c.xk.x, x1 = xm.y - c.xk.y, x2 = xm.z - c.xk.z;
+    const float e0 = um.x - c.qk.x, e1 = um.y - c.qk.y, e2 = um.z - c.qk.z;
+    const float lhs = 2.f * (x0 * e0 + x1 * e1 + x2 * e2) + (e0 * e0 + e1 * e1 + e2 * e2);
+    const float rhs = r.b.w;                // s0b (2 + s0b) |xi|^2
+    if (fabsf(lhs - rhs) <= 2e-4f * rhs) {
+      c.deferred = true;                    // settled in FP64 after the loop
+      return;
+    }
+    if (lhs > rhs) {
+      reinterpret_cast<float*>(R + 2 * (int64_t)b + 1)[3] = -rhs;
+      atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
+      c.nbroken++;
+      return;
+    }
+  }
+  if (!c.force) return;
+  float du[3] = {um.x, um.y, um.z};
+  const unsigned fl = __float_as_uint(um.w);
+  if (fl & 7u) {
+    const int m = v.nbr[b];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      if ((fl >> i) & 1u) du[i] += (float)v.dtv[3 * m + i];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) du[i] -= c.uk[i];
+  bond_force<3>(r.a, r.b, du, c.acc);
+  if (c.corr0 >= 0) corr_apply<3>(v, (int64_t)c.corr0 + (b - c.b0), du, c.acc);
+}
+
+// The 3D family loop of one lane: bonds b0 + lane, + L, ...  Unrolled by two
+// with fixed register sets (A, B): while bond b is computed from set A, the
+// record of b + L and the node record of its neighbour are in flight in set
+// B.  The neighbour of b + L is known a bond earlier, from record b - L
+// (records name the neighbour of the bond 2L further on), so the gather does
+// not wait for the record it belongs to.
+template <int L>
+__device__ __forceinline__ void family_loop3(const DevView& v, float4* R, const float4* nr, int b, int b1,
+                                             Bond3Ctx& c) {
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  Rec32 rA, rB, gA, gB;
+  rA.a = rA.b = rB.a = rB.b = gA.a = gA.b = gB.a = gB.b = z4;
+  if (b >= b1) return;
+  rA = ld_stream32(R + 2 * (int64_t)b);
+  gA = ld_keep32(nr + 2 * (int64_t)__ldg(v.nbr + b));
+  int mB = b + L < b1 ? __ldg(v.nbr + b + L) : -1;
+  int mA = -1;
+  for (;;) {
+    // bond b from set A; set B takes b + L
+    int bn = b + L;
+    if (bn < b1) {
+      rB = ld_stream32(R + 2 * (int64_t)bn);
+      gB = ld_keep32(nr + 2 * (int64_t)mB);
+    }
+    mA = __float_as_int(rA.b.z);            // neighbour of b + 2L
+    bond3(v, R, b, rA, gA, c);
+    b = bn;
+    if (b >= b1) break;
+    // bond b from set B; set A takes b + L
+    bn = b + L;
+    if (bn < b1) {
+      rA = ld_stream32(R + 2 * (int64_t)bn);
+      gA = ld_keep32(nr + 2 * (int64_t)mA);
+    }
+    mB = __float_as_int(rB.b.z);
+    bond3(v, R, b, rB, gB, c);
+    b = bn;
+    if (b >= b1) break;
   }
 }
 
@@ -124,25 +224,42 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
     load_u(node, uk);
     float4* R = a.brec;
     bool deferred = false;
-    // Two-stage pipeline per lane: records two bonds ahead, and the
-    // neighbour's node record of the next bond requested before the current
-    // bond is computed, so a record load and a gather are in flight while a
-    // bond is tested and summed.
     int b = b0 + lane;
     const float4 z4 = make_float4(0, 0, 0, 0);
     float4 ra = z4, rb = z4, na = z4, nb = z4;
-    if (b < b1) load_record<D>(R, b, ra, rb);
-    if (b + L < b1) load_record<D>(R, b + L, na, nb);
-    int m = b < b1 ? __float_as_int(D == 3 ? rb.z : ra.w) : -1;
+    if constexpr (D == 3) {
+      Bond3Ctx c;
+      c.xk = xk;
+      c.qk = qk;
+#pragma unroll
+      for (int i = 0; i < 3; i++) { c.uk[i] = uk[i]; c.acc[i] = 0.f; }
+      c.b0 = b0;
+      c.corr0 = corr0;
+      c.nbroken = 0;
+      c.brk = brk;
+      c.force = force;
+      c.deferred = false;
+      family_loop3<L>(v, R, nr, b, b1, c);
+#pragma unroll
+      for (int i = 0; i < 3; i++) acc[i] = c.acc[i];
+      nbroken = c.nbroken;
+      deferred = c.deferred;
+      b = b1;
+    }
+    if (D == 2 && b < b1) load_record<D>(R, b, ra, rb);
+    if (D == 2 && b + L < b1) load_record<D>(R, b + L, na, nb);
+    int m = D == 2 && b < b1 ? __float_as_int(ra.w) : -1;
     Rec32 g;
     g.a = z4;
     g.b = z4;
     if (m >= 0) g = ld_keep32(nr + 2 * m);
-    while (b < b1) {
+    // 2D: two-stage pipeline per lane, records two bonds ahead and the next
+    // neighbour's node record requested before the current bond is computed
+    while (D == 2 && b < b1) {
       const int bn = b + L;
       float4 qa = z4, qb = z4;
       if (bn + L < b1) load_record<D>(R, bn + L, qa, qb);
-      const int mn = bn < b1 ? __float_as_int(D == 3 ? nb.z : na.w) : -1;
+      const int mn = bn < b1 ? __float_as_int(na.w) : -1;
       Rec32 gn;
       gn.a = z4;
       gn.b = z4;
@@ -169,8 +286,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
             cut = true;
           } else if (lhs > rhs) {
             cut = true;
-            int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
-            *mslot = ~m;
+            mark_broken<D>(R, b, m, rhs);
             atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
             nbroken++;
           }
@@ -206,8 +322,8 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
       for (b = b0 + lane; b < b1; b += L) {
         ra = R[(int64_t)RS * b];
         if (D == 3) rb = R[(int64_t)RS * b + 1];
-        const int m = __float_as_int(D == 3 ? rb.z : ra.w);
-        if (m < 0) continue;
+        if (D == 3 ? !(rb.w > 0.f) : __float_as_int(ra.w) < 0) continue;
+        const int m = D == 3 ? v.nbr[b] : __float_as_int(ra.w);
         const float4 xm = nr[2 * m], um = nr[2 * m + 1];
         const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
         const float e0 = um.x - qk.x, e1 = um.y - qk.y, e2 = D == 3 ? um.z - qk.z : 0.f;
@@ -222,8 +338,7 @@ __device__ __forceinline__ void mixed_family_item(const StepArgs& a, const float
         }
         if (!(fabsf(lhs - rhs) <= 2e-4f * rhs)) continue;
         if (stretch_over_fp64<D>(v, a.u_n, node, m, bond_s0(v.fam_s0[f], v.s0_pert, h))) {
-          int* mslot = (int*)(R + (int64_t)RS * b + (D == 3 ? 1 : 0)) + (D == 3 ? 2 : 3);
-          *mslot = ~m;
+          mark_broken<D>(R, b, m, rhs);
           atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
           nbroken++;
         } else if (force) {
@@ -361,12 +476,13 @@ __global__ void __launch_bounds__(256, D == 3 ? 4 : 6) k_step_mixed(StepArgs a) 
 // Mixed-precision bond records from the FP32 coefficients, the bond states and
 // the per-bond thresholds.
 template <int D>
-__global__ void k_pack_bonds(DevView v, float pertf, float4* rec) {
+__global__ void k_pack_bonds(DevView v, float pertf, int lanes, float4* rec) {
   const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (f >= v.n_fam) return;
   const int k = v.fam_node[f];
   const int64_t nb = v.n_bond;
-  for (int b = v.fam_ptr[f] + (threadIdx.x & 31); b < v.fam_ptr[f + 1]; b += 32) {
+  const int b1 = v.fam_ptr[f + 1];
+  for (int b = v.fam_ptr[f] + (threadIdx.x & 31); b < b1; b += 32) {
     const int m = v.nbr[b];
     const bool intact = (v.state[b >> 5] >> (b & 31)) & 1u;
     const int mb = intact ? m : ~m;
@@ -378,8 +494,10 @@ __global__ void k_pack_bonds(DevView v, float pertf, float4* rec) {
       const float4 xk = v.Xf[k], xm = v.Xf[m];
       const float x0 = xm.x - xk.x, x1 = xm.y - xk.y, x2 = xm.z - xk.z;
       const float thr = s0b * (2.f + s0b) * (x0 * x0 + x1 * x1 + x2 * x2);
+      const int ahead = b + 2 * lanes < b1 ? v.nbr[b + 2 * lanes] : -1;
       rec[2 * (int64_t)b] = make_float4(v.coef32[b], v.coef32[nb + b], v.coef32[2 * nb + b], v.coef32[3 * nb + b]);
-      rec[2 * (int64_t)b + 1] = make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(mb), thr);
+      rec[2 * (int64_t)b + 1] =
+          make_float4(v.coef32[4 * nb + b], v.coef32[5 * nb + b], __int_as_float(ahead), intact ? thr : -thr);
     }
   }
 }
@@ -420,11 +538,11 @@ cudaError_t launch_step_mixed(const StepArgs& a, int lp, int lf, cudaStream_t s)
   return a.v.dim == 2 ? mixed_dispatch<2>(a, lp, lf, s) : mixed_dispatch<3>(a, lp, lf, s);
 }
 
-cudaError_t launch_pack_bonds(const DevView& v, float pertf, float4* rec, cudaStream_t s) {
+cudaError_t launch_pack_bonds(const DevView& v, float pertf, int lanes, float4* rec, cudaStream_t s) {
   if (v.n_fam == 0) return cudaSuccess;
   const int blocks = (v.n_fam + 7) / 8;
-  if (v.dim == 2) k_pack_bonds<2><<<blocks, 256, 0, s>>>(v, pertf, rec);
-  else k_pack_bonds<3><<<blocks, 256, 0, s>>>(v, pertf, rec);
+  if (v.dim == 2) k_pack_bonds<2><<<blocks, 256, 0, s>>>(v, pertf, lanes, rec);
+  else k_pack_bonds<3><<<blocks, 256, 0, s>>>(v, pertf, lanes, rec);
   return cudaGetLastError();
 }
 
