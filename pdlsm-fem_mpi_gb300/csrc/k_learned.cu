@@ -14,13 +14,14 @@
 // near-linear on inputs unlike its training set (ReLU did not), so the
 // correction stays useful once it has removed the smooth error the training
 // residuals were made of.  Training (forward, backward,
-// Adam) runs with BF16 GEMM operands and FP32 accumulation in the tiled
-// kernels below; inference of one residual is one block-wide kernel
-// (k_infer_block) per Krylov iteration.
+// Adam) runs its GEMMs on the tensor cores (mma.sync, BF16 operands, FP32
+// accumulation, split K for the long products); inference of one residual
+// is one block-wide kernel (k_infer_block) per Krylov iteration.
 // Reductions have a fixed order and there are no atomics, so results are
 // reproducible.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "learned.h"
@@ -34,69 +35,128 @@ using bf16 = __nv_bfloat16;
 
 // C[M x N] = alpha op(A)[M x K] op(B)[K x N] + beta C, A and B in BF16, C in FP32:
 // op(A)(m, k) = TA ? A[k lda + m] : A[m lda + k]; op(B)(k, n) = TB ? B[n ldb + k] : B[k ldb + n].
-// 64 x 64 tiles, 16-deep K slices in shared memory, 4 x 4 outputs per thread.
+// Tensor cores: mma.sync m16n8k16 with BF16 operands and FP32 accumulators.
+// A block of 4 warps computes a 64 x 64 tile of C over the K range of its
+// split (blockIdx.z); each warp a 32 x 32 quarter as 2 x 4 MMA tiles.  K
+// slices of 32 are staged in shared memory as As[m][k] and Bs[n][k] (k
+// contiguous, rows padded to 40 BF16 against bank conflicts).  With several
+// splits the partial tiles go to `part` and k_gemm_reduce adds them in split
+// order, so the result does not depend on scheduling.
+constexpr int kGT = 64, kGK = 32, kGPad = 40;
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const bf16* __restrict__ A, int lda,
-                                              const bf16* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
-                                              float alpha, float beta) {
-  __shared__ float As[16][65];
-  __shared__ float Bs[16][65];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-  float acc[4][4];
+__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, int kchunk, const bf16* __restrict__ A,
+                                                 int lda, const bf16* __restrict__ B, int ldb, float* __restrict__ C,
+                                                 int ldc, float alpha, float beta, float* __restrict__ part) {
+  __shared__ __align__(16) bf16 As[kGT][kGPad];
+  __shared__ __align__(16) bf16 Bs[kGT][kGPad];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int g = lane >> 2, tg = lane & 3;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  const bf16 zero = __float2bfloat16(0.f);
+  float acc[2][4][4];
 #pragma unroll
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < 2; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += 16) {
-    for (int e = threadIdx.x; e < 1024; e += 256) {
-      const int mm = TA ? e % 64 : e / 16, kk = TA ? e / 64 : e % 16;
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+  for (int k0 = kb; k0 < ke; k0 += kGK) {
+    for (int e = threadIdx.x; e < kGT * kGK; e += blockDim.x) {
+      // threads run along the contiguous index of the source
+      const int mm = TA ? e % kGT : e / kGK, kk = TA ? e / kGT : e % kGK;
       const int m = m0 + mm, k = k0 + kk;
-      float val = 0.f;
-      if (m < M && k < K) val = __bfloat162float(TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k]);
-      As[kk][mm] = val;
+      As[mm][kk] = (m < M && k < ke) ? (TA ? A[(int64_t)k * lda + m] : A[(int64_t)m * lda + k]) : zero;
     }
-    for (int e = threadIdx.x; e < 1024; e += 256) {
-      const int nn = TB ? e / 16 : e % 64, kk = TB ? e % 16 : e / 64;
-      const int nI = n0 + nn, k = k0 + kk;
-      float val = 0.f;
-      if (nI < N && k < K) val = __bfloat162float(TB ? B[(int64_t)nI * ldb + k] : B[(int64_t)k * ldb + nI]);
-      Bs[kk][nn] = val;
+    for (int e = threadIdx.x; e < kGT * kGK; e += blockDim.x) {
+      const int nn = TB ? e / kGK : e % kGT, kk = TB ? e % kGK : e / kGT;
+      const int n = n0 + nn, k = k0 + kk;
+      Bs[nn][kk] = (n < N && k < ke) ? (TB ? B[(int64_t)n * ldb + k] : B[(int64_t)k * ldb + n]) : zero;
     }
     __syncthreads();
 #pragma unroll
-    for (int kk = 0; kk < 16; kk++) {
-      float av[4], bv[4];
+    for (int ks = 0; ks < kGK; ks += 16) {
+      uint32_t af[2][4], bfr[4][2];
 #pragma unroll
-      for (int i = 0; i < 4; i++) av[i] = As[kk][ty * 4 + i];
+      for (int i = 0; i < 2; i++) {
+        const int r = wm + i * 16 + g;
+        af[i][0] = ld_pair(&As[r][ks + 2 * tg]);
+        af[i][1] = ld_pair(&As[r + 8][ks + 2 * tg]);
+        af[i][2] = ld_pair(&As[r][ks + 2 * tg + 8]);
+        af[i][3] = ld_pair(&As[r + 8][ks + 2 * tg + 8]);
+      }
 #pragma unroll
-      for (int j = 0; j < 4; j++) bv[j] = Bs[kk][tx * 4 + j];
+      for (int j = 0; j < 4; j++) {
+        const int c = wn + j * 8 + g;
+        bfr[j][0] = ld_pair(&Bs[c][ks + 2 * tg]);
+        bfr[j][1] = ld_pair(&Bs[c][ks + 2 * tg + 8]);
+      }
 #pragma unroll
-      for (int i = 0; i < 4; i++)
+      for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
     }
     __syncthreads();
   }
+  float* P = part ? part + (int64_t)blockIdx.z * M * N : nullptr;
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int m = m0 + ty * 4 + i;
-    if (m >= M) continue;
+  for (int i = 0; i < 2; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int nI = n0 + tx * 4 + j;
-      if (nI >= N) continue;
-      float* cp = C + (int64_t)m * ldc + nI;
-      *cp = beta == 0.f ? alpha * acc[i][j] : alpha * acc[i][j] + beta * *cp;
-    }
-  }
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int m = m0 + wm + i * 16 + g + (q >= 2 ? 8 : 0);
+        const int n = n0 + wn + j * 8 + 2 * tg + (q & 1);
+        if (m >= M || n >= N) continue;
+        if (P) {
+          P[(int64_t)m * N + n] = acc[i][j][q];
+        } else {
+          float* cp = C + (int64_t)m * ldc + n;
+          *cp = beta == 0.f ? alpha * acc[i][j][q] : alpha * acc[i][j][q] + beta * *cp;
+        }
+      }
+}
+
+// C = alpha sum_z part[z] + beta C, the splits added in order
+__global__ void k_gemm_reduce(int M, int N, int splits, const float* __restrict__ part, float* __restrict__ C,
+                              int ldc, float alpha, float beta) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)M * N) return;
+  float s = 0.f;
+  for (int z = 0; z < splits; z++) s += part[(int64_t)z * M * N + i];
+  float* cp = C + (i / N) * ldc + (i % N);
+  *cp = beta == 0.f ? alpha * s : alpha * s + beta * *cp;
+}
+
+// Splits of K for an M x N x K product: enough blocks to cover the SMs about
+// twice, each split at least 64 deep.
+int gemm_splits(int M, int N, int K) {
+  const int tiles = ((M + kGT - 1) / kGT) * ((N + kGT - 1) / kGT);
+  const int want = (304 + tiles - 1) / tiles;
+  return std::max(1, std::min(want, K / 64));
 }
 
 template <bool TA, bool TB>
 void gemm(int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, float alpha,
-          float beta, cudaStream_t s) {
-  dim3 grid((N + 63) / 64, (M + 63) / 64);
-  k_gemm<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, alpha, beta);
+          float beta, float* work, cudaStream_t s) {
+  const int splits = work ? gemm_splits(M, N, K) : 1;
+  const int kchunk = ((K + splits - 1) / splits + kGK - 1) / kGK * kGK;
+  const int nz = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, nz);
+  k_gemm_tc<TA, TB><<<grid, 128, 0, s>>>(M, N, K, kchunk, A, lda, B, ldb, C, ldc, alpha, beta,
+                                          nz > 1 ? work : nullptr);
+  if (nz > 1) k_gemm_reduce<<<(int)(((int64_t)M * N + 255) / 256), 256, 0, s>>>(M, N, nz, work, C, ldc, alpha, beta);
 }
 
 // Z[m][n] += bias[n]; H = BF16(tanh(Z)) (or Z without activation)
@@ -435,6 +495,19 @@ int grid_of(int64_t n) { return (int)((n + kT - 1) / kT); }
 
 // ----------------------------------------------------------------- MLP ----
 
+int64_t gemm_work_floats(int Bmax, int nin, int H, int nout) {
+  int64_t mx = 0;
+  for (int B = 1; B <= Bmax; B++) {   // any batch size up to Bmax
+    const int shapes[8][3] = {{B, H, nin}, {B, H, H},   {B, nout, H}, {nout, H, B},
+                              {B, H, nout}, {H, H, B}, {B, H, H},    {H, nin, B}};
+    for (const auto& sh : shapes) {
+      const int splits = gemm_splits(sh[0], sh[1], sh[2]);
+      if (splits > 1) mx = std::max(mx, (int64_t)splits * sh[0] * sh[1]);
+    }
+  }
+  return mx;
+}
+
 void Mlp::param_views(float* base, float** W1, float** b1, float** W2, float** b2, float** W3, float** b3) const {
   float* p = base;
   *W1 = p; p += (size_t)H * nin;
@@ -447,17 +520,18 @@ void Mlp::param_views(float* base, float** W1, float** b1, float** W2, float** b
 
 cudaError_t Mlp::forward_backward(int B, const bf16* X, const float* T, const float* wrow, bool grads,
                                   cudaStream_t s) {
+  // split K only with the work space sized for Bmax rows (B <= Bmax)
   float *W1, *b1, *W2, *b2, *W3, *b3;
   param_views(w, &W1, &b1, &W2, &b2, &W3, &b3);
   const bf16* W1h = w16;
   const bf16* W2h = W1h + (size_t)H * nin + H;
   const bf16* W3h = W2h + (size_t)H * H + H;
   const int g1 = grid_of((int64_t)B * H), g3 = grid_of((int64_t)B * nout);
-  gemm<false, true>(B, H, nin, X, nin, W1h, nin, Z1, H, 1.f, 0.f, s);
+  gemm<false, true>(B, H, nin, X, nin, W1h, nin, Z1, H, 1.f, 0.f, work, s);
   k_bias_act<<<g1, kT, 0, s>>>(B, H, Z1, b1, H1, 1);
-  gemm<false, true>(B, H, H, H1, H, W2h, H, Z2, H, 1.f, 0.f, s);
+  gemm<false, true>(B, H, H, H1, H, W2h, H, Z2, H, 1.f, 0.f, work, s);
   k_bias_act<<<g1, kT, 0, s>>>(B, H, Z2, b2, H2, 1);
-  gemm<false, true>(B, nout, H, H2, H, W3h, H, Y, nout, 1.f, 0.f, s);
+  gemm<false, true>(B, nout, H, H2, H, W3h, H, Y, nout, 1.f, 0.f, work, s);
   k_bias_act<<<g3, kT, 0, s>>>(B, nout, Y, b3, nullptr, 0);
   if (!T) return cudaGetLastError();
   k_loss_grad<<<B, kT, 0, s>>>(B, nout, Y, T, wrow, dY, dY16, loss_row);
@@ -466,17 +540,17 @@ cudaError_t Mlp::forward_backward(int B, const bf16* X, const float* T, const fl
   float *gW1, *gb1, *gW2, *gb2, *gW3, *gb3;
   param_views(g, &gW1, &gb1, &gW2, &gb2, &gW3, &gb3);
   // layer 3: gW3 = dY^T H2, gb3 = sum dY, dH2 = dY W3
-  gemm<true, false>(nout, H, B, dY16, nout, H2, H, gW3, H, 1.f, 0.f, s);
+  gemm<true, false>(nout, H, B, dY16, nout, H2, H, gW3, H, 1.f, 0.f, work, s);
   k_colsum<<<grid_of(nout), kT, 0, s>>>(B, nout, dY, gb3);
-  gemm<false, false>(B, H, nout, dY16, nout, W3h, H, dH, H, 1.f, 0.f, s);
+  gemm<false, false>(B, H, nout, dY16, nout, W3h, H, dH, H, 1.f, 0.f, work, s);
   k_act_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z2, dZ, dZ16);
   // layer 2
-  gemm<true, false>(H, H, B, dZ16, H, H1, H, gW2, H, 1.f, 0.f, s);
+  gemm<true, false>(H, H, B, dZ16, H, H1, H, gW2, H, 1.f, 0.f, work, s);
   k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb2);
-  gemm<false, false>(B, H, H, dZ16, H, W2h, H, dH, H, 1.f, 0.f, s);
+  gemm<false, false>(B, H, H, dZ16, H, W2h, H, dH, H, 1.f, 0.f, work, s);
   k_act_back<<<g1, kT, 0, s>>>((int64_t)B * H, dH, Z1, dZ, dZ16);
   // layer 1
-  gemm<true, false>(H, nin, B, dZ16, H, X, nin, gW1, nin, 1.f, 0.f, s);
+  gemm<true, false>(H, nin, B, dZ16, H, X, nin, gW1, nin, 1.f, 0.f, work, s);
   k_colsum<<<grid_of(H), kT, 0, s>>>(B, H, dZ, gb1);
   return cudaGetLastError();
 }
@@ -573,6 +647,15 @@ cudaError_t learned_stage(int B, int nc, const int* idx, const float* S_r, const
 cudaError_t learned_stage_raw(int B, int nc, const float* Xf, bf16* X, cudaStream_t s) {
   const int64_t n = (int64_t)B * nc;
   k_stage_raw<<<grid_of(n), kT, 0, s>>>(n, Xf, X);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_add_scalar(const float* x, float* acc) { *acc += *x; }
+}  // namespace
+
+cudaError_t learned_add_scalar(const float* x, float* acc, cudaStream_t s) {
+  k_add_scalar<<<1, 1, 0, s>>>(x, acc);
   return cudaGetLastError();
 }
 

@@ -293,6 +293,10 @@ pdx_status pdx_learned_setup(pdx_model* m, int cx, int cy, int cz, int hidden, u
   net.dZ16 = L->buf.alloc<__nv_bfloat16>((size_t)B * hidden);
   net.loss_row = L->buf.alloc<float>(B);
   net.loss = L->buf.alloc<float>(1);
+  {
+    const int64_t wf = gemm_work_floats(B, nc, hidden, nc);
+    if (wf > 0) net.work = L->buf.alloc<float>(wf);
+  }
   L->rc = L->buf.alloc<float>(nc);
   L->x16 = L->buf.alloc<__nv_bfloat16>(nc);
   L->y = L->buf.alloc<float>(nc);
@@ -384,31 +388,45 @@ pdx_status pdx_learned_train(pdx_model* m, int epochs, float lr, uint64_t seed, 
   if (ratio.empty()) return set_error(PDX_ERR_NUMERIC, "training pairs are all zero");
   std::nth_element(ratio.begin(), ratio.begin() + ratio.size() / 2, ratio.end());
   L->sigma = ratio[ratio.size() / 2];
+  // every epoch's shuffled order goes to the device at once, and the batch
+  // losses are summed there: the loop issues kernels only and synchronises
+  // once at the end
   std::mt19937_64 rng(seed);
-  std::vector<int> order(n);
+  std::vector<int> order(n), orders((size_t)epochs * n);
   std::iota(order.begin(), order.end(), 0);
-  float last = 0.f;
   for (int ep = 0; ep < epochs; ep++) {
     std::shuffle(order.begin(), order.end(), rng);
-    double sum = 0;
-    int nbatch = 0;
-    for (int i0 = 0; i0 + 1 < n; i0 += B) {
+    std::copy(order.begin(), order.end(), orders.begin() + (size_t)ep * n);
+  }
+  int* d_orders = nullptr;
+  float* d_loss_sum = nullptr;
+  st = cuda_check(cudaMallocAsync(&d_orders, orders.size() * sizeof(int), s), "training orders");
+  if (!st) st = cuda_check(cudaMallocAsync(&d_loss_sum, sizeof(float), s), "training loss");
+  if (st) return st;
+  cudaMemcpyAsync(d_orders, orders.data(), orders.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(d_loss_sum, 0, sizeof(float), s);
+  int nbatch = 0;
+  for (int ep = 0; ep < epochs && !st; ep++) {
+    if (ep == epochs - 1) cudaMemsetAsync(d_loss_sum, 0, sizeof(float), s);
+    nbatch = 0;
+    for (int i0 = 0; i0 + 1 < n && !st; i0 += B) {
       const int b = std::min(B, n - i0);
-      cudaMemcpyAsync(L->bidx, order.data() + i0, b * sizeof(int), cudaMemcpyHostToDevice, s);
-      st = cuda_check(learned_stage(b, nc, L->bidx, L->S_r, L->S_x, L->S_scale, L->sigma, L->Xb, L->Tb, L->Wb, s),
-                      "stage");
+      st = cuda_check(learned_stage(b, nc, d_orders + (size_t)ep * n + i0, L->S_r, L->S_x, L->S_scale, L->sigma,
+                                    L->Xb, L->Tb, L->Wb, s), "stage");
       if (!st) st = cuda_check(L->net.forward_backward(b, L->Xb, L->Tb, L->Wb, true, s), "forward/backward");
       if (!st) st = cuda_check(L->net.adam_step(lr, s), "Adam");
-      if (st) return st;
-      float h = 0;
-      cudaMemcpyAsync(&h, L->net.loss, 4, cudaMemcpyDeviceToHost, s);
-      st = cuda_check(cudaStreamSynchronize(s), "training");
-      if (st) return st;
-      sum += h;
+      if (!st && ep == epochs - 1) st = cuda_check(learned_add_scalar(L->net.loss, d_loss_sum, s), "loss");
       nbatch++;
     }
-    last = nbatch ? (float)(sum / nbatch) : 0.f;
   }
+  float last_sum = 0.f;
+  if (!st) cudaMemcpyAsync(&last_sum, d_loss_sum, sizeof(float), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d_orders, s);
+  cudaFreeAsync(d_loss_sum, s);
+  pdx_status st2 = cuda_check(cudaStreamSynchronize(s), "training");
+  if (st) return st;
+  if (st2) return st2;
+  const float last = nbatch ? last_sum / nbatch : 0.f;
   L->trained = true;
   L->losses = 0;
   L->disabled = false;

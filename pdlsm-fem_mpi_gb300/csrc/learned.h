@@ -46,6 +46,7 @@ struct Mlp {
   __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *dY16 = nullptr, *dZ16 = nullptr;
   float* loss_row = nullptr;
   float* loss = nullptr;
+  float* work = nullptr;             // split-K partial products of the GEMMs (gemm_work_floats)
   int64_t n_params() const { return (int64_t)H * nin + H + (int64_t)H * H + H + (int64_t)nout * H + nout; }
   void param_views(float* base, float** W1, float** b1, float** W2, float** b2, float** W3, float** b3) const;
   // forward on X (B x nin, BF16); with T (B x nout) also the loss
@@ -66,6 +67,10 @@ struct Mlp {
   cudaError_t infer_block(const float* x, float sigma, float* y, float* scale, cudaStream_t s);
 };
 
+// Floats of split-K work space the GEMMs of Mlp::forward_backward need for
+// batches of up to B rows.
+int64_t gemm_work_floats(int B, int nin, int H, int nout);
+
 cudaError_t coarse_restrict(const CoarseSpace& cs, bool average, const double* r, float* out, cudaStream_t s);
 cudaError_t coarse_prolong_add(const CoarseSpace& cs, const float* c, const float* scale, double* z,
                                cudaStream_t s);
@@ -75,6 +80,8 @@ cudaError_t learned_norms(int count, int nc, const float* S, float* norms, cudaS
 cudaError_t learned_stage(int B, int nc, const int* idx, const float* S_r, const float* S_e, const float* norms,
                           float sigma, __nv_bfloat16* X, float* T, float* W, cudaStream_t s);
 cudaError_t learned_stage_raw(int B, int nc, const float* Xf, __nv_bfloat16* X, cudaStream_t s);
+// *acc += *x on the device (one thread; stream ordered)
+cudaError_t learned_add_scalar(const float* x, float* acc, cudaStream_t s);
 cudaError_t learned_random_rhs(int64_t n, uint64_t seed, double* b, cudaStream_t s);
 
 // Everything the learned preconditioner of one model owns.
