@@ -139,13 +139,18 @@ def cpu_sample_batch(cmds, target_s: float = 15.0, threads: int = 0):
     return bonds_steps / el, used, el, o_threads()
 
 
+# The implicit legs (c3, c5) time whole solves; --steps is capped to this many samples.
+IMPLICIT_MAX_STEPS = 5
+
+
 def bench_implicit(args):
     """C5: implicit Newmark; solve time to a 1e-8 true FP64 residual per step for the learned two-level flexible CG
     and for block-Jacobi flexible CG (the plain method), each from the same state after the training steps."""
     import meshgen
     import pdx
     tmp = tempfile.mkdtemp(prefix="pdx_bench_")
-    nsteps = args.train_steps + args.steps + 1
+    steps = min(args.steps, IMPLICIT_MAX_STEPS)   # timed Newmark steps (each a whole solve)
+    nsteps = args.train_steps + steps + 1
     if args.c5_size == "full":
         mesh, kw = meshgen.config_c5(nsteps=nsteps)
         cells = (25, 12, 5)
@@ -177,7 +182,7 @@ def bench_implicit(args):
                 loss = m.learned_train(epochs=100, lr=1e-3, seed=0)
                 t_train = time.perf_counter() - t0
             sec, its, resid = [], [], []
-            for _ in range(args.steps):
+            for _ in range(steps):
                 i = m.newmark_step(method)
                 sec.append(i.seconds)
                 its.append(i.iterations)
@@ -189,7 +194,7 @@ def bench_implicit(args):
     p, l = res[4], res[5]
     du = float(np.linalg.norm(l["u"] - p["u"]) / max(np.linalg.norm(p["u"]), 1e-300))
     line = {"metric": "implicit Newmark solve time to 1e-8 true residual (s per step)", "value": l["sec"],
-            "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.train_steps, "ms_per_step": l["sec"] * 1e3,
+            "unit": "s", "n_gpus": 1, "steps": steps, "warmup": args.train_steps, "ms_per_step": l["sec"] * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
             "data": "synthetic (seeded meshgen config_c5)",
             "config": {"workload": f"c5 ({args.c5_size}): Hex8 box, inclined penny crack, 5% PD zone, Newmark "
@@ -220,17 +225,19 @@ def bench_quasi(args):
     names = {0: "Jacobi PCG", 1: "block-Jacobi PCG", 2: "BiCGStab (Jacobi)", 3: "mixed FP32 PCG + FP64 refinement"}
     res, u_end = {}, {}
     loaded = None
+    # each sample is a whole solve (0.3 to 2 s): at most 5 timed after 1 untimed
+    steps, warmup = min(args.steps, IMPLICIT_MAX_STEPS), min(args.warmup, 1)
     for method in (1, 0, 3, 2):
         with pdx.Model(cmd, device=0, precision=0) as m:
             sec, its, resid, wall = [], [], [], []
-            for rep in range(args.warmup + args.steps):
+            for rep in range(warmup + steps):
                 m.quasi_init()
                 m.quasi_step(method)
                 if loaded is None:
                     loaded = m.assemble(2, m.state()[0])
                 t0 = time.perf_counter()
                 i = m.quasi_step(method)
-                if rep >= args.warmup:
+                if rep >= warmup:
                     wall.append(time.perf_counter() - t0)
                     sec.append(i.seconds)
                     its.append(i.iterations)
@@ -261,7 +268,7 @@ def bench_quasi(args):
                "gpu_vs_direct_rel_diff": float(np.linalg.norm(x_gpu - x_cpu) / max(np.linalg.norm(x_cpu), 1e-300))}
     best = min(res.values(), key=lambda r: r["s_per_increment"])
     line = {"metric": "quasi-static solve time to 1e-8 true residual (s per loaded increment)",
-            "value": best["s_per_increment"], "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "value": best["s_per_increment"], "unit": "s", "n_gpus": 1, "steps": steps, "warmup": warmup,
             "ms_per_step": best["s_per_increment"] * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded meshgen config_c3)",
             "config": {"workload": f"c3: 2D quasi-static 401x401-node plate, PD band 30% of the width, 0.2 W "

@@ -272,6 +272,142 @@ __global__ void k_bicg_x2(int64_t n, const double* alpha, const double* omega, c
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// The same three reductions with their final step folded in: every block
+// writes its partial, and the block that finishes last (an atomic ticket
+// after a memory fence) adds the partials in block order exactly as
+// k_dot_final / k_final_ratio / k_final_omega do, so the bits do not change
+// and three single-block launches per iteration disappear.  The ticket is
+// reset by that last block for the next use.
+__device__ __forceinline__ bool last_block(unsigned* ticket) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last;
+}
+
+__device__ __forceinline__ double sum_partials(const double* part, int np, double* sh) {
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += __ldcg(part + i);
+  return block_sum(s, sh);
+}
+
+// partials of r0 . v; the last block sets alpha = rho / (r0 . v) (0 if the dot is 0)
+__global__ void k_bicg_alpha(int64_t n, const double* r0, const double* v, double* part, unsigned* ticket,
+                             const double* rho, double* alpha) {
+  __shared__ double sh[kThreads];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += r0[i] * v[i];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  if (!last_block(ticket)) return;
+  const double d = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *alpha = d != 0.0 ? *rho / d : 0.0;
+    *ticket = 0;
+  }
+}
+
+// partials of t.s and t.t; the last block sets omega = (t.s) / (t.t) (0 if t.t is 0)
+__global__ void k_bicg_omega(int64_t n, const double* t, const double* s, double* part_ts, double* part_tt,
+                             unsigned* ticket, double* omega) {
+  __shared__ double sh[kThreads];
+  double a = 0, b = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    a += t[i] * s[i];
+    b += t[i] * t[i];
+  }
+  a = block_sum(a, sh);
+  b = block_sum(b, sh);
+  if (threadIdx.x == 0) {
+    part_ts[blockIdx.x] = a;
+    part_tt[blockIdx.x] = b;
+  }
+  if (!last_block(ticket)) return;
+  double sa = 0, sb = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    sa += __ldcg(part_ts + i);
+    sb += __ldcg(part_tt + i);
+  }
+  sa = block_sum(sa, sh);
+  sb = block_sum(sb, sh);
+  if (threadIdx.x == 0) {
+    *omega = sb != 0.0 ? sa / sb : 0.0;
+    *ticket = 0;
+  }
+}
+
+// x += alpha ph + omega sh; r = s - omega t; the last block sets rho_next = r0 . r
+__global__ void k_bicg_x_rho(int64_t n, const double* alpha, const double* omega, const double* ph,
+                             const double* shat, const double* s, const double* t, const double* r0, double* x,
+                             double* r, double* part, unsigned* ticket, double* rho_next) {
+  __shared__ double sh[kThreads];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += *alpha * ph[i] + *omega * shat[i];
+    const double ri = s[i] - *omega * t[i];
+    r[i] = ri;
+    acc += r0[i] * ri;
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  if (!last_block(ticket)) return;
+  const double d = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *rho_next = d;
+    *ticket = 0;
+  }
+}
+
+// Fused PCG steps (precision T of the vectors, FP64 scalars and sums).
+// partials of p.q; the last block stores the sum
+template <typename T>
+__global__ void k_cg_pq(int64_t n, const T* p, const T* q, double* part, unsigned* ticket, double* out) {
+  __shared__ double sh[kThreads];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)p[i] * (double)q[i];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  if (!last_block(ticket)) return;
+  const double d = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *out = d;
+    *ticket = 0;
+  }
+}
+
+// x += alpha p; r -= alpha q (alpha = rz / pq); with dinv also z = D^-1 r and
+// the partials of r.z, the last block storing rz_new
+template <typename T>
+__global__ void k_cg_update_jacobi(int64_t n, const double* rz, const double* pq, const T* p, const T* q, T* x,
+                                   T* r, const double* dinv, T* z, double* part, unsigned* ticket, double* rz_new) {
+  __shared__ double sh[kThreads];
+  const double alpha = *pq != 0.0 ? *rz / *pq : 0.0;
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
+    r[i] = ri;
+    if (dinv) {
+      const T zi = (T)(dinv[i] * (double)ri);
+      z[i] = zi;
+      acc += (double)ri * (double)zi;
+    }
+  }
+  if (!dinv) return;
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  if (!last_block(ticket)) return;
+  const double d = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *rz_new = d;
+    *ticket = 0;
+  }
+}
+
 // Restarted GMRES: Arnoldi basis V (rows of length ld), classical
 // Gram-Schmidt applied twice, Givens rotations of the small Hessenberg column
 // on the host.  Partial sums keep a fixed order (grid-stride, block tree,
@@ -380,9 +516,13 @@ void spmv_t(int64_t n, double avg, const int64_t* ia, const int* ja, const T* a,
 // Preconditioned CG in precision T on (ia, ja, aT); solves for x given b, both in T.
 // Returns iterations; stops when the recursive residual is below rtol*||b|| or max_iter.
 template <typename T>
+// ticket: a zeroed device word for the reductions' last-block step (the
+// caller's; the allocation-free solve keeps it in its fixed work space);
+// graphs: replay chunks of iterations as a CUDA graph (off where nothing
+// may be allocated).
 int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, const T* aT, const T* b, T* x,
              const double* dinv, int64_t nb, const int64_t* bptr, const double* binv, double rtol, int max_iter,
-             double* dscal, T* r, T* z, T* p, T* q) {
+             double* dscal, T* r, T* z, T* p, T* q, unsigned* ticket, bool graphs) {
   cudaStream_t s = c.s;
   double* rz = dscal + 0;
   double* rz_new = dscal + 1;
@@ -415,15 +555,42 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
   // (the caller then sees a true residual above rtol and may switch method)
   double best = INFINITY;
   int best_it = 0;
-  while (it < max_iter) {
-    for (int k = 0; k < chunk && it < max_iter; k++, it++) {
-      spmv_t<T>(n, avg, ia, ja, aT, p, q, s);
-      c.dot<T>(n, p, q, pq);
-      k_cg_update<T><<<g, kThreads, 0, s>>>(n, rz, pq, p, q, x, r);
+  // r.z of the iteration and of the one before in two slots (rz, rz_new by
+  // parity, no copy); the reductions' final step runs in their last block;
+  // with Jacobi the preconditioner and r.z are fused into the update (four
+  // launches per iteration); chunks of ten iterations replay a CUDA graph
+  auto iteration = [&](int k) {
+    double* rz_cur = (k & 1) ? rz_new : rz;
+    double* rz_next = (k & 1) ? rz : rz_new;
+    spmv_t<T>(n, avg, ia, ja, aT, p, q, s);
+    k_cg_pq<T><<<g, kThreads, 0, s>>>(n, p, q, c.part, ticket, pq);
+    if (binv) {
+      k_cg_update_jacobi<T><<<g, kThreads, 0, s>>>(n, rz_cur, pq, p, q, x, r, nullptr, z, c.part, ticket, rz_next);
       precond(r, z);
-      c.dot<T>(n, r, z, rz_new);
-      k_cg_dir<T><<<g, kThreads, 0, s>>>(n, rz_new, rz, z, p);
-      k_copy_scalar<<<1, 1, 0, s>>>(rz_new, rz);
+      c.dot<T>(n, r, z, rz_next);
+    } else {
+      k_cg_update_jacobi<T><<<g, kThreads, 0, s>>>(n, rz_cur, pq, p, q, x, r, dinv, z, c.part, ticket, rz_next);
+    }
+    k_cg_dir<T><<<g, kThreads, 0, s>>>(n, rz_next, rz_cur, z, p);
+  };
+  cudaGraphExec_t gexec = nullptr;
+  if (graphs) {
+    cudaGraph_t graph;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (int k = 0; k < chunk; k++) iteration(k);   // chunks start at an even iteration
+      if (cudaStreamEndCapture(s, &graph) == cudaSuccess) {
+        if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+        cudaGraphDestroy(graph);
+      }
+    }
+    cudaGetLastError();
+  }
+  while (it < max_iter) {
+    if (gexec && max_iter - it >= chunk) {
+      cudaGraphLaunch(gexec, s);
+      it += chunk;
+    } else {
+      for (int k = 0; k < chunk && it < max_iter; k++, it++) iteration(it);
     }
     c.dot<T>(n, r, r, rr);
     double hr = 0;
@@ -439,6 +606,7 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
       break;
     }
   }
+  if (gexec) cudaGraphExecDestroy(gexec);
   return it;
 }
 
@@ -569,6 +737,9 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   double* dinv = nullptr;
   cudaMallocAsync(&dinv, n * sizeof(double), s);
   k_diag_inv<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A.ia, A.ja, A.a, dinv);
+  unsigned* ticket = nullptr;   // the reductions' last-block ticket
+  cudaMallocAsync(&ticket, sizeof(unsigned), s);
+  cudaMemsetAsync(ticket, 0, sizeof(unsigned), s);
   // diagonal blocks for block-Jacobi: consecutive rows in groups of block_dim
   int64_t nb = 0;
   int64_t* bptr = nullptr;
@@ -594,7 +765,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   int iters = 0;
   if (method == 0 || method == 1) {
     iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, nb, bptr, binv, rtol, max_iter, dscal, r, z,
-                             p, q);
+                             p, q, ticket, true);
   } else if (method == 2) {
     // BiCGStab, right Jacobi preconditioning
     double *r0, *v, *ss, *t, *ph, *sh;
@@ -626,21 +797,41 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     cudaMallocAsync(&part2, 2 * kRedBlocks * sizeof(double), s);
     cudaMemcpyAsync(rhos + 1, ones, sizeof(double), cudaMemcpyHostToDevice, s);
     c.dot<double>(n, r0, r, rhos);
+    // Seven launches per iteration (two SpMVs, three fused vector steps, two
+    // with their reductions' final step folded in); a chunk of ten
+    // iterations is captured once as a CUDA graph and replayed, and the
+    // host reads the residual after each chunk.
+    auto iteration = [&](int it) {
+      double* rho_cur = rhos + (it & 1);
+      double* rho_prev = rhos + ((it + 1) & 1);
+      k_bicg_p2<<<g, kThreads, 0, s>>>(n, rho_cur, rho_prev, alpha, omega, r, v, dinv, p, ph);
+      spmv(A, ph, v, s);
+      k_bicg_alpha<<<g, kThreads, 0, s>>>(n, r0, v, c.part, ticket, rho_cur, alpha);
+      k_bicg_s2<<<g, kThreads, 0, s>>>(n, alpha, r, v, dinv, ss, sh);
+      spmv(A, sh, t, s);
+      k_bicg_omega<<<g, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks, ticket, omega);
+      k_bicg_x_rho<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, r0, x, r, c.part, ticket,
+                                          rho_prev);   // rho of the next iteration
+    };
     const int chunk = 10;
+    cudaGraphExec_t gexec = nullptr;
+    {
+      cudaGraph_t graph;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        for (int k = 0; k < chunk; k++) iteration(k);   // chunks start at an even iteration
+        if (cudaStreamEndCapture(s, &graph) == cudaSuccess) {
+          if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+          cudaGraphDestroy(graph);
+        }
+      }
+      cudaGetLastError();
+    }
     while (bnorm > 0 && iters < max_iter) {
-      for (int k = 0; k < chunk && iters < max_iter; k++, iters++) {
-        double* rho_cur = rhos + (iters & 1);
-        double* rho_prev = rhos + ((iters + 1) & 1);
-        k_bicg_p2<<<g, kThreads, 0, s>>>(n, rho_cur, rho_prev, alpha, omega, r, v, dinv, p, ph);
-        spmv(A, ph, v, s);
-        k_dot_partial<double><<<g, kThreads, 0, s>>>(n, r0, v, c.part);
-        k_final_ratio<<<1, kThreads, 0, s>>>(c.part, g, rho_cur, alpha);
-        k_bicg_s2<<<g, kThreads, 0, s>>>(n, alpha, r, v, dinv, ss, sh);
-        spmv(A, sh, t, s);
-        k_dot2_partial<<<g, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks);
-        k_final_omega<<<1, kThreads, 0, s>>>(part2, part2 + kRedBlocks, g, omega);
-        k_bicg_x2<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, r0, x, r, c.part);
-        k_dot_final<<<1, kThreads, 0, s>>>(c.part, g, rho_prev);   // rho of the next iteration
+      if (gexec && max_iter - iters >= chunk) {
+        cudaGraphLaunch(gexec, s);
+        iters += chunk;
+      } else {
+        for (int k = 0; k < chunk && iters < max_iter; k++, iters++) iteration(iters);
       }
       c.dot<double>(n, r, r, rr);
       double hr = 0;
@@ -648,6 +839,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
       cudaStreamSynchronize(s);
       if (!(std::sqrt(hr) > rtol * bnorm) || !std::isfinite(hr)) break;
     }
+    if (gexec) cudaGraphExecDestroy(gexec);
     cudaFreeAsync(part2, s);
     cudaFreeAsync(r0, s); cudaFreeAsync(v, s); cudaFreeAsync(ss, s);
     cudaFreeAsync(t, s); cudaFreeAsync(ph, s); cudaFreeAsync(sh, s);
@@ -680,7 +872,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
       k_convert<double, float><<<g, kThreads, 0, s>>>(n, r, rf);
       cudaMemsetAsync(df, 0, n * sizeof(float), s);
       iters += pcg_core<float>(c, n, avg, A.ia, A.ja, af, rf, df, dinv, 0, nullptr, nullptr, 1e-4,
-                               max_iter - iters, dscal, zf, pf, qf, wf);
+                               max_iter - iters, dscal, zf, pf, qf, wf, ticket, true);
       k_add_to<<<g, kThreads, 0, s>>>(n, df, x);
     }
     cudaFreeAsync(wf, s);
@@ -701,7 +893,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
   res->converged = res->rel_residual <= rtol;
   cudaFreeAsync(r, s); cudaFreeAsync(z, s); cudaFreeAsync(p, s); cudaFreeAsync(q, s); cudaFreeAsync(ax, s);
-  cudaFreeAsync(dinv, s); cudaFreeAsync(c.part, s); cudaFreeAsync(dscal, s);
+  cudaFreeAsync(dinv, s); cudaFreeAsync(c.part, s); cudaFreeAsync(dscal, s); cudaFreeAsync(ticket, s);
   if (bptr) cudaFreeAsync(bptr, s);
   if (binv) cudaFreeAsync(binv, s);
   if (err == cudaSuccess) err = cudaGetLastError();
@@ -1004,8 +1196,11 @@ cudaError_t krylov_pcg_noalloc(const DevCsr& A, const double* b, double* x, doub
   double* ax = q + n;
   if (!use_x0) cudaMemsetAsync(x, 0, n * sizeof(double), s);
   k_diag_inv<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A.ia, A.ja, A.a, dinv);
+  // the reductions' ticket: a word of the fixed work space, zeroed here
+  unsigned* ticket = reinterpret_cast<unsigned*>(dscal + 15);
+  cudaMemsetAsync(ticket, 0, sizeof(unsigned), s);
   const int iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, 0, nullptr, nullptr, rtol, max_iter,
-                                     dscal, r, z, p, q);
+                                     dscal, r, z, p, q, ticket, false);
   // true residual
   const int g = grid_for(n);
   spmv_t<double>(n, avg, A.ia, A.ja, A.a, x, ax, s);
