@@ -126,3 +126,25 @@ def test_plain_solver_judges_and_replaces_a_bad_network(built):
         assert not b.learned_active()
         # once switched off, a method-5 step is a plain solve
         assert abs(its[-1] - np.mean(plain)) <= 20
+
+
+def test_exact_galerkin_correction_bounds_the_learned_gain(built):
+    """The learned network imitates a coarse solve on its grid; the exact
+    Galerkin correction P (P^T A P)^-1 P^T on that grid is the best any such
+    correction can do.  On the small C5 Newmark system (72,943 equations,
+    8 x 4 x 2 coarse cells) it cuts block-Jacobi flexible-CG iterations to a
+    1e-8 residual by less than 3x, so a learned coarse correction on this grid
+    cannot reach a 3x faster solve (oracle/galerkin_study.py, CPU, FP64)."""
+    import subprocess
+    import sys
+    import json
+    from conftest import REPO
+    r = subprocess.run([sys.executable, f"{REPO}/oracle/galerkin_study.py", "--size", "small", "--random", "0"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    s = res["solves"][0]
+    print(f"\nsmall C5: block-Jacobi {s['block_jacobi']} its, with the exact Galerkin correction "
+          f"{s['block_jacobi_galerkin']} its ({s['ratio']:.2f}x)")
+    assert max(s["residuals"]) <= 1.01e-8
+    assert 1.0 < s["ratio"] < 3.0
