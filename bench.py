@@ -227,7 +227,8 @@ def bench_quasi(args):
     loaded = None
     # each sample is a whole solve (0.3 to 2 s): at most 5 timed after 1 untimed
     steps, warmup = min(args.steps, IMPLICIT_MAX_STEPS), min(args.warmup, 1)
-    for method in (1, 0, 3, 2):
+    methods = [int(x) for x in args.c3_methods.split(",")]
+    for method in methods:
         with pdx.Model(cmd, device=0, precision=0) as m:
             sec, its, resid, wall = [], [], [], []
             for rep in range(warmup + steps):
@@ -247,9 +248,9 @@ def bench_quasi(args):
                                increment_wall_s=float(np.mean(wall)), iterations=float(np.mean(its)),
                                max_rel_residual=float(max(resid)))
             n_eq, nnz = m.info.n_eq, m.info.nnz
-    ref = u_end[1]
+    ref = u_end[methods[0]]
     for k in res:
-        res[k]["u_rel_diff_vs_block_jacobi"] = float(np.linalg.norm(u_end[k] - ref) / max(np.linalg.norm(ref), 1e-300))
+        res[k][f"u_rel_diff_vs_method_{methods[0]}"] = float(np.linalg.norm(u_end[k] - ref) / max(np.linalg.norm(ref), 1e-300))
     ia, ja, a, f = loaded
     cpu = None
     if not args.no_cpu_baseline:
@@ -274,7 +275,7 @@ def bench_quasi(args):
             "config": {"workload": f"c3: 2D quasi-static 401x401-node plate, PD band 30% of the width, 0.2 W "
                                    f"pre-crack, 1e-6 m top-edge pull, {n_eq} equations, nnz {nnz}",
                        "best_method": best["method"]},
-            "methods": [res[k] for k in (1, 0, 3, 2)], "cpu_baseline": cpu}
+            "methods": [res[k] for k in methods], "cpu_baseline": cpu}
     return line
 
 
@@ -401,6 +402,9 @@ def main():
                          "one launch; c3: quasi-static increments, Krylov methods beside a CPU direct solve; "
                          "c5: implicit Newmark, learned vs plain preconditioner")
     ap.add_argument("--specimens", type=int, default=256, help="c4: number of specimens")
+    ap.add_argument("--c3-methods", default="1,0,3,2",
+                    help="c3: Krylov methods to time, comma separated (0 PCG, 1 block-Jacobi PCG, 2 BiCGStab, "
+                         "3 mixed PCG + FP64 refinement, 6 GMRES)")
     ap.add_argument("--c5-size", default="full", choices=["full", "medium", "small"],
                     help="c5: 201x101x41 nodes (full), 101x51x21 (medium) or 61x31x13 (small)")
     ap.add_argument("--train-steps", type=int, default=20, help="c5: Newmark steps that collect training pairs")
