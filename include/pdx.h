@@ -57,17 +57,21 @@ typedef struct pdx_model_info {
 
 typedef struct pdx_solve_opts {
   int method;      /* 0 Jacobi PCG, 1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 mixed PCG + FP64 refinement,
-                      6 GMRES(30) (Jacobi) */
+                      6 GMRES(30) (Jacobi), 7 mixed BiCGStab + FP64 refinement (FP32 inner solves with
+                      an FP32 copy of the matrix; FP64 residuals and updates) */
   double rtol;     /* relative true residual ||b - A x|| / ||b|| */
   int max_iter;
   int use_x0;      /* 1: x holds the initial guess */
 } pdx_solve_opts;
 
 typedef struct pdx_solve_info {
-  int iterations;
+  int iterations;        /* summed over the requested method and its fallbacks */
   double rel_residual;   /* true FP64 residual ||b - A x|| / ||b|| */
   double seconds;        /* device time of the solve */
   int converged;
+  int method_used;       /* the method whose iterate was returned: the requested
+                            one, or 2 (BiCGStab) / 6 (GMRES) after a fallback */
+  int refinements;       /* methods 3 and 7: FP64 refinement steps (FP32 inner solves) */
 } pdx_solve_info;
 
 const char* pdx_last_error(void);
@@ -190,7 +194,7 @@ pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, co
  * K_N = beta dt^2 K + M assembled on the GPU (pdfemAssembleKNFR_CSRformat
  * :6327-6397), K_N a = F solved by `method`, update (updateDispVelo
  * :6399-6422).  The reference factorises K_N with PARDISO at every step.
- * method: 0-3 and 6 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
+ * method: 0-3, 6 and 7 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
  * method); 5 flexible CG with block-Jacobi plus the learned coarse correction,
  * falling back to 4 and then BiCGStab when it stalls.  collect = 1 (method 4)
  * stores one training pair per iteration of the solve.  info: iterations,

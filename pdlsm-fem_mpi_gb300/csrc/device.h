@@ -237,6 +237,8 @@ struct KrylovResult {
   int iterations = 0;
   double rel_residual = 0;
   int converged = 0;
+  int method = -1;        // the method that produced the iterate
+  int refinements = 0;    // method 3: FP64 refinement steps
 };
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
                          int block_dim, cudaStream_t s, KrylovResult* res);

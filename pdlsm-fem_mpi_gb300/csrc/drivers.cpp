@@ -112,12 +112,15 @@ pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int met
   cudaError_t e = krylov_solve(A, b, x, method, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
   pdx_status st = cuda_check(e, "Krylov solve");
   if (st) return st;
+  int spent = kr->iterations;   // iterations are summed over the fallbacks
   if (!kr->converged) {
     // BiCGStab as the fallback of a stalled CG on the unsymmetric stiffness
     if (method != 2 && method != 6) {
       e = krylov_solve(A, b, x, 2, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
       st = cuda_check(e, "Krylov solve");
       if (st) return st;
+      kr->iterations += spent;
+      spent = kr->iterations;
     }
     if (!kr->converged && method != 6) {
       // GMRES(30) when BiCGStab does not converge: once a crack has cut a
@@ -129,6 +132,7 @@ pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int met
       e = krylov_solve(A, b, x, 6, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
       st = cuda_check(e, "Krylov solve");
       if (st) return st;
+      kr->iterations += spent;
     }
     if (!kr->converged)
       return set_error(PDX_ERR_NOCONV, "Krylov solve stopped at relative residual " + std::to_string(kr->rel_residual));
@@ -397,7 +401,8 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   if (!m) return set_error(PDX_ERR_INVALID, "null model");
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
-  if (method < 0 || (method > 3 && method != 6)) return set_error(PDX_ERR_INVALID, "method must be 0..3 or 6");
+  if (method < 0 || (method > 3 && method < 6) || method > 7)
+    return set_error(PDX_ERR_INVALID, "method must be 0..3, 6 or 7");
   if (m->cmd.fail_flag == 1)
     return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   cudaSetDevice(m->device);
@@ -405,12 +410,7 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   float ms = 0.f;
   pdx_status st = quasi_increment(m, (int)m->steps_done + 1, method, &kr, &ms);
   if (!st) st = rf_record(m, m->steps_done);
-  if (info) {
-    info->iterations = kr.iterations;
-    info->rel_residual = kr.rel_residual;
-    info->seconds = ms * 1e-3;
-    info->converged = kr.converged;
-  }
+  fill_solve_info(info, kr, ms * 1e-3);
   if (st) return st;
   st = quasi_advance(m);
   if (st) return st;

@@ -6,15 +6,28 @@
 //   method 1  PCG, block-Jacobi (the d x d diagonal block of every node)
 //   method 2  BiCGStab, Jacobi (K is unsymmetric: family k's row uses A_k and
 //             delta_k while row m uses A_m and delta_m)
-//   method 3  PCG in FP32 (FP32 matrix copy and vectors) inside FP64 iterative
-//             refinement: r = b - A x in FP64, A d ~= r in FP32, x += d
+//   method 3  block-Jacobi PCG in FP32 (FP32 matrix copy and vectors) inside
+//             FP64 iterative refinement: r = b - A x in FP64, A d ~= r in FP32,
+//             x += d
 //   method 6  GMRES(30), right Jacobi (the fallback once BiCGStab diverges)
+//   method 7  BiCGStab in FP32 inside the same FP64 iterative refinement (the
+//             mixed-precision solve for the unsymmetric stiffness, on which
+//             CG stalls)
 //
 // Convergence is always judged on the true FP64 residual ||b - A x|| / ||b||.
 // Scalars stay on the device; iterations are launched in chunks and the host
 // reads the residual once per chunk.  Reductions are two-pass (per-block
 // partials then one block) so results are bitwise reproducible.
+//
+// GB300 runs FP64 arithmetic (and float<->double conversion) at 2 lanes per
+// clock per SM against about 128 for FP32, so in the FP64 methods the
+// arithmetic of the mat-vec and the vector steps, not memory, is the limit:
+// every scalar ratio (alpha, beta) is formed once, by the last block of the
+// reduction that produces it, and not per thread; the FP32 inner solve of
+// method 3 does its element arithmetic in FP32 and converts only its block
+// partials to FP64.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -27,6 +40,7 @@ namespace {
 
 constexpr int kRedBlocks = 1024;
 constexpr int kCgStallIts = 400;
+constexpr double kInnerTol = 1e-4;   // relative residual of the FP32 inner solves (methods 3, 7)
 constexpr int kThreads = 256;
 
 template <typename T, int L>
@@ -45,32 +59,41 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, const int64_t* __restri
   if (row < n && lane == 0) y[row] = s;
 }
 
+// Sum over the block, returned to every thread: warp shuffles (xor tree),
+// then thread 0 adds the warp sums in warp order.  Two barriers instead of
+// the eight of a shared-memory tree; the extra FP64 adds of the shuffle
+// levels cost less than the barriers (a dot product with its final step:
+// 5.0 against 5.7 us on the GB300).  sh: at least 33 words.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+    sh[32] = t;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
 template <typename T>
 __global__ void k_dot_partial(int64_t n, const T* x, const T* y, double* part) {
   __shared__ double sh[kThreads];
   double s = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     s += (double)x[i] * (double)y[i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
 __global__ void k_dot_final(const double* part, int np, double* out) {
   __shared__ double sh[kThreads];
   double s = 0;
   for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *out = sh[0];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = s;
 }
 
 // inverse of the diagonal blocks; blocks given by bptr (rows [bptr[i], bptr[i+1]))
@@ -123,30 +146,19 @@ __global__ void k_apply_block(int64_t nb, const int64_t* bptr, const double* bin
   }
 }
 
-// x += alpha p ; r -= alpha q   with alpha = num/den from device scalars
+// p = z + beta p, beta = rz_new / rz_old set by the last block of the
+// reduction that summed rz_new
 template <typename T>
-__global__ void k_cg_update(int64_t n, const double* num, const double* den, const T* p, const T* q, T* x, T* r) {
-  const double alpha = *den != 0.0 ? *num / *den : 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    r[i] = (T)((double)r[i] - alpha * (double)q[i]);
-  }
+__global__ void k_cg_dir(int64_t n, const T* beta, const T* z, T* p) {
+  const T b = *beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + b * p[i];
 }
 
-// p = z + (rz_new / rz_old) p ; rz_old = rz_new (last block thread 0 copies after all)
 template <typename T>
-__global__ void k_cg_dir(int64_t n, const double* rz_new, const double* rz_old, const T* z, T* p) {
-  const double beta = *rz_old != 0.0 ? *rz_new / *rz_old : 0.0;
+__global__ void k_jacobi(int64_t n, const T* dinv, const T* r, T* z) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = (T)((double)z[i] + beta * (double)p[i]);
-}
-
-__global__ void k_copy_scalar(const double* src, double* dst) { *dst = *src; }
-
-template <typename T>
-__global__ void k_jacobi(int64_t n, const double* dinv, const T* r, T* z) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    z[i] = (T)(dinv[i] * (double)r[i]);
+    z[i] = dinv[i] * r[i];
 }
 
 __global__ void k_diag_inv(int64_t n, const int64_t* ia, const int* ja, const double* a, double* dinv) {
@@ -175,114 +187,30 @@ __global__ void k_sub(int64_t n, const T* b, const T* q, T* r) {
     r[i] = b[i] - q[i];
 }
 
-__global__ void k_add_to(int64_t n, const float* d, double* x) {
+// x += sign d
+__global__ void k_add_to(int64_t n, const float* d, double sign, double* x) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] += (double)d[i];
+    x[i] += sign * (double)d[i];
 }
 
 // Fused BiCGStab steps.  The dot products keep the fixed order of
-// k_dot_partial / k_dot_final (grid-stride partial sums, one block tree,
-// one final block), so the fused solve gives the same bits as separate
-// kernels; scalars stay on the device.
+// k_dot_partial / k_dot_final (grid-stride partial sums over red_grid
+// blocks, block_sum, one final block), so the fused solve gives the same
+// bits as separate kernels; scalars stay on the device.
 
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-  sh[threadIdx.x] = v;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  const double r = sh[0];
-  __syncthreads();
-  return r;
-}
 
-// p = r + beta (p - omega v), beta = (rho / rho_prev)(alpha / omega); ph = D^-1 p
-__global__ void k_bicg_p2(int64_t n, const double* rho, const double* rho_prev, const double* alpha,
-                          const double* omega, const double* r, const double* v, const double* dinv, double* p,
-                          double* ph) {
-  const double beta = (*rho / *rho_prev) * (*alpha / *omega);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double pi = r[i] + beta * (p[i] - *omega * v[i]);
-    p[i] = pi;
-    ph[i] = dinv[i] * pi;
-  }
-}
-
-// *out = num / (sum of the partials), 0 if the sum is 0
-__global__ void k_final_ratio(const double* part, int np, const double* num, double* out) {
-  __shared__ double sh[kThreads];
-  double s = 0;
-  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
-  const double d = block_sum(s, sh);
-  if (threadIdx.x == 0) *out = d != 0.0 ? *num / d : 0.0;
-}
-
-// s = r - alpha v; sh = D^-1 s
-__global__ void k_bicg_s2(int64_t n, const double* alpha, const double* r, const double* v, const double* dinv,
-                          double* s, double* sh) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double si = r[i] - *alpha * v[i];
-    s[i] = si;
-    sh[i] = dinv[i] * si;
-  }
-}
-
-// per-block partials of t.s and t.t
-__global__ void k_dot2_partial(int64_t n, const double* t, const double* s, double* part_ts, double* part_tt) {
-  __shared__ double sh[kThreads];
-  double a = 0, b = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    a += t[i] * s[i];
-    b += t[i] * t[i];
-  }
-  a = block_sum(a, sh);
-  b = block_sum(b, sh);
-  if (threadIdx.x == 0) {
-    part_ts[blockIdx.x] = a;
-    part_tt[blockIdx.x] = b;
-  }
-}
-
-// omega = (t.s) / (t.t), 0 if t.t is 0
-__global__ void k_final_omega(const double* part_ts, const double* part_tt, int np, double* omega) {
-  __shared__ double sh[kThreads];
-  double a = 0, b = 0;
-  for (int i = threadIdx.x; i < np; i += blockDim.x) {
-    a += part_ts[i];
-    b += part_tt[i];
-  }
-  a = block_sum(a, sh);
-  b = block_sum(b, sh);
-  if (threadIdx.x == 0) *omega = b != 0.0 ? a / b : 0.0;
-}
-
-// x += alpha ph + omega sh; r = s - omega t; per-block partials of r0 . r (the next rho)
-__global__ void k_bicg_x2(int64_t n, const double* alpha, const double* omega, const double* ph, const double* shat,
-                          const double* s, const double* t, const double* r0, double* x, double* r, double* part) {
-  __shared__ double sh[kThreads];
-  double acc = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += *alpha * ph[i] + *omega * shat[i];
-    const double ri = s[i] - *omega * t[i];
-    r[i] = ri;
-    acc += r0[i] * ri;
-  }
-  acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
-}
-
-// The same three reductions with their final step folded in: every block
-// writes its partial, and the block that finishes last (an atomic ticket
-// after a memory fence) adds the partials in block order exactly as
-// k_dot_final / k_final_ratio / k_final_omega do, so the bits do not change
-// and three single-block launches per iteration disappear.  The ticket is
-// reset by that last block for the next use.
+// The reductions with their final step folded in: every block writes its
+// partial, and the block that finishes last (thread 0 fences its partial,
+// then takes an atomic ticket) adds the partials in block order exactly as
+// k_dot_final does, so the bits do not change and a single-block launch per
+// reduction disappears.  The ticket is reset by that last block for the next
+// use.
 __device__ __forceinline__ bool last_block(unsigned* ticket) {
   __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
   __syncthreads();
   return last;
 }
@@ -293,117 +221,232 @@ __device__ __forceinline__ double sum_partials(const double* part, int np, doubl
   return block_sum(s, sh);
 }
 
+// Reductions in the precision T of the vectors.  FP64: the block tree of
+// block_sum.  FP32: the products are summed in FP32 within a thread and a
+// block (warp shuffles), and only the block partials are widened to FP64 for
+// the final sum, so no FP64 arithmetic runs per element.
+__device__ __forceinline__ double block_total(double v, double* sh) { return block_sum(v, sh); }
+__device__ __forceinline__ float block_total(float v, double* shd) {
+  float* sh = reinterpret_cast<float*>(shd);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  __syncthreads();
+  return t;   // valid in thread 0
+}
+
+// the block's partial, stored in T (part viewed as T*)
+template <typename T>
+__device__ __forceinline__ void put_partial(double* part, T v) {
+  if (threadIdx.x == 0) reinterpret_cast<T*>(part)[blockIdx.x] = v;
+}
+
+template <typename T>
+__device__ __forceinline__ double sum_partials_t(const double* part, int np, double* sh) {
+  const T* pt = reinterpret_cast<const T*>(part);
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += (double)__ldcg(pt + i);
+  return block_sum(s, sh);
+}
+
+// BiCGStab scalars: FP64 masters (rho, alpha, omega, beta) formed by the
+// last blocks, and their copies in T that the element loops read (the same
+// words when T is double).
+template <typename T>
+struct BicgScalars {
+  double* alpha;
+  double* omega;
+  double* beta;
+  T* alpha_t;
+  T* omega_t;
+  T* beta_t;
+};
+
+// starting scalars: alpha = omega = rho_prev = 1
+__global__ void k_bicg_start(double* alpha, double* omega, double* rho_prev) {
+  *alpha = 1.0;
+  *omega = 1.0;
+  *rho_prev = 1.0;
+}
+
+// beta of the first iteration, (rho / rho_prev)(alpha / omega) with the
+// starting values; later ones are set by k_bicg_x_rho
+template <typename T>
+__global__ void k_bicg_beta0(const double* rho, const double* rho_prev, BicgScalars<T> c) {
+  const double b = (*rho / *rho_prev) * (*c.alpha / *c.omega);
+  *c.beta = b;
+  *c.beta_t = (T)b;
+  *c.alpha_t = (T)*c.alpha;
+  *c.omega_t = (T)*c.omega;
+}
+
+// p = r + beta (p - omega v); ph = D^-1 p
+template <typename T>
+__global__ void k_bicg_p2(int64_t n, const T* beta_p, const T* omega_p, const T* r, const T* v, const T* dinv, T* p,
+                          T* ph) {
+  const T beta = *beta_p, omega = *omega_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T pi = r[i] + beta * (p[i] - omega * v[i]);
+    p[i] = pi;
+    ph[i] = dinv[i] * pi;
+  }
+}
+
+// s = r - alpha v; sh = D^-1 s
+template <typename T>
+__global__ void k_bicg_s2(int64_t n, const T* alpha_p, const T* r, const T* v, const T* dinv, T* s, T* sh) {
+  const T alpha = *alpha_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T si = r[i] - alpha * v[i];
+    s[i] = si;
+    sh[i] = dinv[i] * si;
+  }
+}
+
 // partials of r0 . v; the last block sets alpha = rho / (r0 . v) (0 if the dot is 0)
-__global__ void k_bicg_alpha(int64_t n, const double* r0, const double* v, double* part, unsigned* ticket,
-                             const double* rho, double* alpha) {
+template <typename T>
+__global__ void k_bicg_alpha(int64_t n, const T* r0, const T* v, double* part, unsigned* ticket, const double* rho,
+                             BicgScalars<T> c) {
   __shared__ double sh[kThreads];
-  double acc = 0;
+  T acc = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     acc += r0[i] * v[i];
-  acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  put_partial<T>(part, block_total(acc, sh));
   if (!last_block(ticket)) return;
-  const double d = sum_partials(part, gridDim.x, sh);
+  const double d = sum_partials_t<T>(part, gridDim.x, sh);
   if (threadIdx.x == 0) {
-    *alpha = d != 0.0 ? *rho / d : 0.0;
+    const double a = d != 0.0 ? *rho / d : 0.0;
+    *c.alpha = a;
+    *c.alpha_t = (T)a;
     *ticket = 0;
   }
 }
 
 // partials of t.s and t.t; the last block sets omega = (t.s) / (t.t) (0 if t.t is 0)
-__global__ void k_bicg_omega(int64_t n, const double* t, const double* s, double* part_ts, double* part_tt,
-                             unsigned* ticket, double* omega) {
+template <typename T>
+__global__ void k_bicg_omega(int64_t n, const T* t, const T* s, double* part_ts, double* part_tt, unsigned* ticket,
+                             BicgScalars<T> c) {
   __shared__ double sh[kThreads];
-  double a = 0, b = 0;
+  T a = 0, b = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     a += t[i] * s[i];
     b += t[i] * t[i];
   }
-  a = block_sum(a, sh);
-  b = block_sum(b, sh);
-  if (threadIdx.x == 0) {
-    part_ts[blockIdx.x] = a;
-    part_tt[blockIdx.x] = b;
-  }
+  put_partial<T>(part_ts, block_total(a, sh));
+  put_partial<T>(part_tt, block_total(b, sh));
   if (!last_block(ticket)) return;
-  double sa = 0, sb = 0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-    sa += __ldcg(part_ts + i);
-    sb += __ldcg(part_tt + i);
-  }
-  sa = block_sum(sa, sh);
-  sb = block_sum(sb, sh);
+  const double sa = sum_partials_t<T>(part_ts, gridDim.x, sh);
+  const double sb = sum_partials_t<T>(part_tt, gridDim.x, sh);
   if (threadIdx.x == 0) {
-    *omega = sb != 0.0 ? sa / sb : 0.0;
+    const double o = sb != 0.0 ? sa / sb : 0.0;
+    *c.omega = o;
+    *c.omega_t = (T)o;
     *ticket = 0;
   }
 }
 
-// x += alpha ph + omega sh; r = s - omega t; the last block sets rho_next = r0 . r
-__global__ void k_bicg_x_rho(int64_t n, const double* alpha, const double* omega, const double* ph,
-                             const double* shat, const double* s, const double* t, const double* r0, double* x,
-                             double* r, double* part, unsigned* ticket, double* rho_next) {
+// x += alpha ph + omega sh; r = s - omega t; the last block sets rho_next =
+// r0 . r and the next iteration's beta = (rho_next / rho)(alpha / omega)
+template <typename T>
+__global__ void k_bicg_x_rho(int64_t n, const T* ph, const T* shat, const T* s, const T* t, const T* r0, T* x, T* r,
+                             double* part, unsigned* ticket, const double* rho, double* rho_next, BicgScalars<T> c) {
   __shared__ double sh[kThreads];
-  double acc = 0;
+  const T alpha = *c.alpha_t, omega = *c.omega_t;
+  T acc = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += *alpha * ph[i] + *omega * shat[i];
-    const double ri = s[i] - *omega * t[i];
+    x[i] += alpha * ph[i] + omega * shat[i];
+    const T ri = s[i] - omega * t[i];
     r[i] = ri;
     acc += r0[i] * ri;
   }
-  acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  put_partial<T>(part, block_total(acc, sh));
   if (!last_block(ticket)) return;
-  const double d = sum_partials(part, gridDim.x, sh);
+  const double d = sum_partials_t<T>(part, gridDim.x, sh);
   if (threadIdx.x == 0) {
     *rho_next = d;
+    const double b = (d / *rho) * (*c.alpha / *c.omega);
+    *c.beta = b;
+    *c.beta_t = (T)b;
     *ticket = 0;
   }
 }
 
-// Fused PCG steps (precision T of the vectors, FP64 scalars and sums).
-// partials of p.q; the last block stores the sum
+// Fused PCG steps in the precision T of the vectors (reductions as above).
+// partials of p.q; the last block sets alpha = rz / (p.q) (0 if p.q is 0)
 template <typename T>
-__global__ void k_cg_pq(int64_t n, const T* p, const T* q, double* part, unsigned* ticket, double* out) {
+__global__ void k_cg_pq(int64_t n, const T* p, const T* q, double* part, unsigned* ticket, const double* rz,
+                        T* alpha) {
   __shared__ double sh[kThreads];
-  double acc = 0;
+  T acc = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    acc += (double)p[i] * (double)q[i];
-  acc = block_sum(acc, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+    acc += p[i] * q[i];
+  put_partial<T>(part, block_total(acc, sh));
   if (!last_block(ticket)) return;
-  const double d = sum_partials(part, gridDim.x, sh);
+  const double d = sum_partials_t<T>(part, gridDim.x, sh);
   if (threadIdx.x == 0) {
-    *out = d;
+    *alpha = (T)(d != 0.0 ? *rz / d : 0.0);
     *ticket = 0;
   }
 }
 
-// x += alpha p; r -= alpha q (alpha = rz / pq); with dinv also z = D^-1 r and
-// the partials of r.z, the last block storing rz_new
+// x += alpha p; r -= alpha q; with dinv also z = D^-1 r and the partials of
+// r.z, the last block storing rz_new and beta = rz_new / rz (0 if rz is 0)
 template <typename T>
-__global__ void k_cg_update_jacobi(int64_t n, const double* rz, const double* pq, const T* p, const T* q, T* x,
-                                   T* r, const double* dinv, T* z, double* part, unsigned* ticket, double* rz_new) {
+__global__ void k_cg_update_jacobi(int64_t n, const T* alpha_p, const T* p, const T* q, T* x, T* r, const T* dinv,
+                                   T* z, double* part, unsigned* ticket, const double* rz, double* rz_new, T* beta) {
   __shared__ double sh[kThreads];
-  const double alpha = *pq != 0.0 ? *rz / *pq : 0.0;
-  double acc = 0;
+  const T alpha = *alpha_p;
+  T acc = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    const T ri = (T)((double)r[i] - alpha * (double)q[i]);
+    x[i] = x[i] + alpha * p[i];
+    const T ri = r[i] - alpha * q[i];
     r[i] = ri;
     if (dinv) {
-      const T zi = (T)(dinv[i] * (double)ri);
+      const T zi = dinv[i] * ri;
       z[i] = zi;
-      acc += (double)ri * (double)zi;
+      acc += ri * zi;
     }
   }
   if (!dinv) return;
+  put_partial<T>(part, block_total(acc, sh));
+  if (!last_block(ticket)) return;
+  const double d = sum_partials_t<T>(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *rz_new = d;
+    *beta = (T)(*rz != 0.0 ? d / *rz : 0.0);
+    *ticket = 0;
+  }
+}
+
+// block-Jacobi z = B^-1 r over the node blocks and the partials of r.z; the
+// last block stores rz_new and beta = rz_new / rz (0 if rz is 0)
+template <typename T>
+__global__ void k_cg_block_rz(int64_t nb, const int64_t* bptr, const double* binv, const T* r, T* z, double* part,
+                              unsigned* ticket, const double* rz, double* rz_new, T* beta) {
+  __shared__ double sh[kThreads];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = bptr[i];
+    const int s = (int)(bptr[i + 1] - r0);
+    double v[3] = {0, 0, 0};
+    for (int c = 0; c < s; c++) v[c] = (double)r[r0 + c];
+    for (int rr = 0; rr < s; rr++) {
+      double zi = 0;
+      for (int c = 0; c < s; c++) zi += binv[i * 9 + rr * 3 + c] * v[c];
+      z[r0 + rr] = (T)zi;
+      acc += v[rr] * (double)(T)zi;
+    }
+  }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
   if (!last_block(ticket)) return;
   const double d = sum_partials(part, gridDim.x, sh);
   if (threadIdx.x == 0) {
     *rz_new = d;
+    *beta = (T)(*rz != 0.0 ? d / *rz : 0.0);
     *ticket = 0;
   }
 }
@@ -486,13 +529,19 @@ struct Work {
 };
 
 int grid_for(int64_t n) { return (int)std::min<int64_t>((n + kThreads - 1) / kThreads, kRedBlocks); }
+// Blocks of the reductions (dot products, and the vector steps that end in
+// one): two per SM, so the last block adds few partials.  On the 320k-row
+// plate system a dot product with its final step folded in took 5.0 us with
+// 304 blocks and 7.6 us with 1024; plain vector steps keep grid_for.
+constexpr int kRedGrid = 304;
+int red_grid(int64_t n) { return (int)std::min<int64_t>((n + kThreads - 1) / kThreads, kRedGrid); }
 
 struct Ctx {
   cudaStream_t s;
   double* part;   // kRedBlocks
   template <typename T>
   void dot(int64_t n, const T* x, const T* y, double* out) {
-    const int g = grid_for(n);
+    const int g = red_grid(n);
     k_dot_partial<T><<<g, kThreads, 0, s>>>(n, x, y, part);
     k_dot_final<<<1, kThreads, 0, s>>>(part, g, out);
   }
@@ -521,14 +570,15 @@ template <typename T>
 // graphs: replay chunks of iterations as a CUDA graph (off where nothing
 // may be allocated).
 int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, const T* aT, const T* b, T* x,
-             const double* dinv, int64_t nb, const int64_t* bptr, const double* binv, double rtol, int max_iter,
+             const T* dinv, int64_t nb, const int64_t* bptr, const double* binv, double rtol, int max_iter,
              double* dscal, T* r, T* z, T* p, T* q, unsigned* ticket, bool graphs) {
   cudaStream_t s = c.s;
   double* rz = dscal + 0;
   double* rz_new = dscal + 1;
-  double* pq = dscal + 2;
   double* bb = dscal + 3;
   double* rr = dscal + 4;
+  T* alpha = reinterpret_cast<T*>(dscal + 5);   // set by k_cg_pq
+  T* beta = reinterpret_cast<T*>(dscal + 6);    // set with rz_new
   const int g = grid_for(n);
   spmv_t<T>(n, avg, ia, ja, aT, x, q, s);
   k_sub<T><<<g, kThreads, 0, s>>>(n, b, q, r);
@@ -556,22 +606,27 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
   double best = INFINITY;
   int best_it = 0;
   // r.z of the iteration and of the one before in two slots (rz, rz_new by
-  // parity, no copy); the reductions' final step runs in their last block;
-  // with Jacobi the preconditioner and r.z are fused into the update (four
-  // launches per iteration); chunks of ten iterations replay a CUDA graph
+  // parity, no copy); the reductions' final step, with the ratio alpha or
+  // beta, runs in their last block; the preconditioner and r.z are fused
+  // into the update (Jacobi) or into one block-Jacobi kernel: four launches
+  // per iteration, five with block-Jacobi; chunks of ten iterations replay a
+  // CUDA graph
+  const int gb = binv ? red_grid(nb) : 0;
+  const int gr = red_grid(n);
   auto iteration = [&](int k) {
     double* rz_cur = (k & 1) ? rz_new : rz;
     double* rz_next = (k & 1) ? rz : rz_new;
     spmv_t<T>(n, avg, ia, ja, aT, p, q, s);
-    k_cg_pq<T><<<g, kThreads, 0, s>>>(n, p, q, c.part, ticket, pq);
+    k_cg_pq<T><<<gr, kThreads, 0, s>>>(n, p, q, c.part, ticket, rz_cur, alpha);
     if (binv) {
-      k_cg_update_jacobi<T><<<g, kThreads, 0, s>>>(n, rz_cur, pq, p, q, x, r, nullptr, z, c.part, ticket, rz_next);
-      precond(r, z);
-      c.dot<T>(n, r, z, rz_next);
+      k_cg_update_jacobi<T><<<g, kThreads, 0, s>>>(n, alpha, p, q, x, r, nullptr, z, c.part, ticket, rz_cur,
+                                                   rz_next, beta);
+      k_cg_block_rz<T><<<gb, kThreads, 0, s>>>(nb, bptr, binv, r, z, c.part, ticket, rz_cur, rz_next, beta);
     } else {
-      k_cg_update_jacobi<T><<<g, kThreads, 0, s>>>(n, rz_cur, pq, p, q, x, r, dinv, z, c.part, ticket, rz_next);
+      k_cg_update_jacobi<T><<<gr, kThreads, 0, s>>>(n, alpha, p, q, x, r, dinv, z, c.part, ticket, rz_cur,
+                                                    rz_next, beta);
     }
-    k_cg_dir<T><<<g, kThreads, 0, s>>>(n, rz_next, rz_cur, z, p);
+    k_cg_dir<T><<<g, kThreads, 0, s>>>(n, beta, z, p);
   };
   cudaGraphExec_t gexec = nullptr;
   if (graphs) {
@@ -608,6 +663,103 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
   }
   if (gexec) cudaGraphExecDestroy(gexec);
   return it;
+}
+
+// BiCGStab with right Jacobi preconditioning in precision T on (ia, ja, aT),
+// from the iterate x (in T).  Stops when the recursive residual is at most
+// rtol ||b|| (read after each chunk of ten iterations), on a non-finite
+// residual, at max_iter, or (stall > 0) once the residual has not halved for
+// `stall` iterations.  Seven launches per iteration: two SpMVs and three
+// fused vector steps, two of them with their reductions' final step folded
+// in; a chunk of ten iterations is captured once as a CUDA graph and
+// replayed.  w: eight work vectors of n (w[0] the residual r, w[3] the
+// direction p); part2: 2 kRedBlocks words.  Returns iterations.
+template <typename T>
+int bicg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, const T* aT, const T* b, T* x,
+              const T* dinv, double rtol, int max_iter, int stall, double* dscal, T* const w[8], double* part2,
+              unsigned* ticket) {
+  cudaStream_t s = c.s;
+  T *r = w[0], *r0 = w[1], *v = w[2], *p = w[3], *ss = w[4], *t = w[5], *ph = w[6], *sh = w[7];
+  const int g = grid_for(n);
+  const int gr = red_grid(n);
+  BicgScalars<T> sc;
+  sc.alpha = dscal + 2;
+  sc.omega = dscal + 3;
+  sc.beta = dscal + 14;
+  if constexpr (std::is_same<T, double>::value) {
+    sc.alpha_t = sc.alpha;
+    sc.omega_t = sc.omega;
+    sc.beta_t = sc.beta;
+  } else {
+    sc.alpha_t = reinterpret_cast<T*>(dscal + 4);
+    sc.omega_t = sc.alpha_t + 1;
+    sc.beta_t = reinterpret_cast<T*>(dscal + 5);
+  }
+  double* bb = dscal + 6;
+  double* rr = dscal + 7;
+  double* rhos = dscal + 12;   // rho of the iteration and of the one before, by parity
+  spmv_t<T>(n, avg, ia, ja, aT, x, v, s);   // v holds A x for the moment
+  k_sub<T><<<g, kThreads, 0, s>>>(n, b, v, r);
+  cudaMemcpyAsync(r0, r, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(v, 0, n * sizeof(T), s);
+  cudaMemsetAsync(p, 0, n * sizeof(T), s);
+  k_bicg_start<<<1, 1, 0, s>>>(sc.alpha, sc.omega, rhos + 1);
+  c.dot<T>(n, b, b, bb);
+  c.dot<T>(n, r0, r, rhos);
+  k_bicg_beta0<T><<<1, 1, 0, s>>>(rhos, rhos + 1, sc);
+  double hb = 0;
+  cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const double bnorm = std::sqrt(hb);
+  auto iteration = [&](int it) {
+    double* rho_cur = rhos + (it & 1);
+    double* rho_next = rhos + ((it + 1) & 1);
+    k_bicg_p2<T><<<g, kThreads, 0, s>>>(n, sc.beta_t, sc.omega_t, r, v, dinv, p, ph);
+    spmv_t<T>(n, avg, ia, ja, aT, ph, v, s);
+    k_bicg_alpha<T><<<gr, kThreads, 0, s>>>(n, r0, v, c.part, ticket, rho_cur, sc);
+    k_bicg_s2<T><<<g, kThreads, 0, s>>>(n, sc.alpha_t, r, v, dinv, ss, sh);
+    spmv_t<T>(n, avg, ia, ja, aT, sh, t, s);
+    k_bicg_omega<T><<<gr, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks, ticket, sc);
+    k_bicg_x_rho<T><<<gr, kThreads, 0, s>>>(n, ph, sh, ss, t, r0, x, r, c.part, ticket, rho_cur, rho_next, sc);
+  };
+  const int chunk = 10;
+  cudaGraphExec_t gexec = nullptr;
+  {
+    cudaGraph_t graph;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (int k = 0; k < chunk; k++) iteration(k);   // chunks start at an even iteration
+      if (cudaStreamEndCapture(s, &graph) == cudaSuccess) {
+        if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+        cudaGraphDestroy(graph);
+      }
+    }
+    cudaGetLastError();
+  }
+  int iters = 0;
+  double best = INFINITY;
+  int best_it = 0;
+  while (bnorm > 0 && iters < max_iter) {
+    if (gexec && max_iter - iters >= chunk) {
+      cudaGraphLaunch(gexec, s);
+      iters += chunk;
+    } else {
+      for (int k = 0; k < chunk && iters < max_iter; k++, iters++) iteration(iters);
+    }
+    c.dot<T>(n, r, r, rr);
+    double hr = 0;
+    cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const double rn = std::sqrt(hr);
+    if (!(rn > rtol * bnorm) || !std::isfinite(hr)) break;
+    if (rn < 0.5 * best) {
+      best = rn;
+      best_it = iters;
+    } else if (stall > 0 && iters - best_it >= stall) {
+      break;
+    }
+  }
+  if (gexec) cudaGraphExecDestroy(gexec);
+  return iters;
 }
 
 // GMRES(kGmresRestart) with right Jacobi preconditioning, A (D^-1 y) = b,
@@ -744,7 +896,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   int64_t nb = 0;
   int64_t* bptr = nullptr;
   double* binv = nullptr;
-  if (method == 1) {
+  if (method == 1 || method == 3) {
     const int bd = block_dim > 0 ? block_dim : 3;
     nb = (n + bd - 1) / bd;
     std::vector<int64_t> hp(nb + 1);
@@ -763,97 +915,34 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   cudaMallocAsync(&ax, n * sizeof(double), s);
   const int g = grid_for(n);
   int iters = 0;
+  int outer_steps = 0;
   if (method == 0 || method == 1) {
     iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, nb, bptr, binv, rtol, max_iter, dscal, r, z,
                              p, q, ticket, true);
   } else if (method == 2) {
-    // BiCGStab, right Jacobi preconditioning
-    double *r0, *v, *ss, *t, *ph, *sh;
-    cudaMallocAsync(&r0, n * sizeof(double), s);
-    cudaMallocAsync(&v, n * sizeof(double), s);
-    cudaMallocAsync(&ss, n * sizeof(double), s);
-    cudaMallocAsync(&t, n * sizeof(double), s);
-    cudaMallocAsync(&ph, n * sizeof(double), s);
-    cudaMallocAsync(&sh, n * sizeof(double), s);
-    double* alpha = dscal + 2;
-    double* omega = dscal + 3;
-    double* bb = dscal + 6;
-    double* rr = dscal + 7;
-    spmv(A, x, ax, s);
-    k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
-    cudaMemcpyAsync(r0, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    cudaMemsetAsync(v, 0, n * sizeof(double), s);
-    cudaMemsetAsync(p, 0, n * sizeof(double), s);
-    const double ones[4] = {1.0, 1.0, 1.0, 1.0};
-    cudaMemcpyAsync(dscal, ones, 4 * sizeof(double), cudaMemcpyHostToDevice, s);
-    c.dot<double>(n, b, b, bb);
-    double hb = 0;
-    cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    const double bnorm = std::sqrt(hb);
-    // rho of the iteration and of the one before in two slots (no copies)
-    double* rhos = dscal + 12;
+    // BiCGStab, right Jacobi preconditioning, from the caller's x
+    double* w[8] = {r, nullptr, nullptr, p, nullptr, nullptr, nullptr, nullptr};
+    for (int k : {1, 2, 4, 5, 6, 7}) cudaMallocAsync(&w[k], n * sizeof(double), s);
     double* part2 = nullptr;
     cudaMallocAsync(&part2, 2 * kRedBlocks * sizeof(double), s);
-    cudaMemcpyAsync(rhos + 1, ones, sizeof(double), cudaMemcpyHostToDevice, s);
-    c.dot<double>(n, r0, r, rhos);
-    // Seven launches per iteration (two SpMVs, three fused vector steps, two
-    // with their reductions' final step folded in); a chunk of ten
-    // iterations is captured once as a CUDA graph and replayed, and the
-    // host reads the residual after each chunk.
-    auto iteration = [&](int it) {
-      double* rho_cur = rhos + (it & 1);
-      double* rho_prev = rhos + ((it + 1) & 1);
-      k_bicg_p2<<<g, kThreads, 0, s>>>(n, rho_cur, rho_prev, alpha, omega, r, v, dinv, p, ph);
-      spmv(A, ph, v, s);
-      k_bicg_alpha<<<g, kThreads, 0, s>>>(n, r0, v, c.part, ticket, rho_cur, alpha);
-      k_bicg_s2<<<g, kThreads, 0, s>>>(n, alpha, r, v, dinv, ss, sh);
-      spmv(A, sh, t, s);
-      k_bicg_omega<<<g, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks, ticket, omega);
-      k_bicg_x_rho<<<g, kThreads, 0, s>>>(n, alpha, omega, ph, sh, ss, t, r0, x, r, c.part, ticket,
-                                          rho_prev);   // rho of the next iteration
-    };
-    const int chunk = 10;
-    cudaGraphExec_t gexec = nullptr;
-    {
-      cudaGraph_t graph;
-      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        for (int k = 0; k < chunk; k++) iteration(k);   // chunks start at an even iteration
-        if (cudaStreamEndCapture(s, &graph) == cudaSuccess) {
-          if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
-          cudaGraphDestroy(graph);
-        }
-      }
-      cudaGetLastError();
-    }
-    while (bnorm > 0 && iters < max_iter) {
-      if (gexec && max_iter - iters >= chunk) {
-        cudaGraphLaunch(gexec, s);
-        iters += chunk;
-      } else {
-        for (int k = 0; k < chunk && iters < max_iter; k++, iters++) iteration(iters);
-      }
-      c.dot<double>(n, r, r, rr);
-      double hr = 0;
-      cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
-      cudaStreamSynchronize(s);
-      if (!(std::sqrt(hr) > rtol * bnorm) || !std::isfinite(hr)) break;
-    }
-    if (gexec) cudaGraphExecDestroy(gexec);
+    iters = bicg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, rtol, max_iter, 0, dscal, w, part2, ticket);
     cudaFreeAsync(part2, s);
-    cudaFreeAsync(r0, s); cudaFreeAsync(v, s); cudaFreeAsync(ss, s);
-    cudaFreeAsync(t, s); cudaFreeAsync(ph, s); cudaFreeAsync(sh, s);
-  } else if (method == 3) {
-    // FP32 PCG inside FP64 iterative refinement
-    float *af, *rf, *df, *zf, *pf, *qf, *wf;
-    cudaMallocAsync(&wf, n * sizeof(float), s);
+    for (int k : {1, 2, 4, 5, 6, 7}) cudaFreeAsync(w[k], s);
+  } else if (method == 3 || method == 7) {
+    // FP32 inner solves (PCG, or BiCGStab for the unsymmetric stiffness)
+    // inside FP64 iterative refinement: r = b - A x in FP64, A d ~= r with
+    // the FP32 matrix copy to kInnerTol, x += d
+    float *af, *rf, *df, *dinvf;
+    float* wf[8];
+    for (int k = 0; k < 8; k++) cudaMallocAsync(&wf[k], n * sizeof(float), s);
+    cudaMallocAsync(&dinvf, n * sizeof(float), s);
     cudaMallocAsync(&af, A.nnz * sizeof(float), s);
     cudaMallocAsync(&rf, n * sizeof(float), s);
     cudaMallocAsync(&df, n * sizeof(float), s);
-    cudaMallocAsync(&zf, n * sizeof(float), s);
-    cudaMallocAsync(&pf, n * sizeof(float), s);
-    cudaMallocAsync(&qf, n * sizeof(float), s);
+    double* part2 = nullptr;
+    if (method == 7) cudaMallocAsync(&part2, 2 * kRedBlocks * sizeof(double), s);
     k_convert<double, float><<<grid_for(A.nnz), kThreads, 0, s>>>(A.nnz, A.a, af);
+    k_convert<double, float><<<g, kThreads, 0, s>>>(n, dinv, dinvf);
     double* bb = dscal + 8;
     double* rr = dscal + 9;
     c.dot<double>(n, b, b, bb);
@@ -861,6 +950,7 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     cudaMemcpyAsync(&hb, bb, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     const double bnorm = std::sqrt(hb);
+    double last = INFINITY;
     for (int outer = 0; outer < 60 && bnorm > 0 && iters < max_iter; outer++) {
       spmv(A, x, ax, s);
       k_residual<<<g, kThreads, 0, s>>>(n, b, ax, r);
@@ -868,16 +958,35 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
       double hr = 0;
       cudaMemcpyAsync(&hr, rr, sizeof(double), cudaMemcpyDeviceToHost, s);
       cudaStreamSynchronize(s);
-      if (!(std::sqrt(hr) > rtol * bnorm)) break;
+      const double rn = std::sqrt(hr);
+      if (!(rn > rtol * bnorm)) break;   // converged
+      if (!(rn < 0.5 * last)) {
+        // the last correction did not halve the FP64 residual: the FP32
+        // matrix's rounding (about 6e-8 relative) times the condition number
+        // bounds what a refinement step can gain.  A step that made things
+        // worse is taken back; the caller falls back to an FP64 method.
+        if (!(rn < last)) {
+          k_add_to<<<g, kThreads, 0, s>>>(n, df, -1.0, x);
+          outer_steps--;
+        }
+        break;
+      }
+      last = rn;
       k_convert<double, float><<<g, kThreads, 0, s>>>(n, r, rf);
       cudaMemsetAsync(df, 0, n * sizeof(float), s);
-      iters += pcg_core<float>(c, n, avg, A.ia, A.ja, af, rf, df, dinv, 0, nullptr, nullptr, 1e-4,
-                               max_iter - iters, dscal, zf, pf, qf, wf, ticket, true);
-      k_add_to<<<g, kThreads, 0, s>>>(n, df, x);
+      if (method == 3)
+        iters += pcg_core<float>(c, n, avg, A.ia, A.ja, af, rf, df, dinvf, nb, bptr, binv, kInnerTol,
+                                 max_iter - iters, dscal, wf[0], wf[1], wf[2], wf[3], ticket, true);
+      else
+        iters += bicg_core<float>(c, n, avg, A.ia, A.ja, af, rf, df, dinvf, kInnerTol, max_iter - iters, kCgStallIts,
+                                  dscal, wf, part2, ticket);
+      k_add_to<<<g, kThreads, 0, s>>>(n, df, 1.0, x);
+      outer_steps++;
     }
-    cudaFreeAsync(wf, s);
+    if (part2) cudaFreeAsync(part2, s);
+    for (int k = 0; k < 8; k++) cudaFreeAsync(wf[k], s);
+    cudaFreeAsync(dinvf, s);
     cudaFreeAsync(af, s); cudaFreeAsync(rf, s); cudaFreeAsync(df, s);
-    cudaFreeAsync(zf, s); cudaFreeAsync(pf, s); cudaFreeAsync(qf, s);
   } else if (method == 6) {
     iters = gmres_core(c, A, b, x, dinv, rtol, max_iter, dscal, z);
   }
@@ -892,6 +1001,8 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   res->iterations = iters;
   res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
   res->converged = res->rel_residual <= rtol;
+  res->method = method;
+  res->refinements = outer_steps;
   cudaFreeAsync(r, s); cudaFreeAsync(z, s); cudaFreeAsync(p, s); cudaFreeAsync(q, s); cudaFreeAsync(ax, s);
   cudaFreeAsync(dinv, s); cudaFreeAsync(c.part, s); cudaFreeAsync(dscal, s); cudaFreeAsync(ticket, s);
   if (bptr) cudaFreeAsync(bptr, s);
@@ -1108,6 +1219,8 @@ cudaError_t krylov_fcg(const DevCsr& A, const double* b, double* x, double rtol,
   res->iterations = it;
   res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
   res->converged = !stalled && res->rel_residual <= rtol;
+  res->method = coarse ? 5 : 4;
+  res->refinements = 0;
   cudaFreeAsync(r, s);
   cudaFreeAsync(z, s);
   cudaFreeAsync(pqs, s);
@@ -1213,6 +1326,8 @@ cudaError_t krylov_pcg_noalloc(const DevCsr& A, const double* b, double* x, doub
   res->iterations = iters;
   res->rel_residual = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
   res->converged = res->rel_residual <= rtol;
+  res->method = 0;
+  res->refinements = 0;
   if (err == cudaSuccess) err = cudaGetLastError();
   return err;
 }

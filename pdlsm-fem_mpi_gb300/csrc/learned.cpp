@@ -172,7 +172,7 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
   const int maxit = m->cmd.solve_maxit;
   const int bd = m->mesh.dim;
   Learned* L = m->learned;
-  if (method <= 3 || method == 6) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
+  if (method <= 3 || method >= 6) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
   if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
   if (L->disabled) return plain_solve(m, b, x, nullptr, kr);
@@ -492,7 +492,7 @@ pdx_status pdx_newmark_init(pdx_model* m) {
 pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_info* info) {
   NEED_DEV(m);
   if (!m->newmark_ready) return set_error(PDX_ERR_INVALID, "pdx_newmark_init first");
-  if (method < 0 || method > 6) return set_error(PDX_ERR_INVALID, "method must be 0..6");
+  if (method < 0 || method > 7) return set_error(PDX_ERR_INVALID, "method must be 0..7");
   const int ne = m->setup.n_eq;
   double* u_all = m->d_u[0];
   double* upred = m->d_u[1];
@@ -519,10 +519,7 @@ pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_inf
   cudaEventDestroy(e1);
   if (st) return st;
   if (info) {
-    info->iterations = kr.iterations;
-    info->rel_residual = kr.rel_residual;
-    info->seconds = ms * 1e-3;
-    info->converged = kr.converged;
+    fill_solve_info(info, kr, ms * 1e-3);
   }
   if (!kr.converged)
     return set_error(PDX_ERR_NOCONV, "Newmark solve stopped at relative residual " + std::to_string(kr.rel_residual));

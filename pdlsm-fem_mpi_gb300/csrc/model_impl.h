@@ -213,4 +213,13 @@ extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);
 bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& err);
 void learned_destroy(pdx_model* m);
+inline void fill_solve_info(pdx_solve_info* info, const KrylovResult& kr, double seconds) {
+  if (!info) return;
+  info->iterations = kr.iterations;
+  info->rel_residual = kr.rel_residual;
+  info->seconds = seconds;
+  info->converged = kr.converged;
+  info->method_used = kr.method;
+  info->refinements = kr.refinements;
+}
 }  // namespace pdx

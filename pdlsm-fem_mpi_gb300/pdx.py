@@ -45,7 +45,7 @@ class SolveOpts(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("seconds", C.c_double),
-                ("converged", C.c_int)]
+                ("converged", C.c_int), ("method_used", C.c_int), ("refinements", C.c_int)]
 
 
 EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_model_destroy",
@@ -364,7 +364,8 @@ def solve_csr(ia: np.ndarray, ja: np.ndarray, a: np.ndarray, b: np.ndarray, meth
               rtol: float = 1e-8, max_iter: int = 20000, x0: Optional[np.ndarray] = None):
     """Solve A x = b on the GPU (pdx_solve_csr).  method: 0 Jacobi PCG,
     1 block-Jacobi PCG, 2 BiCGStab (Jacobi), 3 FP32 PCG in FP64 refinement,
-    6 GMRES(30) (right Jacobi).  Returns (x, SolveInfo)."""
+    6 GMRES(30) (right Jacobi), 7 FP32 BiCGStab in FP64 refinement.
+    Returns (x, SolveInfo)."""
     n = len(ia) - 1
     ia = np.ascontiguousarray(ia, dtype=np.int64)
     ja = np.ascontiguousarray(ja, dtype=np.int64)

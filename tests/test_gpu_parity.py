@@ -154,7 +154,7 @@ def test_newmark_matrix_matches_reference(built):
     assert rel(f, gn["FN"]) < 1e-12
 
 
-@pytest.mark.parametrize("method", [0, 1, 2, 3, 6])
+@pytest.mark.parametrize("method", [0, 1, 2, 3, 6, 7])
 def test_krylov_solves_reference_system(built, method):
     gs = golden("b13_static")
     x, info = pdx.solve_csr(gs["K_ia"], gs["K_ja"], gs["K_a"], gs["F"], method=method, rtol=1e-12,
@@ -167,6 +167,10 @@ def test_krylov_solves_reference_system(built, method):
     print(f"\nmethod {method}: {info.iterations} iterations, reported {info.rel_residual:.2e}, true {true_res:.2e}")
     if info.converged:
         assert true_res <= 1.01e-12
+        assert info.method_used == method
+        if method in (3, 7):
+            # FP32 inner solves to 1e-4: a 1e-12 FP64 residual takes several refinement steps
+            assert info.refinements >= 2
         # the reference's direct solve, in equation order; the system's 2-norm
         # condition number is 6.4e3, so a 1e-12 residual bounds the relative
         # error by 6.4e-9
@@ -400,7 +404,7 @@ def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
     assert int((bs32 != bs_o).sum()) <= max(2, int(0.01 * (bs_o == 0).sum()))
 
 
-@pytest.mark.parametrize("method", [1, 2, 3, 6])
+@pytest.mark.parametrize("method", [1, 2, 3, 6, 7])
 def test_quasi_static_increments_match_reference(built, method):
     """Three quasi-static increments, one pdx_quasi_step each, against the
     reference's direct-solve trajectory: the Krylov solves stop at a 1e-8 true
