@@ -144,8 +144,9 @@ IMPLICIT_MAX_STEPS = 5
 
 
 def bench_implicit(args):
-    """C5: implicit Newmark; solve time to a 1e-8 true FP64 residual per step for the learned two-level flexible CG
-    and for block-Jacobi flexible CG (the plain method), each from the same state after the training steps."""
+    """C5: implicit Newmark; solve time to a 1e-8 true FP64 residual per step for the learned two-level flexible CG,
+    for block-Jacobi flexible CG (the plain method) and for block-Jacobi PCG in FP32 inside FP64 refinement (the
+    mixed method), each from the same state after the training steps."""
     import meshgen
     import pdx
     tmp = tempfile.mkdtemp(prefix="pdx_bench_")
@@ -162,7 +163,7 @@ def bench_implicit(args):
         cells = (8, 4, 2)
     cmd = meshgen.write_case(mesh, tmp, "c5", **kw)
     res = {}
-    for method in (4, 5):
+    for method in (4, 5, 3):
         with pdx.Model(cmd, device=0) as m:
             if method == 5:
                 m.learned_setup(cells, hidden=128, seed=0, max_samples=(args.train_steps + args.probes) * 200)
@@ -181,18 +182,21 @@ def bench_implicit(args):
                 t0 = time.perf_counter()
                 loss = m.learned_train(epochs=100, lr=1e-3, seed=0)
                 t_train = time.perf_counter() - t0
-            sec, its, resid = [], [], []
+            sec, its, resid, refine, used = [], [], [], [], set()
             for _ in range(steps):
                 i = m.newmark_step(method)
                 sec.append(i.seconds)
                 its.append(i.iterations)
                 resid.append(i.rel_residual)
+                refine.append(i.refinements)
+                used.add(i.method_used)
             u = m.state()[0]
             res[method] = dict(sec=float(np.mean(sec)), its=float(np.mean(its)), resid=float(max(resid)), u=u,
                                loss=loss, t_train=t_train, t_collect=t_collect, pairs=pairs, n_eq=m.info.n_eq,
-                               nnz=m.info.nnz)
-    p, l = res[4], res[5]
+                               nnz=m.info.nnz, refine=float(np.mean(refine)), used=sorted(used))
+    p, l, x = res[4], res[5], res[3]
     du = float(np.linalg.norm(l["u"] - p["u"]) / max(np.linalg.norm(p["u"]), 1e-300))
+    dx = float(np.linalg.norm(x["u"] - p["u"]) / max(np.linalg.norm(p["u"]), 1e-300))
     line = {"metric": "implicit Newmark solve time to 1e-8 true residual (s per step)", "value": l["sec"],
             "unit": "s", "n_gpus": 1, "steps": steps, "warmup": args.train_steps, "ms_per_step": l["sec"] * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
@@ -207,7 +211,12 @@ def bench_implicit(args):
                         "iterations": l["its"], "max_rel_residual": l["resid"], "training_pairs": l["pairs"],
                         "final_loss": l["loss"], "train_s": l["t_train"], "collect_s": l["t_collect"]},
             "speedup_vs_plain": p["sec"] / l["sec"] if l["sec"] > 0 else None,
-            "u_rel_diff_learned_vs_plain": du}
+            "u_rel_diff_learned_vs_plain": du,
+            "mixed": {"method": "block-Jacobi PCG in FP32 (FP32 matrix copy) inside FP64 refinement",
+                      "s_per_step": x["sec"], "iterations": x["its"], "refinement_steps": x["refine"],
+                      "finished_by": x["used"], "max_rel_residual": x["resid"],
+                      "speedup_vs_plain": p["sec"] / x["sec"] if x["sec"] > 0 else None,
+                      "u_rel_diff_vs_plain": dx}}
     return line
 
 
@@ -375,7 +384,7 @@ def implicit_summary(args):
             setattr(sub, k, v)
         try:
             r = bench_quasi(sub) if name == "c3" else bench_implicit(sub)
-            keep = ("metric", "value", "unit", "config", "methods", "plain", "learned", "speedup_vs_plain")
+            keep = ("metric", "value", "unit", "config", "methods", "plain", "learned", "speedup_vs_plain", "mixed")
             out[name] = {k: r[k] for k in keep if k in r}
         except Exception as e:   # the explicit line stands without it
             out[name] = {"error": f"{type(e).__name__}: {e}"}
