@@ -102,16 +102,32 @@ def hold_clocks(index: int, advance, min_s: float = 1.0):
     return out
 
 
-def profile_traffic():
-    """DRAM bytes (read + write) per step-kernel launch from the committed ncu summary of this workload."""
+TRAFFIC_PROFILE = {("c2", "MIXED"): "k_step_mixed_c2.md", ("c2", "FP64"): "k_step_fp64_c2.md",
+                   ("c4", "MIXED"): "k_step_mixed_c4.md"}
+
+
+def profile_traffic(workload: str, precision: str, alg_bytes: float):
+    """DRAM bytes (read + write) per step-kernel launch from the committed ncu summary of this workload, scaled
+    by algorithmic bytes when the capture ran a smaller case (C4: 64 of the 256 plates).  Returns (bytes, file)."""
+    name = TRAFFIC_PROFILE.get((workload, precision))
+    if not name:
+        return None, None
+    vals = {}
     try:
-        with open(os.path.join(REPO, "profiles", "k_step_mixed_c2.md")) as f:
+        with open(os.path.join(REPO, "profiles", name)) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":", 1)[1])
+                for key in ("traffic_bytes_per_launch", "algorithmic_bytes_per_launch"):
+                    if line.startswith(key + ":"):
+                        vals[key] = float(line.split(":", 1)[1])
     except (OSError, ValueError):
-        pass
-    return None
+        return None, None
+    if "traffic_bytes_per_launch" not in vals:
+        return None, None
+    t = vals["traffic_bytes_per_launch"]
+    a = vals.get("algorithmic_bytes_per_launch")
+    if a:
+        t *= alg_bytes / a
+    return int(round(t)), f"profiles/{name}"
 
 
 def make_batch_workload(tmp: str, n_spec: int, nsteps: int, precision: str):
@@ -552,6 +568,7 @@ def main():
     e2e = info.n_bond * args.e2e_steps / t_e2e
     peak, kind = measured_peaks()
     achieved = alg["bytes"] / (t_s / args.steps) / 1e9
+    traffic, traffic_src = profile_traffic(args.workload, args.precision, alg["bytes"])
     line = {"metric": "explicit PD bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 forces / f64 state" if args.precision == "MIXED"
@@ -560,9 +577,9 @@ def main():
                     "d2h_bytes_per_step": info.n_eq * 8, "steps": args.e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
-                         "traffic": (profile_traffic() if args.precision == "MIXED" and args.workload == "c2"
-                                     else None),
-                         "traffic_unit": "bytes per launch (ncu, profiles/k_step_mixed_c2.md)", "peak_kind": kind,
+                         "traffic": traffic,
+                         "traffic_unit": f"bytes per launch (ncu, {traffic_src}; scaled by algorithmic bytes to "
+                                         f"this workload)" if traffic_src else None, "peak_kind": kind,
                          "algorithmic_bytes_per_step": alg["bytes"], "kernel": "k_step"},
             "gpu_launches": args.steps, "clocks": clk,
             "model": {"n_node": info.n_node, "n_fam": info.n_fam, "n_bond": info.n_bond, "n_eq": info.n_eq,

@@ -130,7 +130,10 @@ pdx_status pdx_explicit_advance(pdx_model* m, int nsteps);
 pdx_status pdx_explicit_advance_timed(pdx_model* m, int nsteps, double* ms);
 /* One explicit step through host buffers, the contract of timeIntegration_LM
  * (pdsolve.cpp:5113-5132): u_n and u_nm1 (n_eq, active DOFs) in, u_np1 out;
- * prescribed values and bond states are the model's.  Copies are inside. */
+ * prescribed values and bond states are the model's.  With page-locked
+ * buffers (cudaHostAlloc / cudaHostRegister, all three) the GPU reads and
+ * writes them in place over the coherent host link; pageable buffers are
+ * copied through device staging.  Returns after u_np1 is written. */
 pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1);
 int64_t pdx_explicit_step_count(const pdx_model* m);
 /* Reaction forces of the RF keyword's essential BCs, one row per recorded

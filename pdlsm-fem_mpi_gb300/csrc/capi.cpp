@@ -1030,23 +1030,47 @@ pdx_status pdx_explicit_advance_timed(pdx_model* m, int nsteps, double* ms) {
   return st;
 }
 
+namespace {
+// The device address of a page-locked (pinned or registered) host buffer,
+// or null for pageable memory.
+const void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+}  // namespace
+
+// With page-locked host buffers (all three), the step reads u_n and u_{n-1}
+// and writes u_{n+1} in place over the coherent host link: one load kernel
+// (scatter and FP32 shadow fused), the step, one gather kernel into the
+// caller's buffer.  Pageable buffers take staged copies and the same kernels.
 pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1) {
   NEED_DEVICE(m);
   if (!u_n || !u_nm1 || !u_np1) return set_error(PDX_ERR_INVALID, "null argument");
   const size_t ne = (size_t)m->setup.n_eq;
-  cudaMemcpyAsync(m->d_tmp_eq[0], u_n, ne * 8, cudaMemcpyHostToDevice, m->stream);
-  cudaMemcpyAsync(m->d_tmp_eq[1], u_nm1, ne * 8, cudaMemcpyHostToDevice, m->stream);
-  launch_scatter_eq(m->view, m->d_tmp_eq[0], m->d_u[m->cur], m->stream);
-  launch_scatter_eq(m->view, m->d_tmp_eq[1], m->d_u[1 - m->cur], m->stream);
-  if (m->mixed) launch_shadow(m->view, m->d_u[m->cur], m->d_uf[m->cur], m->stream);
+  const double* dn = static_cast<const double*>(mapped_host(u_n));
+  const double* dm = static_cast<const double*>(mapped_host(u_nm1));
+  double* dout = static_cast<double*>(const_cast<void*>(mapped_host(u_np1)));
+  if (!dn || !dm || !dout) {
+    cudaMemcpyAsync(m->d_tmp_eq[0], u_n, ne * 8, cudaMemcpyHostToDevice, m->stream);
+    cudaMemcpyAsync(m->d_tmp_eq[1], u_nm1, ne * 8, cudaMemcpyHostToDevice, m->stream);
+    dn = m->d_tmp_eq[0];
+    dm = m->d_tmp_eq[1];
+    dout = nullptr;
+  }
+  launch_load_pair(m->view, dn, dm, m->d_u[m->cur], m->d_u[1 - m->cur], m->mixed ? m->d_uf[m->cur] : nullptr,
+                   m->stream);
   pdx_status st = explicit_step_launch(m, m->steps_done == 0 ? 0 : 1, m->steps_done);
   if (st) return st;
   st = fc2_pass(m);
   if (!st) st = rf_record(m, m->steps_done);
   if (st) return st;
   m->steps_done++;
-  launch_gather_eq(m->view, m->d_u[m->cur], m->d_tmp_eq[2], m->stream);
-  cudaMemcpyAsync(u_np1, m->d_tmp_eq[2], ne * 8, cudaMemcpyDeviceToHost, m->stream);
+  launch_gather_eq(m->view, m->d_u[m->cur], dout ? dout : m->d_tmp_eq[2], m->stream);
+  if (!dout) cudaMemcpyAsync(u_np1, m->d_tmp_eq[2], ne * 8, cudaMemcpyDeviceToHost, m->stream);
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit step");
 }
 

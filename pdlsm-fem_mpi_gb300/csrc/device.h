@@ -225,6 +225,8 @@ cudaError_t launch_fc2_candidates(const Fc2Args& a, cudaStream_t s);
 cudaError_t launch_fc2_cut(const Fc2Args& a, cudaStream_t s);
 cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, double beta, double dt, cudaStream_t s);
 cudaError_t launch_shadow(const DevView& v, const double* u_all, float4* uf, cudaStream_t s);
+cudaError_t launch_load_pair(const DevView& v, const double* un_eq, const double* unm1_eq, double* u_cur,
+                             double* u_prev, float4* uf, cudaStream_t s);
 
 // Krylov solvers on a device CSR matrix (k_krylov.cu)
 struct DevCsr {

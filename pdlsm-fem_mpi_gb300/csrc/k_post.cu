@@ -326,6 +326,36 @@ __global__ void k_advance_prescribed_quasi(DevView v, double* u_all) {
   if (v.eq[i] < 0 && ((v.bcflag[n] >> d) & 1u) && u_all[i] == 0.0) u_all[i] = v.dtv[3 * n + d];
 }
 
+// u_n and u_{n-1} in equation order into the node-ordered states in one pass
+// (prescribed DOFs keep their device values), and with uf the FP32 shadow of
+// u_n as k_shadow writes it.  The inputs may be the caller's page-locked host
+// buffers, read over the coherent host link without a staging copy.
+template <int D>
+__global__ void k_load_pair(DevView v, const double* un_eq, const double* unm1_eq, double* u_cur, double* u_prev,
+                            float4* uf) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= v.n_node) return;
+  float c[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = 0; d < D; d++) {
+    const int64_t i = (int64_t)n * D + d;
+    const int e = v.eq[i];
+    double x;
+    if (e >= 0) {
+      x = un_eq[e];
+      u_cur[i] = x;
+      u_prev[i] = unm1_eq[e];
+    } else {
+      x = u_cur[i];
+    }
+    c[d] = (float)x;
+  }
+  if (uf) {
+    uf[2 * n] = v.Xf[n];
+    uf[2 * n + 1] = make_float4(c[0], c[1], D == 3 ? c[2] : 0.f, __uint_as_float((unsigned)v.bcflag[n]));
+  }
+}
+
 template <int D>
 __global__ void k_shadow(DevView v, const double* u, float4* uf) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -485,6 +515,14 @@ cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cud
   const int blocks = (int)((n + 255) / 256);
   if (v.dim == 2) k_advance_prescribed_quasi<2><<<blocks, 256, 0, s>>>(v, u_all);
   else k_advance_prescribed_quasi<3><<<blocks, 256, 0, s>>>(v, u_all);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_load_pair(const DevView& v, const double* un_eq, const double* unm1_eq, double* u_cur,
+                             double* u_prev, float4* uf, cudaStream_t s) {
+  const int blocks = (v.n_node + 255) / 256;
+  if (v.dim == 2) k_load_pair<2><<<blocks, 256, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
+  else k_load_pair<3><<<blocks, 256, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
   return cudaGetLastError();
 }
 
