@@ -65,23 +65,52 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
     for (int i = 0; i < 3; i++) xk[i] = v.X[3 * node + i];
 #pragma unroll
     for (int i = 0; i < D; i++) ukst[i] = a.u_n[(int64_t)node * D + i];
+    const bool k_moves = v.bcflag[node] != 0;
+    const float s0f = (float)s0fam, pertf = (float)v.s0_pert;
     for (int b = b0 + lane; b < b1; b += L) {
       const uint32_t w = v.state[b >> 5];
       if (!((w >> (b & 31)) & 1u)) continue;
       const int m = __ldcs(&v.nbr[b]);
+      double eta[3] = {0, 0, 0};
+      bool have_eta = false;
       if (brk) {
         const uint32_t h = bond_hash(v.s0_seed32, node, m);
-        double xi[3], eta[3] = {0, 0, 0};
+        double xi[3];
 #pragma unroll
         for (int i = 0; i < 3; i++) xi[i] = v.X[3 * m + i] - xk[i];
 #pragma unroll
         for (int i = 0; i < D; i++) eta[i] = a.u_n[(int64_t)m * D + i] - ukst[i];
-        const double xx = xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2];
-        const double lhs = 2.0 * (xi[0] * eta[0] + xi[1] * eta[1] + xi[2] * eta[2]) +
-                           (eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
-        const double sc = bond_s0(s0fam, v.s0_pert, h);
-        const double rhs = sc * (2.0 + sc) * xx;
-        const bool cut = fabs(lhs - rhs) <= 1e-9 * rhs ? stretch_over_fp64<D>(v, a.u_n, node, m, sc) : lhs > rhs;
+        have_eta = true;
+        // The test 2 xi.eta + eta.eta > s (2 + s) |xi|^2 in FP32 first, on
+        // xi and eta rounded from their FP64 values (integer-pipe
+        // conversion): its rounding error is below 1e-6 of the sum of the
+        // terms' magnitudes, so outside a band of 1e-5 of that sum the FP32
+        // answer is the FP64 one; inside it the FP64 test (and within 1e-9
+        // the reference's own expression) decides.  This keeps the square
+        // norms, the threshold and the comparison off the 2-lane FP64 pipe
+        // for nearly every bond.
+        float xf[3], ef[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < 3; i++) xf[i] = d2f_bits(xi[i]);
+#pragma unroll
+        for (int i = 0; i < D; i++) ef[i] = d2f_bits(eta[i]);
+        const float xx32 = xf[0] * xf[0] + xf[1] * xf[1] + xf[2] * xf[2];
+        const float ee32 = ef[0] * ef[0] + ef[1] * ef[1] + ef[2] * ef[2];
+        const float lhs32 = 2.f * (xf[0] * ef[0] + xf[1] * ef[1] + xf[2] * ef[2]) + ee32;
+        const float sc32 = bond_s0_f32(s0f, pertf, h);
+        const float rhs32 = sc32 * (2.f + sc32) * xx32;
+        const float band = 1e-5f * (2.f * sqrtf(xx32 * ee32) + ee32 + rhs32);
+        bool cut;
+        if (fabsf(lhs32 - rhs32) > band) {
+          cut = lhs32 > rhs32;
+        } else {
+          const double xx = xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2];
+          const double lhs = 2.0 * (xi[0] * eta[0] + xi[1] * eta[1] + xi[2] * eta[2]) +
+                             (eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
+          const double sc = bond_s0(s0fam, v.s0_pert, h);
+          const double rhs = sc * (2.0 + sc) * xx;
+          cut = fabs(lhs - rhs) <= 1e-9 * rhs ? stretch_over_fp64<D>(v, a.u_n, node, m, sc) : lhs > rhs;
+        }
         if (cut) {
           atomicAnd(&v.state[b >> 5], ~(1u << (b & 31)));
           nbroken++;
@@ -90,9 +119,15 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
       }
       if (a.mode == 2) continue;
       double du[D];
-      load_u(m, du);
+      if (have_eta && !k_moves && v.bcflag[m] == 0) {
+        // no varying prescribed value at either end: u_m - u_k is eta
 #pragma unroll
-      for (int i = 0; i < D; i++) du[i] -= uk[i];
+        for (int i = 0; i < D; i++) du[i] = eta[i];
+      } else {
+        load_u(m, du);
+#pragma unroll
+        for (int i = 0; i < D; i++) du[i] -= uk[i];
+      }
       bond_block<D, double>(v.coef64, v.corr64, v.n_bond, v.n_corr_bond, b,
                             corr0 >= 0 ? (int64_t)corr0 + (b - b0) : -1, du, acc);
     }
