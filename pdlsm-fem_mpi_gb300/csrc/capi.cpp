@@ -1045,8 +1045,9 @@ const void* mapped_host(const void* p) {
 
 // With page-locked host buffers (all three), the step reads u_n and u_{n-1}
 // and writes u_{n+1} in place over the coherent host link: one load kernel
-// (scatter and FP32 shadow fused), the step, one gather kernel into the
-// caller's buffer.  Pageable buffers take staged copies and the same kernels.
+// (scatter and FP32 shadow fused), the step, one store kernel into the
+// caller's buffer, both moving each block's equation range as consecutive
+// words.  Pageable buffers take staged copies.
 pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double* u_nm1, double* u_np1) {
   NEED_DEVICE(m);
   if (!u_n || !u_nm1 || !u_np1) return set_error(PDX_ERR_INVALID, "null argument");
@@ -1069,7 +1070,8 @@ pdx_status pdx_explicit_step_host(pdx_model* m, const double* u_n, const double*
   if (!st) st = rf_record(m, m->steps_done);
   if (st) return st;
   m->steps_done++;
-  launch_gather_eq(m->view, m->d_u[m->cur], dout ? dout : m->d_tmp_eq[2], m->stream);
+  if (dout) launch_store_eq(m->view, m->d_u[m->cur], dout, m->stream);
+  else launch_gather_eq(m->view, m->d_u[m->cur], m->d_tmp_eq[2], m->stream);
   if (!dout) cudaMemcpyAsync(u_np1, m->d_tmp_eq[2], ne * 8, cudaMemcpyDeviceToHost, m->stream);
   return cuda_check(cudaStreamSynchronize(m->stream), "explicit step");
 }

@@ -227,6 +227,7 @@ cudaError_t launch_newmark_matrix(int64_t nnz, double* k, const double* m, doubl
 cudaError_t launch_shadow(const DevView& v, const double* u_all, float4* uf, cudaStream_t s);
 cudaError_t launch_load_pair(const DevView& v, const double* un_eq, const double* unm1_eq, double* u_cur,
                              double* u_prev, float4* uf, cudaStream_t s);
+cudaError_t launch_store_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s);
 
 // Krylov solvers on a device CSR matrix (k_krylov.cu)
 struct DevCsr {

@@ -12,6 +12,8 @@
 // a time), through per-bond / per-element column offsets precomputed from the
 // reference's CSR pattern (setCSRIndexes_gloStiffMat :959-1121).  No atomics,
 // no binary search (findCSRIndexOfMat :1773-1802).
+#include <climits>
+
 #include "device.h"
 
 namespace pdx {
@@ -326,13 +328,61 @@ __global__ void k_advance_prescribed_quasi(DevView v, double* u_all) {
   if (v.eq[i] < 0 && ((v.bcflag[n] >> d) & 1u) && u_all[i] == 0.0) u_all[i] = v.dtv[3 * n + d];
 }
 
+// Equation range [lo, hi] of the DOFs of a block's nodes (256 nodes per
+// block), for staging host-resident equation-ordered vectors through shared
+// memory: with the usual numbering (DOFs numbered in node order, prescribed
+// ones skipped) the range is contiguous and holds exactly the block's DOFs,
+// so the host link sees coalesced runs instead of 8-byte accesses three
+// apart.  lo > hi when the block has no free DOF.
+template <int D>
+__device__ __forceinline__ void block_eq_range(const DevView& v, int* s_lo, int* s_hi) {
+  if (threadIdx.x == 0) {
+    *s_lo = INT_MAX;
+    *s_hi = -1;
+  }
+  __syncthreads();
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  int lo = INT_MAX, hi = -1;
+  if (n < v.n_node) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      const int e = v.eq[(int64_t)n * D + d];
+      if (e >= 0) {
+        lo = min(lo, e);
+        hi = max(hi, e);
+      }
+    }
+  }
+  if (hi >= 0) {
+    atomicMin(s_lo, lo);
+    atomicMax(s_hi, hi);
+  }
+  __syncthreads();
+}
+
+constexpr int kStageNodes = 256;
+
 // u_n and u_{n-1} in equation order into the node-ordered states in one pass
 // (prescribed DOFs keep their device values), and with uf the FP32 shadow of
 // u_n as k_shadow writes it.  The inputs may be the caller's page-locked host
-// buffers, read over the coherent host link without a staging copy.
+// buffers: each block first copies its equation range of both vectors into
+// shared memory with consecutive loads (when the range fits, as it does for
+// the usual numbering), then scatters from there.
 template <int D>
-__global__ void k_load_pair(DevView v, const double* un_eq, const double* unm1_eq, double* u_cur, double* u_prev,
-                            float4* uf) {
+__global__ void __launch_bounds__(kStageNodes) k_load_pair(DevView v, const double* un_eq, const double* unm1_eq,
+                                                          double* u_cur, double* u_prev, float4* uf) {
+  __shared__ double s_n[kStageNodes * D], s_m[kStageNodes * D];
+  __shared__ int s_lo, s_hi;
+  block_eq_range<D>(v, &s_lo, &s_hi);
+  const int lo = s_lo, cnt = s_hi - s_lo + 1;
+  const bool staged = cnt > 0 && cnt <= kStageNodes * D;
+  if (staged) {
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+      s_n[k] = un_eq[lo + k];
+      s_m[k] = unm1_eq[lo + k];
+    }
+  }
+  __syncthreads();
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= v.n_node) return;
   float c[3] = {0.f, 0.f, 0.f};
@@ -342,9 +392,9 @@ __global__ void k_load_pair(DevView v, const double* un_eq, const double* unm1_e
     const int e = v.eq[i];
     double x;
     if (e >= 0) {
-      x = un_eq[e];
+      x = staged ? s_n[e - lo] : un_eq[e];
       u_cur[i] = x;
-      u_prev[i] = unm1_eq[e];
+      u_prev[i] = staged ? s_m[e - lo] : unm1_eq[e];
     } else {
       x = u_cur[i];
     }
@@ -354,6 +404,42 @@ __global__ void k_load_pair(DevView v, const double* un_eq, const double* unm1_e
     uf[2 * n] = v.Xf[n];
     uf[2 * n + 1] = make_float4(c[0], c[1], D == 3 ? c[2] : 0.f, __uint_as_float((unsigned)v.bcflag[n]));
   }
+}
+
+// u_eq[e] = u_all[i] for the free DOFs, u_eq possibly the caller's
+// page-locked host buffer: each block assembles its equation range in shared
+// memory and writes it with consecutive stores (only the positions its own
+// DOFs fill), else stores directly.
+template <int D>
+__global__ void __launch_bounds__(kStageNodes) k_store_eq(DevView v, const double* u_all, double* u_eq) {
+  __shared__ double s_u[kStageNodes * D];
+  __shared__ unsigned char s_set[kStageNodes * D];
+  __shared__ int s_lo, s_hi;
+  block_eq_range<D>(v, &s_lo, &s_hi);
+  const int lo = s_lo, cnt = s_hi - s_lo + 1;
+  const bool staged = cnt > 0 && cnt <= kStageNodes * D;
+  if (staged)
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) s_set[k] = 0;
+  __syncthreads();
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n < v.n_node) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      const int64_t i = (int64_t)n * D + d;
+      const int e = v.eq[i];
+      if (e < 0) continue;
+      if (staged) {
+        s_u[e - lo] = u_all[i];
+        s_set[e - lo] = 1;
+      } else {
+        u_eq[e] = u_all[i];
+      }
+    }
+  }
+  if (!staged) return;
+  __syncthreads();
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+    if (s_set[k]) u_eq[lo + k] = s_u[k];
 }
 
 template <int D>
@@ -520,9 +606,16 @@ cudaError_t launch_advance_prescribed_quasi(const DevView& v, double* u_all, cud
 
 cudaError_t launch_load_pair(const DevView& v, const double* un_eq, const double* unm1_eq, double* u_cur,
                              double* u_prev, float4* uf, cudaStream_t s) {
-  const int blocks = (v.n_node + 255) / 256;
-  if (v.dim == 2) k_load_pair<2><<<blocks, 256, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
-  else k_load_pair<3><<<blocks, 256, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
+  const int blocks = (v.n_node + kStageNodes - 1) / kStageNodes;
+  if (v.dim == 2) k_load_pair<2><<<blocks, kStageNodes, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
+  else k_load_pair<3><<<blocks, kStageNodes, 0, s>>>(v, un_eq, unm1_eq, u_cur, u_prev, uf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_store_eq(const DevView& v, const double* u_all, double* u_eq, cudaStream_t s) {
+  const int blocks = (v.n_node + kStageNodes - 1) / kStageNodes;
+  if (v.dim == 2) k_store_eq<2><<<blocks, kStageNodes, 0, s>>>(v, u_all, u_eq);
+  else k_store_eq<3><<<blocks, kStageNodes, 0, s>>>(v, u_all, u_eq);
   return cudaGetLastError();
 }
 
