@@ -67,6 +67,8 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
     for (int i = 0; i < D; i++) ukst[i] = a.u_n[(int64_t)node * D + i];
     const bool k_moves = v.bcflag[node] != 0;
     const float s0f = (float)s0fam, pertf = (float)v.s0_pert;
+    const float4 xkf = v.Xf[node];
+    const float xkmag = fmaxf(fabsf(xkf.x), fmaxf(fabsf(xkf.y), fabsf(xkf.z)));
     for (int b = b0 + lane; b < b1; b += L) {
       const uint32_t w = v.state[b >> 5];
       if (!((w >> (b & 31)) & 1u)) continue;
@@ -75,35 +77,41 @@ __device__ __forceinline__ void fp64_family_item(const StepArgs& a, int64_t t) {
       bool have_eta = false;
       if (brk) {
         const uint32_t h = bond_hash(v.s0_seed32, node, m);
-        double xi[3];
-#pragma unroll
-        for (int i = 0; i < 3; i++) xi[i] = v.X[3 * m + i] - xk[i];
 #pragma unroll
         for (int i = 0; i < D; i++) eta[i] = a.u_n[(int64_t)m * D + i] - ukst[i];
         have_eta = true;
-        // The test 2 xi.eta + eta.eta > s (2 + s) |xi|^2 in FP32 first, on
-        // xi and eta rounded from their FP64 values (integer-pipe
-        // conversion): its rounding error is below 1e-6 of the sum of the
-        // terms' magnitudes, so outside a band of 1e-5 of that sum the FP32
-        // answer is the FP64 one; inside it the FP64 test (and within 1e-9
-        // the reference's own expression) decides.  This keeps the square
+        // The test 2 xi.eta + eta.eta > s (2 + s) |xi|^2 in FP32 first: eta
+        // rounded from its FP64 value (integer-pipe conversion), xi from the
+        // FP32 node positions.  The FP32 arithmetic errs by less than 1e-6 of
+        // the sum of the terms' magnitudes and the positions' rounding by
+        // less than 2.1e-7 max|X| in the length of xi (so in lhs and rhs by
+        // 2.1e-7 max|X| (2|eta| + 2 s (2+s) |xi|)); outside a band of ten
+        // times the first and about five times the second the FP32 answer is the
+        // FP64 one, and inside it the FP64 test (and within 1e-9 the
+        // reference's own expression) decides.  This keeps xi, the square
         // norms, the threshold and the comparison off the 2-lane FP64 pipe
         // for nearly every bond.
-        float xf[3], ef[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int i = 0; i < 3; i++) xf[i] = d2f_bits(xi[i]);
+        const float4 xmf = v.Xf[m];
+        const float xf[3] = {xmf.x - xkf.x, xmf.y - xkf.y, xmf.z - xkf.z};
+        const float xmag = fmaxf(xkmag, fmaxf(fabsf(xmf.x), fmaxf(fabsf(xmf.y), fabsf(xmf.z))));
+        float ef[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < D; i++) ef[i] = d2f_bits(eta[i]);
         const float xx32 = xf[0] * xf[0] + xf[1] * xf[1] + xf[2] * xf[2];
         const float ee32 = ef[0] * ef[0] + ef[1] * ef[1] + ef[2] * ef[2];
         const float lhs32 = 2.f * (xf[0] * ef[0] + xf[1] * ef[1] + xf[2] * ef[2]) + ee32;
         const float sc32 = bond_s0_f32(s0f, pertf, h);
-        const float rhs32 = sc32 * (2.f + sc32) * xx32;
-        const float band = 1e-5f * (2.f * sqrtf(xx32 * ee32) + ee32 + rhs32);
+        const float q = sc32 * (2.f + sc32);
+        const float rhs32 = q * xx32;
+        const float band = 1e-5f * (2.f * sqrtf(xx32 * ee32) + ee32 + rhs32) +
+                           1e-6f * xmag * (2.f * sqrtf(ee32) + 2.f * q * sqrtf(xx32));
         bool cut;
         if (fabsf(lhs32 - rhs32) > band) {
           cut = lhs32 > rhs32;
         } else {
+          double xi[3];
+#pragma unroll
+          for (int i = 0; i < 3; i++) xi[i] = v.X[3 * m + i] - xk[i];
           const double xx = xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2];
           const double lhs = 2.0 * (xi[0] * eta[0] + xi[1] * eta[1] + xi[2] * eta[2]) +
                              (eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
