@@ -425,8 +425,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-implicit", action="store_true",
                     help="c2: leave out the implicit sub-record (C3 increment, C5 small Newmark solves)")
-    ap.add_argument("--lanes", type=int, default=0, help="lanes per PD family (0: default, -1: timed on the model)")
-    ap.add_argument("--fe-lanes", type=int, default=0, help="lanes per FE-only node (0: default, -1: timed)")
+    ap.add_argument("--lanes", type=int, default=-1,
+                    help="lanes per PD family (-1: timed on the model by the library's autotuner, the default; "
+                         "0: the library's fixed default)")
+    ap.add_argument("--fe-lanes", type=int, default=-1, help="lanes per FE-only node (-1: timed, 0: fixed default)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2: 3D box with hole (default); c1: 2D strip plate; c4: batch of uneven 2D plates in "
                          "one launch; c3: quasi-static increments, Krylov methods beside a CPU direct solve; "
@@ -503,6 +505,9 @@ def main():
     else:
         model = pdx.Model.batch(cmd, device=local, precision=prec, lanes=args.lanes, fe_lanes=args.fe_lanes)
     info = model.info
+    config["lanes"] = {"per_family": info.lanes, "per_fe_node": info.fe_lanes,
+                       "chosen": "timed on the model (pdx_options lanes = -1)" if args.lanes < 0 or args.fe_lanes < 0
+                       else "fixed"}
     alg = algorithmic_bytes(model)
     # warm-up steps (step 0 included), then the timed region in windows that
     # restart from the initial state, each within the steps the model keeps
