@@ -20,16 +20,17 @@
 // partials then one block) so results are bitwise reproducible.
 //
 // GB300 runs FP64 arithmetic (and float<->double conversion) at 2 lanes per
-// clock per SM against about 128 for FP32, so in the FP64 methods the
-// arithmetic of the mat-vec and the vector steps, not memory, is the limit:
-// every scalar ratio (alpha, beta) is formed once, by the last block of the
-// reduction that produces it, and not per thread; the FP32 inner solve of
-// method 3 does its element arithmetic in FP32 and converts only its block
-// partials to FP64.
+// clock per SM against about 128 for FP32: the FP64 mat-vec at 30 nonzeros
+// per row is bound by that rate (FP64 pipe 77 % busy, DRAM 48 %), and a
+// division in every thread costs microseconds per kernel.  Every scalar ratio
+// (alpha, beta, omega) is therefore formed once, by the last block of the
+// reduction that produces it; the FP32 inner solves of methods 3 and 7 do
+// their element arithmetic in FP32 and widen only their block partials to
+// FP64.
 #include <algorithm>
-#include <type_traits>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "device.h"
@@ -1035,7 +1036,7 @@ struct FcgDirs {
   int m;                           // kept directions, most recent first
 };
 
-// sum of np partials in the order of k_dot_final (thread-strided, then a tree)
+// sum of np partials in the order of k_dot_final (thread-strided, then block_sum)
 __device__ __forceinline__ double reduce_partials(const double* part, int np, double* sh) {
   double s = 0;
   for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
