@@ -248,7 +248,8 @@ def bench_quasi(args):
     mesh, kw = meshgen.config_c3(nsteps=2)
     cmd = meshgen.write_case(mesh, tmp, "c3", **kw)
     names = {0: "Jacobi PCG", 1: "block-Jacobi PCG", 2: "BiCGStab (Jacobi)", 3: "mixed FP32 PCG + FP64 refinement",
-             6: "GMRES(30)", 7: "mixed FP32 BiCGStab + FP64 refinement"}
+             6: "GMRES(30)", 7: "mixed FP32 BiCGStab + FP64 refinement",
+             8: "BiCGStab, Jacobi + Galerkin coarse correction (20x20-cell lattice)"}
     res, u_end = {}, {}
     loaded = None
     # each sample is a whole solve (0.3 to 2 s): at most 5 timed after 1 untimed
@@ -256,7 +257,7 @@ def bench_quasi(args):
     methods = [int(x) for x in args.c3_methods.split(",")]
     for method in methods:
         with pdx.Model(cmd, device=0, precision=0) as m:
-            sec, its, resid, wall, used, refine = [], [], [], [], set(), []
+            sec, its, resid, wall, used, refine, setup = [], [], [], [], set(), [], []
             for rep in range(warmup + steps):
                 m.quasi_init()
                 m.quasi_step(method)
@@ -271,12 +272,15 @@ def bench_quasi(args):
                     resid.append(i.rel_residual)
                     used.add(names.get(i.method_used, str(i.method_used)))
                     refine.append(i.refinements)
+                    setup.append(i.setup_seconds)
             u_end[method] = m.state()[0]
             res[method] = dict(method=names[method], s_per_increment=float(np.mean(sec)),
                                increment_wall_s=float(np.mean(wall)), iterations=float(np.mean(its)),
                                max_rel_residual=float(max(resid)), finished_by=sorted(used))
             if method in (3, 7):
                 res[method]["refinement_steps"] = float(np.mean(refine))
+            if method == 8:
+                res[method]["coarse_setup_s"] = float(np.mean(setup))
             n_eq, nnz = m.info.n_eq, m.info.nnz
     ref = u_end[methods[0]]
     for k in res:
@@ -434,9 +438,10 @@ def main():
                          "one launch; c3: quasi-static increments, Krylov methods beside a CPU direct solve; "
                          "c5: implicit Newmark, learned vs plain preconditioner")
     ap.add_argument("--specimens", type=int, default=256, help="c4: number of specimens")
-    ap.add_argument("--c3-methods", default="2,7,1,0,3",
+    ap.add_argument("--c3-methods", default="2,8,7,1,0,3",
                     help="c3: Krylov methods to time, comma separated (0 PCG, 1 block-Jacobi PCG, 2 BiCGStab, "
-                         "3 mixed PCG + FP64 refinement, 6 GMRES, 7 mixed BiCGStab + FP64 refinement); the "
+                         "3 mixed PCG + FP64 refinement, 6 GMRES, 7 mixed BiCGStab + FP64 refinement, 8 BiCGStab "
+                         "with Jacobi + Galerkin coarse correction); the "
                          "first is the one the others' solutions are compared with")
     ap.add_argument("--c5-size", default="full", choices=["full", "medium", "small"],
                     help="c5: 201x101x41 nodes (full), 101x51x21 (medium) or 61x31x13 (small)")

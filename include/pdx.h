@@ -72,6 +72,7 @@ typedef struct pdx_solve_info {
   int method_used;       /* the method whose iterate was returned: the requested
                             one, or 2 (BiCGStab) / 6 (GMRES) after a fallback */
   int refinements;       /* methods 3 and 7: FP64 refinement steps (FP32 inner solves) */
+  double setup_seconds;  /* method 8: device time of forming the coarse matrix and its inverse (in seconds) */
 } pdx_solve_info;
 
 const char* pdx_last_error(void);
@@ -197,7 +198,9 @@ pdx_status pdx_pcg_solve_noalloc(int64_t n, int64_t nnz, const int64_t* d_ia, co
  * K_N = beta dt^2 K + M assembled on the GPU (pdfemAssembleKNFR_CSRformat
  * :6327-6397), K_N a = F solved by `method`, update (updateDispVelo
  * :6399-6422).  The reference factorises K_N with PARDISO at every step.
- * method: 0-3, 6 and 7 as pdx_solve_opts.method; 4 block-Jacobi flexible CG (the plain
+ * method: 0-3, 6 and 7 as pdx_solve_opts.method; 8 (2D models) BiCGStab right
+ * preconditioned by Jacobi plus the Galerkin coarse correction P (P^T K P)^-1 P^T
+ * on a lattice coarse grid over the nodes (bilinear P, up to 20 x 20 cells); 4 block-Jacobi flexible CG (the plain
  * method); 5 flexible CG with block-Jacobi plus the learned coarse correction,
  * falling back to 4 and then BiCGStab when it stalls.  collect = 1 (method 4)
  * stores one training pair per iteration of the solve.  info: iterations,
@@ -281,8 +284,9 @@ pdx_status pdx_run(pdx_model* m, const char* results_dir);
  * PARDISO solve replaced by a Krylov method: pdx_quasi_init resets the state
  * (initial DOF values, pre-crack bond states); each pdx_quasi_step assembles
  * K and f_ext - K u through the scatter map, solves K du = f_ext - K u to the
- * command file's tolerance with `method` (as pdx_solve_opts; BiCGStab and
- * then GMRES(30) take over if it does not converge), updates u, applies FC 3 or FC 2 bond
+ * command file's tolerance with `method` (as pdx_solve_opts, or 8 in 2D: the
+ * two-level BiCGStab of pdx_newmark_step; BiCGStab and then GMRES(30) take
+ * over if it does not converge), updates u, applies FC 3 or FC 2 bond
  * failure, recomputes the stresses, records the reaction forces and advances
  * the prescribed DOFs by the reference's quasi-static rule
  * (setVaryEssentialBC, pdsolve.cpp:5263-5311): a varying EBC whose value is

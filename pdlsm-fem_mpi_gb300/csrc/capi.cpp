@@ -692,6 +692,7 @@ void pdx_model_destroy(pdx_model* m) {
     if (m->graph) cudaGraphExecDestroy(m->graph);
     if (m->stream) cudaStreamSynchronize(m->stream);
     learned_destroy(m);
+    twolevel_destroy(m);
     m->buf.free_all();
     if (m->stream) cudaStreamDestroy(m->stream);
   }
@@ -1155,6 +1156,9 @@ pdx_status pdx_solve_csr(long long n, const long long* ia, const long long* ja, 
   if (n <= 0 || !ia || !ja || !a || !rhs || !x) return set_error(PDX_ERR_INVALID, "bad argument");
   pdx_solve_opts o{2, 1e-8, 20000, 0};
   if (opts) o = *opts;
+  if (o.method == 8)
+    return set_error(PDX_ERR_INVALID, "method 8 builds its coarse grid from the model's nodes: use pdx_quasi_step or "
+                                      "pdx_newmark_step");
   if (o.method < 0 || (o.method > 3 && o.method < 6) || o.method > 7)
     return set_error(PDX_ERR_INVALID, "method must be 0..3, 6 or 7");
   const int64_t nnz = ia[n];

@@ -242,9 +242,39 @@ struct KrylovResult {
   int converged = 0;
   int method = -1;        // the method that produced the iterate
   int refinements = 0;    // method 3: FP64 refinement steps
+  double setup_ms = 0;    // method 8: forming the coarse matrix and its inverse
 };
+// Two-level right preconditioner of BiCGStab method 8 (2D): Jacobi plus the
+// Galerkin coarse correction P (P^T A P)^-1 P^T on a lattice coarse grid over
+// the nodes' bounding box, P bilinear per DOF component.  Built by the model
+// (drivers.cpp: twolevel_prepare); the coarse matrix and its inverse are
+// formed on the device for every solve (twolevel_setup).
+struct TwoLevelDev {
+  int nc = 0;                 // coarse DOFs
+  int nxn = 0, nyn = 0;       // coarse nodes per axis
+  int64_t n = 0;              // fine equations
+  const int* pidx = nullptr;  // n * 4: coarse DOF of each bilinear corner
+  const float* pw = nullptr;  // n * 4: weights
+  const int* ecell = nullptr; // n: the equation's cell x | y << 12 | component << 24
+  const int* rptr = nullptr;  // nc + 1: rows of P^T
+  const int* ridx = nullptr;  // fine equation
+  const float* rw = nullptr;  // weight
+  double* B = nullptr;        // n * 32: A P on each row's 4x4-node, 2-component window
+  double* M = nullptr;        // nc x 2 nc: [P^T A P | I], after setup [diagonal | (P^T A P)^-1]
+  double* colk = nullptr;     // nc: reciprocals of the final diagonal
+  double* colbuf = nullptr;   // 2 nc: the pivot column of a step and of the next, contiguous
+  double* diag0 = nullptr;    // nc: the diagonal before elimination
+  double* rpiv = nullptr;     // 2: reciprocal of a step's pivot and of the next
+  double* rc = nullptr;       // nc: restricted vector
+  double* yc = nullptr;       // nc: coarse solution
+  int* ok = nullptr;          // set to 0 when a pivot vanishes
+  // host side: the Gauss-Jordan sequence (2 nc launches on fixed buffers),
+  // captured once as a CUDA graph and replayed for every solve
+  cudaGraphExec_t gj = nullptr;
+};
+cudaError_t twolevel_setup(const DevCsr& A, TwoLevelDev& t, cudaStream_t s, bool* usable);
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
-                         int block_dim, cudaStream_t s, KrylovResult* res);
+                         int block_dim, cudaStream_t s, KrylovResult* res, TwoLevelDev* tl = nullptr);
 cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s);
 
 // Additive second level of a preconditioner: z += C(r) (learned.cpp, k_learned.cu).

@@ -109,7 +109,13 @@ pdx_status solve_device_method(pdx_model* m, const double* b, double* x, int met
   A.ia = m->d_ia;
   A.ja = m->d_ja;
   A.a = m->d_Kval;
-  cudaError_t e = krylov_solve(A, b, x, method, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr);
+  TwoLevelDev* tl = nullptr;
+  if (method == 8) {
+    pdx_status st8 = twolevel_prepare(m);
+    if (st8) return st8;
+    tl = &m->twolevel->dev;
+  }
+  cudaError_t e = krylov_solve(A, b, x, method, m->cmd.solve_tol, m->cmd.solve_maxit, m->mesh.dim, m->stream, kr, tl);
   pdx_status st = cuda_check(e, "Krylov solve");
   if (st) return st;
   int spent = kr->iterations;   // iterations are summed over the fallbacks
@@ -401,8 +407,8 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   if (!m) return set_error(PDX_ERR_INVALID, "null model");
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
-  if (method < 0 || (method > 3 && method < 6) || method > 7)
-    return set_error(PDX_ERR_INVALID, "method must be 0..3, 6 or 7");
+  if (method < 0 || (method > 3 && method < 6) || method > 8)
+    return set_error(PDX_ERR_INVALID, "method must be 0..3 or 6..8");
   if (m->cmd.fail_flag == 1)
     return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   cudaSetDevice(m->device);

@@ -252,7 +252,8 @@ bool read_command(const std::string& path, Command& c, Mesh& m, std::string& bas
       else if (t[1] == "MIXEDPCG") c.solve_method = 3;
       else if (t[1] == "GMRES") c.solve_method = 6;
       else if (t[1] == "MIXEDBICGSTAB") c.solve_method = 7;
-      else return fail(err, 2, "SOLVE must be PCG, BJPCG, BICGSTAB, MIXEDPCG, GMRES or MIXEDBICGSTAB");
+      else if (t[1] == "TWOLEVEL") c.solve_method = 8;
+      else return fail(err, 2, "SOLVE must be PCG, BJPCG, BICGSTAB, MIXEDPCG, GMRES, MIXEDBICGSTAB or TWOLEVEL");
       if (t.size() > 2) c.solve_tol = std::atof(t[2].c_str());
       if (t.size() > 3) c.solve_maxit = std::atoi(t[3].c_str());
     } else {

@@ -13,6 +13,8 @@
 //   method 7  BiCGStab in FP32 inside the same FP64 iterative refinement (the
 //             mixed-precision solve for the unsymmetric stiffness, on which
 //             CG stalls)
+//   method 8  BiCGStab, right preconditioned by Jacobi plus the Galerkin
+//             coarse correction on a lattice coarse grid (2D; TwoLevelDev)
 //
 // Convergence is always judged on the true FP64 residual ||b - A x|| / ||b||.
 // Scalars stay on the device; iterations are launched in chunks and the host
@@ -375,6 +377,179 @@ __global__ void k_bicg_x_rho(int64_t n, const T* ph, const T* shat, const T* s, 
   }
 }
 
+// Two-level preconditioner of method 8 (2D): z = D^-1 v + P (P^T A P)^-1 P^T v
+// with P bilinear per DOF component on a lattice coarse grid (TwoLevelDev).
+// The coarse matrix is formed in two fixed-order passes, so its bits do not
+// depend on scheduling: B = A P on each fine row's window of 4x4 coarse nodes
+// and 2 components (every coupling of a row reaches at most one cell over,
+// which the model checks when it picks the grid), then P^T B on each coarse
+// row's window of 5x5 nodes.
+
+// B[i][s]: one warp per fine row, lane = window slot (x offset -1..2, y
+// offset -1..2, component), the row's entries in CSR order
+__global__ void k_tl_ap(int64_t n, const int64_t* ia, const int* ja, const double* a, TwoLevelDev t) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int s = threadIdx.x & 31;
+  if (row >= n) return;
+  const int q0 = t.ecell[row];   // the row's cell (x, y) and component
+  const int sx = (q0 & 0xfff) + (s & 3) - 1, sy = ((q0 >> 12) & 0xfff) + ((s >> 2) & 3) - 1, sc = s >> 4;
+  double acc = 0;
+  for (int64_t p = ia[row]; p < ia[row + 1]; p++) {
+    const int j = ja[p];
+    const int q = t.ecell[j];
+    const int ex = sx - (q & 0xfff), ey = sy - ((q >> 12) & 0xfff);
+    if ((q >> 24) == sc && (unsigned)ex <= 1u && (unsigned)ey <= 1u)
+      acc += a[p] * (double)t.pw[(int64_t)j * 4 + ex + 2 * ey];
+  }
+  t.B[row * 32 + s] = acc;
+}
+
+// [0 | I]: the augmented matrix before the coarse rows are written
+__global__ void k_tl_init(TwoLevelDev t) {
+  const int64_t w = 2 * (int64_t)t.nc;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < (int64_t)t.nc * w;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = k / w, c = k % w;
+    t.M[k] = c == t.nc + r ? 1.0 : 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *t.ok = 1;
+}
+
+// row I of P^T A P: one block of 64 threads per coarse DOF, thread = slot of
+// the 5x5-node, 2-component window, P^T's row in order
+__global__ void k_tl_coarse(TwoLevelDev t) {
+  const int I = blockIdx.x;
+  const int s = threadIdx.x;
+  if (s >= 50) return;
+  const int nI = I >> 1;
+  const int JX = nI % t.nxn + s % 5 - 2, JY = nI / t.nxn + (s / 5) % 5 - 2, jc = s / 25;
+  if (JX < 0 || JX >= t.nxn || JY < 0 || JY >= t.nyn) return;
+  double acc = 0;
+  for (int k = t.rptr[I]; k < t.rptr[I + 1]; k++) {
+    const int i = t.ridx[k];
+    const int q = t.ecell[i];
+    const int dx = JX - (q & 0xfff) + 1, dy = JY - ((q >> 12) & 0xfff) + 1;
+    if ((unsigned)dx <= 3u && (unsigned)dy <= 3u)
+      acc += (double)t.rw[k] * t.B[(int64_t)i * 32 + jc * 16 + dy * 4 + dx];
+  }
+  t.M[(int64_t)I * 2 * t.nc + (JX + t.nxn * JY) * 2 + jc] = acc;
+}
+
+// Gauss-Jordan elimination of [A_c | I] without pivoting, one launch per
+// column: A_c = P^T A P is symmetric positive definite up to the small
+// unsymmetric part of the PD stiffness, for which elimination in the natural
+// order is stable; a pivot below 1e-10 of its original diagonal clears *ok
+// and the solve runs with Jacobi alone.  Rows are scaled once at the end
+// (the left half ends diagonal), so within a step no thread writes what
+// another reads: step k reads column k (colbuf[k & 1], contiguous) and the
+// reciprocal of its pivot (rpiv[k & 1], one division by one thread of the
+// previous step), and writes column k + 1 and its pivot's reciprocal into
+// the other slots.
+
+// column 0, the original diagonal and the first pivot's reciprocal
+__global__ void k_gj_first(const double* M, int nc, double* colbuf, double* diag0, double* rpiv, int* ok) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nc) return;
+  const int64_t w = 2 * (int64_t)nc;
+  colbuf[r] = M[r * w];
+  diag0[r] = M[r * w + r];
+  if (r == 0) {
+    const double pv = M[0];
+    if (fabs(pv) > 0.0) rpiv[0] = 1.0 / pv;
+    else *ok = 0;
+  }
+}
+
+// M[r][c] -= (M[r][k] / M[k][k]) M[k][c] for r != k and k < c <= k + nc:
+// row k is zero right of column nc + k (the part of I no step has reached
+// yet), so nothing else changes; column k itself is left as it is and never
+// read again
+__global__ void k_gj_step(double* M, int nc, int k, const double* colbuf, double* colbuf_next, const double* rpiv,
+                          double* rpiv_next, const double* diag0, int* ok) {
+  if (*ok == 0) return;
+  const int64_t w = 2 * (int64_t)nc;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nc * nc) return;
+  const int64_t r = t / nc, c = k + 1 + t % nc;
+  double v = M[r * w + c];
+  if (r != k) {
+    const double pk = M[(int64_t)k * w + c];
+    if (pk != 0.0) {
+      const double f = colbuf[r] * rpiv[0];
+      if (f != 0.0) {
+        v -= f * pk;
+        M[r * w + c] = v;
+      }
+    }
+  }
+  if (c == k + 1) {
+    colbuf_next[r] = v;
+    if (r == k + 1) {
+      if (fabs(v) > 1e-10 * fabs(diag0[r])) rpiv_next[0] = 1.0 / v;
+      else *ok = 0;
+    }
+  }
+}
+
+// reciprocals of the final diagonal
+__global__ void k_gj_rdiag(const double* M, int nc, double* rd) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nc) rd[r] = 1.0 / M[(int64_t)r * 2 * nc + r];
+}
+
+// the right half scaled by the rows' reciprocals: the inverse
+__global__ void k_gj_finish(double* M, int nc, const double* rd, const int* ok) {
+  if (*ok == 0) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nc * nc) return;
+  const int64_t r = t / nc, c = t % nc;
+  M[r * 2 * nc + nc + c] *= rd[r];
+}
+
+// rc = P^T v: one block per coarse DOF, P^T's row in order
+__global__ void k_tl_restrict(TwoLevelDev t, const double* v) {
+  __shared__ double sh[kThreads];
+  const int I = blockIdx.x;
+  double acc = 0;
+  for (int k = t.rptr[I] + threadIdx.x; k < t.rptr[I + 1]; k += blockDim.x) acc += (double)t.rw[k] * v[t.ridx[k]];
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) t.rc[I] = acc;
+}
+
+// yc = (P^T A P)^-1 rc: one block of 128 threads per coarse row of the
+// inverse (four warps keep enough loads in flight for a 7 KB row)
+__global__ void __launch_bounds__(128) k_tl_coarse_mv(TwoLevelDev t) {
+  __shared__ double sh[4];
+  const int row = blockIdx.x;
+  const double* Mi = t.M + (int64_t)row * 2 * t.nc + t.nc;
+  double acc = 0;
+  for (int c = threadIdx.x; c < t.nc; c += blockDim.x) acc += Mi[c] * t.rc[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) t.yc[row] = (sh[0] + sh[1]) + (sh[2] + sh[3]);
+}
+
+// z += P yc
+__global__ void k_tl_prolong_add(TwoLevelDev t, double* z) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n) return;
+  double acc = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float w = t.pw[i * 4 + k];
+    if (w != 0.f) acc += (double)w * t.yc[t.pidx[i * 4 + k]];
+  }
+  z[i] += acc;
+}
+
+void twolevel_apply(const TwoLevelDev& t, const double* v, double* z, cudaStream_t s) {
+  k_tl_restrict<<<t.nc, kThreads, 0, s>>>(t, v);
+  k_tl_coarse_mv<<<t.nc, 128, 0, s>>>(t);
+  k_tl_prolong_add<<<(int)((t.n + 255) / 256), 256, 0, s>>>(t, z);
+}
+
 // Fused PCG steps in the precision T of the vectors (reductions as above).
 // partials of p.q; the last block sets alpha = rz / (p.q) (0 if p.q is 0)
 template <typename T>
@@ -678,7 +853,7 @@ int pcg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, co
 template <typename T>
 int bicg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, const T* aT, const T* b, T* x,
               const T* dinv, double rtol, int max_iter, int stall, double* dscal, T* const w[8], double* part2,
-              unsigned* ticket) {
+              unsigned* ticket, const TwoLevelDev* tl = nullptr) {
   cudaStream_t s = c.s;
   T *r = w[0], *r0 = w[1], *v = w[2], *p = w[3], *ss = w[4], *t = w[5], *ph = w[6], *sh = w[7];
   const int g = grid_for(n);
@@ -716,9 +891,15 @@ int bicg_core(Ctx& c, int64_t n, double avg, const int64_t* ia, const int* ja, c
     double* rho_cur = rhos + (it & 1);
     double* rho_next = rhos + ((it + 1) & 1);
     k_bicg_p2<T><<<g, kThreads, 0, s>>>(n, sc.beta_t, sc.omega_t, r, v, dinv, p, ph);
+    if constexpr (std::is_same<T, double>::value) {
+      if (tl) twolevel_apply(*tl, p, ph, s);   // ph += P (P^T A P)^-1 P^T p
+    }
     spmv_t<T>(n, avg, ia, ja, aT, ph, v, s);
     k_bicg_alpha<T><<<gr, kThreads, 0, s>>>(n, r0, v, c.part, ticket, rho_cur, sc);
     k_bicg_s2<T><<<g, kThreads, 0, s>>>(n, sc.alpha_t, r, v, dinv, ss, sh);
+    if constexpr (std::is_same<T, double>::value) {
+      if (tl) twolevel_apply(*tl, ss, sh, s);
+    }
     spmv_t<T>(n, avg, ia, ja, aT, sh, t, s);
     k_bicg_omega<T><<<gr, kThreads, 0, s>>>(n, t, ss, part2, part2 + kRedBlocks, ticket, sc);
     k_bicg_x_rho<T><<<gr, kThreads, 0, s>>>(n, ph, sh, ss, t, r0, x, r, c.part, ticket, rho_cur, rho_next, sc);
@@ -879,8 +1060,44 @@ cudaError_t spmv(const DevCsr& A, const double* x, double* y, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t twolevel_setup(const DevCsr& A, TwoLevelDev& t, cudaStream_t s, bool* usable) {
+  const int nc = t.nc;
+  k_tl_ap<<<(int)((A.n * 32 + 255) / 256), 256, 0, s>>>(A.n, A.ia, A.ja, A.a, t);
+  k_tl_init<<<1024, 256, 0, s>>>(t);
+  k_tl_coarse<<<nc, 64, 0, s>>>(t);
+  auto gauss_jordan = [&]() {
+    k_gj_first<<<(nc + 255) / 256, 256, 0, s>>>(t.M, nc, t.colbuf, t.diag0, t.rpiv, t.ok);
+    for (int k = 0; k < nc; k++) {
+      const int64_t work = (int64_t)nc * nc;
+      k_gj_step<<<(int)((work + 255) / 256), 256, 0, s>>>(t.M, nc, k, t.colbuf + (k & 1) * nc,
+                                                          t.colbuf + ((k + 1) & 1) * nc, t.rpiv + (k & 1),
+                                                          t.rpiv + ((k + 1) & 1), t.diag0, t.ok);
+    }
+    k_gj_rdiag<<<(nc + 255) / 256, 256, 0, s>>>(t.M, nc, t.colk);
+    k_gj_finish<<<(int)(((int64_t)nc * nc + 255) / 256), 256, 0, s>>>(t.M, nc, t.colk, t.ok);
+  };
+  if (!t.gj) {
+    cudaGraph_t graph;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      gauss_jordan();
+      if (cudaStreamEndCapture(s, &graph) == cudaSuccess) {
+        if (cudaGraphInstantiate(&t.gj, graph, 0) != cudaSuccess) t.gj = nullptr;
+        cudaGraphDestroy(graph);
+      }
+    }
+    cudaGetLastError();
+  }
+  if (t.gj) cudaGraphLaunch(t.gj, s);
+  else gauss_jordan();
+  int ok = 0;
+  cudaMemcpyAsync(&ok, t.ok, sizeof(int), cudaMemcpyDeviceToHost, s);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  *usable = e == cudaSuccess && ok != 0;
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,
-                         int block_dim, cudaStream_t s, KrylovResult* res) {
+                         int block_dim, cudaStream_t s, KrylovResult* res, TwoLevelDev* tl) {
   const int64_t n = A.n;
   const double avg = n ? (double)A.nnz / (double)n : 0.0;
   Ctx c{s, nullptr};
@@ -920,13 +1137,33 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
   if (method == 0 || method == 1) {
     iters = pcg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, nb, bptr, binv, rtol, max_iter, dscal, r, z,
                              p, q, ticket, true);
-  } else if (method == 2) {
-    // BiCGStab, right Jacobi preconditioning, from the caller's x
+  } else if (method == 2 || method == 8) {
+    // BiCGStab, right Jacobi preconditioning, from the caller's x; method 8
+    // adds the Galerkin coarse correction (the coarse matrix and its inverse
+    // are formed here, for this matrix; Jacobi alone if a pivot vanished)
+    bool two_level = false;
+    if (method == 8 && tl) {
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, s);
+      const cudaError_t e = twolevel_setup(A, *tl, s, &two_level);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      res->setup_ms = ms;
+      if (e != cudaSuccess) return e;
+    }
     double* w[8] = {r, nullptr, nullptr, p, nullptr, nullptr, nullptr, nullptr};
     for (int k : {1, 2, 4, 5, 6, 7}) cudaMallocAsync(&w[k], n * sizeof(double), s);
     double* part2 = nullptr;
     cudaMallocAsync(&part2, 2 * kRedBlocks * sizeof(double), s);
-    iters = bicg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, rtol, max_iter, 0, dscal, w, part2, ticket);
+    iters = bicg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, rtol, max_iter, 0, dscal, w, part2, ticket,
+                              two_level ? tl : nullptr);
+    if (method == 8 && !two_level) method = 2;
     cudaFreeAsync(part2, s);
     for (int k : {1, 2, 4, 5, 6, 7}) cudaFreeAsync(w[k], s);
   } else if (method == 3 || method == 7) {

@@ -172,6 +172,11 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
   const int maxit = m->cmd.solve_maxit;
   const int bd = m->mesh.dim;
   Learned* L = m->learned;
+  if (method == 8) {
+    const pdx_status st8 = twolevel_prepare(m);
+    if (st8) return st8;
+    return cuda_check(krylov_solve(A, b, x, 8, tol, maxit, bd, m->stream, kr, &m->twolevel->dev), "Krylov solve");
+  }
   if (method <= 3 || method >= 6) return cuda_check(krylov_solve(A, b, x, method, tol, maxit, bd, m->stream, kr), "Krylov solve");
   if (method == 4) return plain_solve(m, b, x, collect ? L : nullptr, kr);
   if (!L || !L->trained) return set_error(PDX_ERR_INVALID, "learned preconditioner not set up and trained");
@@ -195,6 +200,98 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
 }
 
 }  // namespace
+
+// Coarse grid of the two-level BiCGStab (method 8): kTwoLevelCells cells per
+// axis over the nodes' bounding box, fewer where a coupling of the matrix (a
+// bond or an element) is longer than a cell, so that every row's couplings
+// stay within one cell of its own (the windows of k_tl_ap and k_tl_coarse).
+// On C3's loaded increment (320k equations) a numpy study of the exact
+// Galerkin correction gave 95 BiCGStab iterations with 20x20 cells, 60 with
+// 40x40 and 40 with 80x80, against 1,835 with Jacobi; 20x20 keeps the
+// coarse inverse (882 DOFs) a few milliseconds to form.
+constexpr int kTwoLevelCells = 20;
+
+pdx_status twolevel_prepare(pdx_model* m) {
+  if (m->twolevel) return PDX_OK;
+  if (m->mesh.dim != 2) return set_error(PDX_ERR_UNSUPPORTED, "method 8 (two-level BiCGStab) is built for 2D models");
+  const int N = m->mesh.n_node;
+  const int64_t n = m->setup.n_eq;
+  const std::vector<double>& X = m->mesh.X;
+  std::vector<int> eq_node((size_t)n, 0);
+  for (int k = 0; k < N; k++)
+    for (int i = 0; i < 2; i++) {
+      const int e = m->setup.eq[(size_t)k * 2 + i];
+      if (e >= 0) eq_node[e] = k;
+    }
+  double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300}, reach[2] = {0.0, 0.0};
+  for (int k = 0; k < N; k++)
+    for (int a = 0; a < 2; a++) {
+      lo[a] = std::min(lo[a], X[(size_t)k * 3 + a]);
+      hi[a] = std::max(hi[a], X[(size_t)k * 3 + a]);
+    }
+  const std::vector<int64_t>& ia = m->setup.csr_ia;
+  const std::vector<int64_t>& ja = m->setup.csr_ja;
+  for (int64_t r = 0; r < n && (size_t)r + 1 < ia.size(); r++) {
+    const int kr = eq_node[r];
+    for (int64_t p = ia[r]; p < ia[r + 1]; p++) {
+      const int kc = eq_node[ja[p]];
+      for (int a = 0; a < 2; a++) reach[a] = std::max(reach[a], std::fabs(X[(size_t)kr * 3 + a] - X[(size_t)kc * 3 + a]));
+    }
+  }
+  int cells[3] = {1, 1, 0};
+  for (int a = 0; a < 2; a++) {
+    const double len = hi[a] - lo[a];
+    if (len > 0 && reach[a] > 0)
+      cells[a] = std::max(1, std::min(kTwoLevelCells, (int)std::floor(len / (1.001 * reach[a]))));
+  }
+  std::vector<int> pidx, rptr, ridx;
+  std::vector<float> pw, rw, aw;
+  int nc = 0, np = 0, cells_out[3] = {0, 0, 0};
+  build_coarse(m, cells, pidx, pw, rptr, ridx, rw, aw, nc, np, cells_out);
+  std::vector<int> ecell((size_t)n, 0);
+  for (int64_t e = 0; e < n; e++) {
+    const int q = pidx[(size_t)e * 4];   // corner 0: the cell's lower-left coarse node and the component
+    const int node = q >> 1;
+    ecell[e] = (node % (cells_out[0] + 1)) | ((node / (cells_out[0] + 1)) << 12) | ((q & 1) << 24);
+  }
+  TwoLevelHost* T = new TwoLevelHost();
+  m->twolevel = T;
+  TwoLevelDev& t = T->dev;
+  cudaStream_t s = m->stream;
+  t.nc = nc;
+  t.nxn = cells_out[0] + 1;
+  t.nyn = cells_out[1] + 1;
+  t.n = n;
+  t.pidx = dev_upload(T->buf, pidx, s);
+  t.pw = dev_upload(T->buf, pw, s);
+  t.ecell = dev_upload(T->buf, ecell, s);
+  t.rptr = dev_upload(T->buf, rptr, s);
+  t.ridx = dev_upload(T->buf, ridx, s);
+  t.rw = dev_upload(T->buf, rw, s);
+  t.B = T->buf.alloc<double>((size_t)n * 32);
+  t.M = T->buf.alloc<double>((size_t)nc * 2 * nc);
+  t.colk = T->buf.alloc<double>(nc);
+  t.colbuf = T->buf.alloc<double>(2 * (size_t)nc);
+  t.diag0 = T->buf.alloc<double>(nc);
+  t.rpiv = T->buf.alloc<double>(2);
+  t.rc = T->buf.alloc<double>(nc);
+  t.yc = T->buf.alloc<double>(nc);
+  t.ok = T->buf.alloc<int>(1);
+  const pdx_status st = cuda_check(cudaStreamSynchronize(s), "two-level set-up");   // host arrays leave scope
+  if (st || !t.pidx || !t.pw || !t.ecell || !t.rptr || !t.ridx || !t.rw || !t.B || !t.M || !t.colk || !t.colbuf || !t.diag0 || !t.rpiv || !t.rc || !t.yc || !t.ok) {
+    twolevel_destroy(m);
+    return st ? st : set_error(PDX_ERR_CUDA, "two-level set-up: device allocation failed");
+  }
+  return PDX_OK;
+}
+
+void twolevel_destroy(pdx_model* m) {
+  if (!m->twolevel) return;
+  if (m->twolevel->dev.gj) cudaGraphExecDestroy(m->twolevel->dev.gj);
+  m->twolevel->buf.free_all();
+  delete m->twolevel;
+  m->twolevel = nullptr;
+}
 
 void learned_destroy(pdx_model* m) {
   if (!m->learned) return;
@@ -492,7 +589,7 @@ pdx_status pdx_newmark_init(pdx_model* m) {
 pdx_status pdx_newmark_step(pdx_model* m, int method, int collect, pdx_solve_info* info) {
   NEED_DEV(m);
   if (!m->newmark_ready) return set_error(PDX_ERR_INVALID, "pdx_newmark_init first");
-  if (method < 0 || method > 7) return set_error(PDX_ERR_INVALID, "method must be 0..7");
+  if (method < 0 || method > 8) return set_error(PDX_ERR_INVALID, "method must be 0..8");
   const int ne = m->setup.n_eq;
   double* u_all = m->d_u[0];
   double* upred = m->d_u[1];

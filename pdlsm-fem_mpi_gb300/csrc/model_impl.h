@@ -103,6 +103,12 @@ struct DevBuf {
 
 struct Learned;
 
+// The coarse grid of the two-level BiCGStab (method 8) of a 2D model.
+struct TwoLevelHost {
+  DevBuf buf;
+  TwoLevelDev dev;
+};
+
 }  // namespace pdx
 
 struct pdx_model {
@@ -184,6 +190,7 @@ struct pdx_model {
   double* d_acc = nullptr;
   bool newmark_ready = false;
   pdx::Learned* learned = nullptr;
+  pdx::TwoLevelHost* twolevel = nullptr;   // built at the first method-8 solve
   int cur = 0;                       // index of the buffer holding u_n
   int64_t steps_done = 0;
   // explicit runs apply a step's FC 3 failure pass at the start of the next
@@ -213,6 +220,9 @@ extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);
 bool merge_batch(const std::vector<pdx_model*>& parts, pdx_model* out, Error& err);
 void learned_destroy(pdx_model* m);
+// method 8's coarse grid for the model (2D only), built once
+pdx_status twolevel_prepare(pdx_model* m);
+void twolevel_destroy(pdx_model* m);
 inline void fill_solve_info(pdx_solve_info* info, const KrylovResult& kr, double seconds) {
   if (!info) return;
   info->iterations = kr.iterations;
@@ -221,5 +231,6 @@ inline void fill_solve_info(pdx_solve_info* info, const KrylovResult& kr, double
   info->converged = kr.converged;
   info->method_used = kr.method;
   info->refinements = kr.refinements;
+  info->setup_seconds = kr.setup_ms * 1e-3;
 }
 }  // namespace pdx

@@ -45,7 +45,8 @@ class SolveOpts(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("seconds", C.c_double),
-                ("converged", C.c_int), ("method_used", C.c_int), ("refinements", C.c_int)]
+                ("converged", C.c_int), ("method_used", C.c_int), ("refinements", C.c_int),
+                ("setup_seconds", C.c_double)]
 
 
 EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_model_destroy",

@@ -431,7 +431,7 @@ def test_element_path_and_lane_counts_match_oracle(built, lanes, fe_lanes):
     assert int((bs32 != bs_o).sum()) <= max(2, int(0.01 * (bs_o == 0).sum()))
 
 
-@pytest.mark.parametrize("method", [1, 2, 3, 6, 7])
+@pytest.mark.parametrize("method", [1, 2, 3, 6, 7, 8])
 def test_quasi_static_increments_match_reference(built, method):
     """Three quasi-static increments, one pdx_quasi_step each, against the
     reference's direct-solve trajectory: the Krylov solves stop at a 1e-8 true
