@@ -205,10 +205,11 @@ pdx_status solve_newmark_system(pdx_model* m, int method, bool collect, double* 
 // axis over the nodes' bounding box, fewer where a coupling of the matrix (a
 // bond or an element) is longer than a cell, so that every row's couplings
 // stay within one cell of its own (the windows of k_tl_ap and k_tl_coarse).
-// On C3's loaded increment (320k equations) a numpy study of the exact
-// Galerkin correction gave 95 BiCGStab iterations with 20x20 cells, 60 with
-// 40x40 and 40 with 80x80, against 1,835 with Jacobi; 20x20 keeps the
-// coarse inverse (882 DOFs) a few milliseconds to form.
+// On C3's loaded increment (320k equations) the exact Galerkin correction
+// gives 168 BiCGStab iterations with 10x10 cells, 132 with 14x14, 95 with
+// 20x20, 83 with 28x28 and 60 with 40x40, against 1,835 with Jacobi
+// (oracle/twolevel_study.py); 20x20 keeps the coarse inverse (882 DOFs) a
+// few milliseconds to form.
 constexpr int kTwoLevelCells = 20;
 
 pdx_status twolevel_prepare(pdx_model* m) {
