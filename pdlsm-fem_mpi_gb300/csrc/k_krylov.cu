@@ -394,6 +394,7 @@ __global__ void k_tl_ap(int64_t n, const int64_t* ia, const int* ja, const doubl
   const int q0 = t.ecell[row];   // the row's cell (x, y) and component
   const int sx = (q0 & 0xfff) + (s & 3) - 1, sy = ((q0 >> 12) & 0xfff) + ((s >> 2) & 3) - 1, sc = s >> 4;
   double acc = 0;
+#pragma unroll 4
   for (int64_t p = ia[row]; p < ia[row + 1]; p++) {
     const int j = ja[p];
     const int q = t.ecell[j];
