@@ -417,7 +417,9 @@ __global__ void k_tl_init(TwoLevelDev t) {
 }
 
 // row I of P^T A P: one block of 64 threads per coarse DOF, thread = slot of
-// the 5x5-node, 2-component window, P^T's row in order
+// the 5x5-node, 2-component window, P^T's row in order.  A coarse DOF with no
+// free fine equation in its support (a hole, prescribed DOFs only) gets a
+// unit diagonal: its restricted residual is always zero, so it stays zero.
 __global__ void k_tl_coarse(TwoLevelDev t) {
   const int I = blockIdx.x;
   const int s = threadIdx.x;
@@ -425,6 +427,10 @@ __global__ void k_tl_coarse(TwoLevelDev t) {
   const int nI = I >> 1;
   const int JX = nI % t.nxn + s % 5 - 2, JY = nI / t.nxn + (s / 5) % 5 - 2, jc = s / 25;
   if (JX < 0 || JX >= t.nxn || JY < 0 || JY >= t.nyn) return;
+  if (t.rptr[I] == t.rptr[I + 1]) {
+    if (s == 12 + 25 * (I & 1)) t.M[(int64_t)I * 2 * t.nc + I] = 1.0;   // the diagonal slot
+    return;
+  }
   double acc = 0;
   for (int k = t.rptr[I]; k < t.rptr[I + 1]; k++) {
     const int i = t.ridx[k];
