@@ -268,9 +268,13 @@ struct TwoLevelDev {
   double* rc = nullptr;       // nc: restricted vector
   double* yc = nullptr;       // nc: coarse solution
   int* ok = nullptr;          // set to 0 when a pivot vanishes
+  unsigned long long* hash = nullptr;   // fingerprint of the matrix values (device word)
   // host side: the Gauss-Jordan sequence (2 nc launches on fixed buffers),
   // captured once as a CUDA graph and replayed for every solve
   cudaGraphExec_t gj = nullptr;
+  // host side: the fingerprint of the values whose coarse inverse M holds
+  bool have_inverse = false;
+  unsigned long long inverse_of = 0;
 };
 cudaError_t twolevel_setup(const DevCsr& A, TwoLevelDev& t, cudaStream_t s, bool* usable);
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,

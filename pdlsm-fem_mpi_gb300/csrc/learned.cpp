@@ -278,8 +278,9 @@ pdx_status twolevel_prepare(pdx_model* m) {
   t.rc = T->buf.alloc<double>(nc);
   t.yc = T->buf.alloc<double>(nc);
   t.ok = T->buf.alloc<int>(1);
+  t.hash = T->buf.alloc<unsigned long long>(1);
   const pdx_status st = cuda_check(cudaStreamSynchronize(s), "two-level set-up");   // host arrays leave scope
-  if (st || !t.pidx || !t.pw || !t.ecell || !t.rptr || !t.ridx || !t.rw || !t.B || !t.M || !t.colk || !t.colbuf || !t.diag0 || !t.rpiv || !t.rc || !t.yc || !t.ok) {
+  if (st || !t.pidx || !t.pw || !t.ecell || !t.rptr || !t.ridx || !t.rw || !t.B || !t.M || !t.colk || !t.colbuf || !t.diag0 || !t.rpiv || !t.rc || !t.yc || !t.ok || !t.hash) {
     twolevel_destroy(m);
     return st ? st : set_error(PDX_ERR_CUDA, "two-level set-up: device allocation failed");
   }
