@@ -513,17 +513,20 @@ def test_reaction_forces_match_reference(built, tmp_path):
     assert last[0] == 60 and abs(last[3] - g[-1, 3]) <= 1e-5 * abs(g[-1, 3])
 
 
-def test_fc2_in_newmark_steps_matches_reference(built):
+@pytest.mark.parametrize("method", [2, 8])
+def test_fc2_in_newmark_steps_matches_reference(built, method):
     """FC 2 after every Newmark step (10 steps, sigma_ult 3e7), the reference
-    solving K_N directly and this build with BiCGStab to 1e-13: displacement
-    trajectory and the broken-bond set."""
+    solving K_N directly and this build with BiCGStab (method 2) or the
+    two-level BiCGStab (method 8, its coarse inverse formed again whenever
+    FC 2 has changed K) to 1e-13: displacement trajectory and the
+    broken-bond set."""
     g = golden("p21_nmfc2")
     with pdx.Model(case_cmd("p21", "p21_nmfc2"), device=0, precision=0) as m:
         m.newmark_init()
         worst = 0.0
         for i in range(10):
-            info = m.newmark_step(2)
-            assert info.converged
+            info = m.newmark_step(method)
+            assert info.converged and info.method_used == method
             u, _, _, bs = m.state()
             worst = max(worst, rel(u, g["u_traj"][i]))
     print(f"\n[p21_nmfc2] worst displacement error {worst:.2e}, "
