@@ -244,6 +244,24 @@ def test_c3_fifty_increments_and_direct_solve(built):
     e2, e50 = rel(du_eq(u2), xd), rel(du_eq(u.reshape(-1)), xd)
     print(f"    increment 2 vs direct {e2:.2e}, after 50 increments {e50:.2e}")
     assert e50 <= e2 * 1.01
+    # the same 50 increments with the two-level BiCGStab (method 8): every
+    # increment converges, nothing is cut, and the final state is as close to
+    # the direct solution of the loaded increment as BiCGStab's
+    with pdx.Model(cmd, device=0, precision=0) as m8:
+        m8.quasi_init()
+        t0 = time.perf_counter()
+        its8 = []
+        for k in range(50):
+            info = m8.quasi_step(8)
+            assert info.converged and info.rel_residual <= 1e-8 and info.method_used == 8
+            its8.append(info.iterations)
+        t8 = time.perf_counter() - t0
+        u8, _, _, bs8 = m8.state()
+    e50_8 = rel(du_eq(u8.reshape(-1)), xd)
+    print(f"    two-level: 50 increments in {t8:.1f} s ({sum(its8)} iterations), after 50 increments {e50_8:.2e} "
+          f"from the direct solution")
+    np.testing.assert_array_equal(bs8, bs)
+    assert e50_8 <= max(e50, e2) * 1.5
 
 
 @pytest.mark.gpu
