@@ -11,9 +11,10 @@ product does), and counts SciPy BiCGStab iterations to 1e-8 with Jacobi alone
 and with Jacobi plus the exact Galerkin correction P (P^T K P)^-1 P^T
 (additive, dense LU of the coarse matrix) for each coarse grid given.
 
-    python oracle/twolevel_study.py [20x20 40x40 ...] [--no-jacobi]
+    python oracle/twolevel_study.py [20x20 40x40 ...] [--no-jacobi] [--n 401]
 
-Prints one JSON line per preconditioner.
+--n sets the plate's nodes per side (the C3 configuration has 401).  Prints
+one JSON line per preconditioner.
 """
 from __future__ import annotations
 
@@ -61,10 +62,16 @@ def prolongation2d(X: np.ndarray, eq: np.ndarray, cells, n: int) -> sp.csr_matri
 
 
 def main() -> None:
-    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    argv = sys.argv[1:]
+    nside = 401
+    if "--n" in argv:
+        i = argv.index("--n")
+        nside = int(argv[i + 1])
+        del argv[i:i + 2]
+    args = [a for a in argv if not a.startswith("--")]
     cells_list = [tuple(int(c) for c in a.split("x")) for a in args] or [(20, 20)]
     d = tempfile.mkdtemp(prefix="pdx_twolevel_")
-    mesh, kw = meshgen.config_c3(nsteps=2)
+    mesh, kw = meshgen.config_c3(n=nside, nsteps=2)
     cmd = meshgen.write_case(mesh, d, "c3", **kw)
     host = pdx.Model(cmd, device=-1)
     o = orc.Oracle(host)
