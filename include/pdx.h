@@ -145,6 +145,25 @@ int64_t pdx_explicit_step_count(const pdx_model* m);
  * and Newmark steps 1..n (row 0 stays zero).  *count = rows recorded; rows
  * (max_rows x 4) may be NULL. */
 pdx_status pdx_reaction_forces(const pdx_model* m, double* rows, int64_t max_rows, int64_t* count);
+/* FC 1 crack state (2D models with FC 1; replaces the crack-path rows the
+ * reference writes to <title>_cp.out, pdsolve.cpp:7481-7489, and its
+ * cdp_crack array).  One row of 8 doubles per pre-existing crack: the current
+ * segment (x0, y0, x1, y1; x1, y1 the tip, x0, y0 the tip before the last
+ * growth) and the last evaluation's KI, KII, Keq and 1 if the tip then moved
+ * (0 otherwise).  pdx_quasi_step evaluates the cracks after every increment
+ * (and in quasi-static runs grows the PD region behind a moved tip); a
+ * static run evaluates them once.  *n_cracks = number of cracks; rows
+ * (max_cracks x 8) may be NULL. */
+pdx_status pdx_crack_state(const pdx_model* m, double* rows, int max_cracks, int* n_cracks);
+/* One FC 1 growth step with tips given by the caller (2D; a model without a
+ * device too): every crack k with moved[k] != 0 gets the segment from its
+ * current tip to (tips[2k], tips[2k+1]); then, as after a moved tip in a
+ * quasi-static increment (updateEnrichRegion and updateBondstate,
+ * pdsolve.cpp:8871-9004), the elements those segments cut (and the FE
+ * elements within me * min_delta of them) become PD, new PD nodes get
+ * families after the existing ones, and every bond crossing a new segment
+ * breaks.  The set-up arrays (pdx_model_array) and the device model follow. */
+pdx_status pdx_crack_advance(pdx_model* m, const double* tips, const uint8_t* moved);
 
 /* Current state: u_all (N*d), node stress sigma (N*6, slots xx yy zz xy yz zx as
  * calGlobalNodeStresses pdsolve.cpp:9540-9604), damage phi (N, calLocalDamage

@@ -15,6 +15,8 @@
 //   ref_driver explicit_fc2 <cmd.in> <outdir> <every>  (FC 2 after every step)
 //   ref_driver newmark_fc2  <cmd.in> <outdir>          (Newmark with FC 2 after every step)
 //   ref_driver quasi_fc2    <cmd.in> <outdir>          (quasi-static with FC 2 and its load ratio)
+//   ref_driver quasi_fc1    <cmd.in> <outdir>          (quasi-static with FC 1: SIFs, crack growth,
+//                                                       PD-region growth and its load ratio)
 //   ref_driver solve    <cmd.in>             (the reference's own pdfemSolver)
 //
 // Every loop below calls the reference's member functions in the order its own
@@ -425,7 +427,10 @@ void run_newmark(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   out.f64("sigma_final", node_sigma(d), {(long long)N, 6});
 }
 
-void run_quasi(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
+// fc: 0 no failure step, 2 FC 2, 1 FC 1 (the deck's failure flag decides
+// which criterion failureProcess applies; fc only selects the dumps)
+void run_quasi(datModel& d, pdsolve& sol, Dumper& out, int fc = 0) {
+  const bool fc2 = fc != 0;
   d.ci_solvFlag = 2;
   int neq = num_eq(d);
   int nsteps = d.getnumTstep();
@@ -450,6 +455,11 @@ void run_quasi(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   const std::string rf_path = out.dir + "/rf.txt";
   std::ofstream rf_out, crack_out;
   if (rf) { rf_out.open(rf_path); rf_out << std::setprecision(17); }
+  // FC 1: the crack-path rows the reference writes (crack, tip x, tip y, KI,
+  // KII, Keq) at full precision, and the PD-region size after each increment
+  const std::string cp_path = out.dir + "/cp.txt";
+  std::vector<double> fc1_rows;   // n_pde, n_fam, addLoad, rati per increment
+  if (fc == 1) { crack_out.open(cp_path); crack_out << std::setprecision(17) << std::scientific; }
   for (int n = 1; n < nsteps + 1; n++) {
     sol.pdfemQuasiStaticAssembleEquasSys_CSRformat(d, neq, addLoad);
     if (n == 1 || n == 2) {
@@ -468,6 +478,12 @@ void run_quasi(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
       sol.calGlobalNodeStresses(d);
       rati = sol.failureProcess(d, d.ci_topk, addLoad, crack_out);
       if (rf) sol.calReacForc(d, rf_out, n);
+      if (fc == 1) {
+        fc1_rows.push_back((double)d.civ_pdeIDX.size());
+        fc1_rows.push_back((double)d.getTotnumFami());
+        fc1_rows.push_back(addLoad ? 1.0 : 0.0);
+        fc1_rows.push_back(rati);
+      }
     }
     std::vector<double> u = all_dof_values(d);
     traj.insert(traj.end(), u.begin(), u.end());
@@ -486,6 +502,29 @@ void run_quasi(datModel& d, pdsolve& sol, Dumper& out, bool fc2 = false) {
   if (fc2) {
     out.f64("u_after", traj_after, {(long long)nsteps, (long long)N, (long long)D});
     out.i64("bond_state_final", bond_states(d));
+    if (fc == 1) {
+      crack_out.close();
+      std::ifstream in(cp_path);
+      std::vector<double> cp;
+      std::string tok;
+      while (in >> tok)
+        if (tok != "\"***\"") cp.push_back(std::strtod(tok.c_str(), nullptr));
+      const long long nc = d.ci_numCrack;
+      out.f64("crack_rows", cp, {(long long)nsteps, nc, 6});
+      out.f64("region_rows", fc1_rows, {(long long)nsteps, 4});
+      std::vector<long long> pde(d.civ_pdeIDX.begin(), d.civ_pdeIDX.end());
+      out.i64("pde_final", pde);
+      std::vector<long long> fnode, foff(1, 0), fmem;
+      for (int f = 0; f < d.getTotnumFami(); f++) {
+        pdFamily* p = d.op_getFami(f);
+        fnode.push_back(p->getNodeID(0) - 1);
+        for (int m = 0; m < p->getNumNode(); m++) fmem.push_back(p->getNodeID(m) - 1);
+        foff.push_back((long long)fmem.size());
+      }
+      out.i64("fam_node_final", fnode);
+      out.i64("fam_off_final", foff);
+      out.i64("fam_members_final", fmem);
+    }
     if (rf) {
       rf_out.close();
       std::ifstream in(rf_path);
@@ -536,7 +575,8 @@ int main(int argc, char** argv) {
   else if (mode == "newmark") run_newmark(dat, sol, out);
   else if (mode == "newmark_fc2") run_newmark(dat, sol, out, true);
   else if (mode == "quasi") run_quasi(dat, sol, out);
-  else if (mode == "quasi_fc2") run_quasi(dat, sol, out, true);
+  else if (mode == "quasi_fc2") run_quasi(dat, sol, out, 2);
+  else if (mode == "quasi_fc1") run_quasi(dat, sol, out, 1);
   else { std::fprintf(stderr, "unknown mode %s\n", mode.c_str()); return 2; }
   return 0;
 }

@@ -204,6 +204,10 @@ static pdx_status upload_model(pdx_model* m) {
     m->d_fc2_fam = m->buf.alloc<int>(m->fc2_cap);
     m->d_fc2_count = m->buf.alloc<int>(1);
     m->d_fc2_max = m->buf.alloc<double>(1);
+  }
+  // the varying EBCs' velocities, for the load-ratio step of FC 1 and FC 2
+  // quasi-static runs
+  if (m->fc2 || (m->cmd.fail_flag == 1 && D == 2 && m->batch.empty())) {
     std::vector<double> vel((size_t)N * 3, 0.0);
     for (const EssentialBC& b : me.ebcs)
       if (b.varying)
@@ -312,6 +316,57 @@ static pdx_status upload_model(pdx_model* m) {
                                            std::to_string(m->setup.fam_node[f] + 1) + ") is singular");
   }
   return PDX_OK;
+}
+
+pdx_status rebuild_device(pdx_model* m) {
+  const size_t nd = (size_t)m->mesh.n_node * m->mesh.dim;
+  std::vector<double> u(nd), sig((size_t)m->mesh.n_node * 6), rf;
+  cudaMemcpyAsync(u.data(), m->d_u[0], nd * 8, cudaMemcpyDeviceToHost, m->stream);
+  cudaMemcpyAsync(sig.data(), m->d_sigma, sig.size() * 8, cudaMemcpyDeviceToHost, m->stream);
+  if (m->rf && m->d_rf_hist) {
+    rf.resize((size_t)m->rf_cap * 4);
+    cudaMemcpyAsync(rf.data(), m->d_rf_hist, rf.size() * 8, cudaMemcpyDeviceToHost, m->stream);
+  }
+  pdx_status st = cuda_check(cudaStreamSynchronize(m->stream), "state before rebuild");
+  if (st) return st;
+  if (m->graph) {
+    cudaGraphExecDestroy(m->graph);
+    m->graph = nullptr;
+  }
+  learned_destroy(m);
+  twolevel_destroy(m);
+  m->buf.free_all();
+  m->d_vel = m->d_acc = nullptr;
+  m->newmark_ready = false;
+  m->prep = Prepared();
+  Error err{0, ""};
+  if (!prepare_model(m, err)) return set_error(err.code == 6 ? PDX_ERR_SINGULAR : PDX_ERR_PARSE, err.msg);
+  st = upload_model(m);
+  if (st) return st;
+  for (int i = 0; i < 2; i++) cudaMemcpyAsync(m->d_u[i], u.data(), nd * 8, cudaMemcpyHostToDevice, m->stream);
+  cudaMemcpyAsync(m->d_sigma, sig.data(), sig.size() * 8, cudaMemcpyHostToDevice, m->stream);
+  if (!rf.empty() && m->d_rf_hist)
+    cudaMemcpyAsync(m->d_rf_hist, rf.data(), rf.size() * 8, cudaMemcpyHostToDevice, m->stream);
+  m->cur = 0;
+  return cuda_check(cudaStreamSynchronize(m->stream), "device rebuild");
+}
+
+pdx_status upload_bond_states(pdx_model* m) {
+  const Setup& s = m->setup;
+  Prepared& p = m->prep;
+  const int nf = (int)s.fam_node.size();
+  std::fill(p.state_bits.begin(), p.state_bits.end(), 0u);
+  p.fam_intact.assign(nf, 0);
+  for (int f = 0; f < nf; f++)
+    for (int64_t q = s.fam_off[f] + 1; q < s.fam_off[f + 1]; q++)
+      if (s.bond_state[q]) {
+        const int64_t b = p.fam_ptr[f] + (q - s.fam_off[f] - 1);
+        p.state_bits[b >> 5] |= 1u << (b & 31);
+        p.fam_intact[f]++;
+      }
+  cudaMemcpyAsync(m->d_state, p.state_bits.data(), p.state_bits.size() * 4, cudaMemcpyHostToDevice, m->stream);
+  cudaMemcpyAsync(m->d_intact, p.fam_intact.data(), p.fam_intact.size() * 4, cudaMemcpyHostToDevice, m->stream);
+  return cuda_check(cudaStreamSynchronize(m->stream), "bond state upload");
 }
 
 pdx_status model_stress(pdx_model* m, const double* d_u_all, bool sigma, bool phi) {
@@ -553,6 +608,8 @@ pdx_status pdx_model_create_from_cmd(const char* cmd_path, const pdx_options* op
 // set-up is complete; deletes the model on failure.
 static pdx_status finish_create(pdx_model* m, const pdx_options& o, pdx_model** out) {
   m->mixed = o.precision >= 0 ? o.precision : m->cmd.precision;
+  m->cracks = m->mesh.cracks;
+  m->crack_sif.assign(m->cracks.size(), {0.0, 0.0, 0.0, 0.0});
   m->verbose = o.verbose;
   // Lanes per family / per FE-only node: given (> 0), the fixed default (0),
   // or timed on this model by pdx_explicit_init (< 0, autotune_lanes).  The
@@ -1088,6 +1145,19 @@ pdx_status pdx_reaction_forces(const pdx_model* m, double* rows, int64_t max_row
   cudaSetDevice(m->device);
   cudaMemcpyAsync(rows, m->d_rf_hist, (size_t)std::min(n, max_rows) * 4 * 8, cudaMemcpyDeviceToHost, m->stream);
   return cuda_check(cudaStreamSynchronize(m->stream), "reaction forces");
+}
+
+pdx_status pdx_crack_state(const pdx_model* m, double* rows, int max_cracks, int* n_cracks) {
+  if (!m) return set_error(PDX_ERR_INVALID, "null model");
+  const int n = (int)m->cracks.size();
+  if (n_cracks) *n_cracks = n;
+  for (int k = 0; rows && k < n && k < max_cracks; k++) {
+    const auto& c = m->cracks[k];
+    const auto& f = m->crack_sif[k];
+    const double r[8] = {c[0], c[1], c[3], c[4], f[0], f[1], f[2], f[3]};
+    std::memcpy(rows + (size_t)k * 8, r, sizeof r);
+  }
+  return PDX_OK;
 }
 
 pdx_status pdx_get_state(pdx_model* m, double* u_all, double* sigma, double* phi, uint8_t* bond_state) {

@@ -183,6 +183,21 @@ cudaError_t launch_force(const ForceArgs& a, cudaStream_t s);
 // (3D records name the neighbour of the bond 2 * lanes further on)
 cudaError_t launch_pack_bonds(const DevView& v, float pertf, int lanes, float4* rec, cudaStream_t s);
 cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
+// FC 1 sample points of the interaction-integral path (2D): per point
+// {kind, n0, n1, n2, n3}; kind 0 is an FE element evaluated at its centre
+// (nodes n0..n3, a triangle repeats its third node), kind 1 a PD node n0 of
+// family n1.  Writes per point the displacement gradient (dux/dx, duy/dy,
+// dux/dy, duy/dx) and the stress (xx, yy, xy): 7 doubles.
+struct Fc1PointArgs {
+  DevView v;
+  const double* u;          // n_node * 2
+  const double* sigma;      // n_node * 6 node stresses
+  const double* D;          // 3 x 3 constitutive matrix
+  const int* pts;           // 5 per point
+  int n_pts;
+  double* out;              // 7 per point
+};
+cudaError_t launch_fc1_points(const Fc1PointArgs& a, cudaStream_t s);
 cudaError_t launch_assemble(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_newmark_predict(const DevView& v, const double* u, const double* vel, const double* acc,
                                    double dt, double beta, double* upred, cudaStream_t s);

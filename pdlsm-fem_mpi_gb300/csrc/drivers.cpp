@@ -215,6 +215,13 @@ pdx_status run_static(pdx_model* m, const std::string& dir) {
   if (st) return st;
   (void)N; (void)D;
   std::printf("static solve: %d iterations, relative residual %.3e\n", kr.iterations, kr.rel_residual);
+  if (m->cmd.fail_flag == 1 && m->mesh.dim == 2) {
+    // the static solver's failure pass (pdsolve.cpp:5637): SIFs of every
+    // crack, printed as the reference prints them with solver flag 1
+    st = fc1_pass(m, false);
+    if (st) return st;
+    for (const auto& f : m->crack_sif) std::printf("KI= %e, KII=%e, Keq=%e\n", f[0], f[1], f[2]);
+  }
   write_vtk(m, out_name(m, dir, "static"), h.u, h.sigma, h.phi, m->cmd.vtk_binary);
   return PDX_OK;
 }
@@ -253,6 +260,14 @@ pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, fl
   launch_axpby_scale(ne, du, 1.0, ueq, 1.0, m->stream);
   launch_scatter_eq(m->view, ueq, u_all, m->stream);
   m->steps_done = n;
+  if (m->cmd.fail_flag == 1 && m->mesh.dim == 2) {
+    // FC 1: stresses, then SIFs, crack growth and the PD-region and bond
+    // updates (which may re-derive the device model), then damage
+    st = model_stress(m, u_all, true, false);
+    if (!st) st = fc1_pass(m, true);
+    if (st) return st;
+    return model_stress(m, m->d_u[0], false, true);
+  }
   if (m->fc2) {
     // FC 2 with the cut count and the largest sigma1 for the load ratio
     st = fc2_pass(m, true);
@@ -277,6 +292,16 @@ pdx_status quasi_increment(pdx_model* m, int n, int method, KrylovResult* kr, fl
 // takes dt * velocity once, from 0, and holds).
 pdx_status quasi_advance(pdx_model* m) {
   double* u_all = m->d_u[0];
+  if (m->cmd.fail_flag == 1 && m->d_ebc_vel) {
+    // FC 1 (failureProcess :6601-6614): the load holds while a tip moved,
+    // otherwise rati = 1.001 K_Ic / Keq of the last crack
+    if (m->fc1_moved) return PDX_OK;
+    const double kic = m->mesh.KIc, mx = m->fc1_keq;
+    const double rati = std::fabs(mx) < 1e-20 * kic ? 1.0 : 1.001 * kic / mx;
+    m->quasi_load++;
+    return cuda_check(launch_advance_prescribed_ratio(m->view, u_all, m->d_ebc_vel, m->cmd.dt, rati, m->stream),
+                      "prescribed values");
+  }
   if (m->fc2) {
     if (m->fc2_kept > 0) return PDX_OK;   // bonds were cut: the load holds
     const double sig = m->mesh.sigult, mx = m->fc2_max;
@@ -290,20 +315,34 @@ pdx_status quasi_advance(pdx_model* m) {
 }
 
 pdx_status run_quasi(pdx_model* m, const std::string& dir) {
-  pdx_status st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
+  pdx_status st = fc1_reset(m);
+  if (!st) st = pdx_explicit_init(m);   // u = initial DOF values, bond states reset
   m->explicit_run = false;
   if (st) return st;
-  double* u_all = m->d_u[0];
   m->cur = 0;
   m->quasi_load = 0;
+  // <title>_cp.out: the crack path of FC 1, one row per increment with each
+  // crack's tip and the last crack's KI, KII and Keq, as the reference writes
+  // it (pdsolve.cpp:6496-6504, 7481-7489)
+  std::ofstream cp(dir + "/" + m->mesh.title + "_cp.out");
+  cp << std::left << std::scientific << std::setprecision(4);
+  const bool fc1 = m->cmd.fail_flag == 1 && m->mesh.dim == 2;
+  if (fc1) cp << "crack ID\t tip_x\t tip_y \t KI \tKII \t Keq\n";
   AsyncWriter writer(m);
   for (int n = 1; n <= m->cmd.nsteps; n++) {
     KrylovResult kr;
     st = quasi_increment(m, n, m->cmd.solve_method, &kr, nullptr);
     if (!st) st = rf_record(m, n);
     if (st) return st;
+    if (fc1 && !m->cracks.empty()) {
+      const auto& last = m->crack_sif.back();
+      for (size_t k = 0; k < m->cracks.size(); k++)
+        cp << k << "\t" << m->cracks[k][3] << "\t" << m->cracks[k][4] << "\t" << last[0] << "\t" << last[1] << "\t"
+           << last[2] << " \"***\"\t";
+      cp << std::endl;
+    }
     if (n % std::max(1, m->cmd.save_freq) == 0 || n == m->cmd.nsteps || n == 1) {
-      st = writer.submit(u_all, out_name(m, dir, std::to_string(n)));
+      st = writer.submit(m->d_u[0], out_name(m, dir, std::to_string(n)));
       if (st) return st;
     }
     st = quasi_advance(m);
@@ -378,9 +417,11 @@ extern "C" pdx_status pdx_run(pdx_model* m, const char* results_dir) {
   const std::string dir(results_dir);
   // FC 2 breaks bonds after every explicit or Newmark step and every
   // quasi-static increment (with its load-ratio control), as the reference
-  // does; FC 1 is not built
-  if (m->cmd.solver != 1 && m->cmd.fail_flag == 1)
-    return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
+  // does; FC 1 grows cracks after every quasi-static increment and reports
+  // the SIFs of a static solve (in dynamic runs the reference only moves its
+  // tip records, without breaking a bond: not offered)
+  if (m->cmd.solver == 0 && m->cmd.fail_flag == 1)
+    return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 runs with the static and quasi-static solvers");
   switch (m->cmd.solver) {
     case 0: return m->cmd.newmark ? run_newmark(m, dir) : run_explicit(m, dir);
     case 1: return run_static(m, dir);
@@ -394,7 +435,8 @@ extern "C" pdx_status pdx_quasi_init(pdx_model* m) {
   if (!m->has_device) return set_error(PDX_ERR_NODEVICE, "model has no GPU device");
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
   cudaSetDevice(m->device);
-  pdx_status st = pdx_explicit_init(m);
+  pdx_status st = fc1_reset(m);
+  if (!st) st = pdx_explicit_init(m);
   if (st) return st;
   m->cur = 0;
   m->steps_done = 0;
@@ -409,8 +451,6 @@ extern "C" pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* i
   if (!m->batch.empty()) return set_error(PDX_ERR_UNSUPPORTED, "quasi-static increments take one specimen");
   if (method < 0 || (method > 3 && method < 6) || method > 8)
     return set_error(PDX_ERR_INVALID, "method must be 0..3 or 6..8");
-  if (m->cmd.fail_flag == 1)
-    return set_error(PDX_ERR_UNSUPPORTED, "failure criterion FC 1 is not implemented");
   cudaSetDevice(m->device);
   KrylovResult kr;
   float ms = 0.f;

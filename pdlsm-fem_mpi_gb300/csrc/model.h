@@ -108,6 +108,10 @@ struct Setup {
   std::vector<uint8_t> bond_state; // per member (member 0 unused, kept 1)
   // CSR pattern of the stiffness matrix (zero-based, rows = equations)
   std::vector<int64_t> csr_ia, csr_ja;
+  // element algorithm types after the crack updates (1 PD, 2 FE) and the
+  // crack-cut elements found so far (civ_CracEleIDX), kept for FC 1 growth
+  std::vector<int> algo;
+  std::vector<int> crack_elems;
 };
 
 struct Model;
@@ -121,6 +125,18 @@ bool read_mesh(const std::string& path, Mesh& mesh, Error& err);
 // (identical results)
 // pattern = false skips the CSR pattern (and prepare_model its scatter map)
 bool build_setup(const Mesh& mesh, const Command& cmd, Setup& s, Error& err, int device = -1, bool pattern = true);
+// FC 1 growth of the PD region after crack tips moved (updateEnrichRegion,
+// pdsolve.cpp:8871-8908): `segs` holds the new segment (old tip, new tip) of
+// every crack that propagated, in crack order.  Elements cut by a segment,
+// and FE elements within me * min_delta of them, become PD; PDBEs, node types
+// and the CSR pattern are rebuilt; the new PD nodes get families appended
+// after the existing ones (intact bonds), and the families touching the new
+// PD elements gain their volume.  *grew tells whether any element became PD.
+void grow_pd_region(const Mesh& mesh, const Command& cmd, Setup& s,
+                    const std::vector<std::array<double, 9>>& segs, bool* grew);
+// updateBondstate (pdsolve.cpp:8910-9004): every intact bond of a family in
+// the blocks around `seg` that crosses it is broken; returns the count
+int cut_bonds_by_segment(const Mesh& mesh, Setup& s, const std::array<double, 9>& seg);
 // family members and offsets of s.fam_node on the GPU, in the host loop's
 // order; err.code 7 on a CUDA failure (k_setup.cu)
 bool gpu_family_search(const Mesh& m, Setup& s, const std::vector<double>& delta_node, double md, int device,

@@ -191,6 +191,14 @@ struct pdx_model {
   bool newmark_ready = false;
   pdx::Learned* learned = nullptr;
   pdx::TwoLevelHost* twolevel = nullptr;   // built at the first method-8 solve
+  // FC 1 (2D): the current crack segments (previous tip, tip), per crack the
+  // last evaluation (KI, KII, Keq, moved), the last crack's Keq (the load
+  // ratio's reference value) and whether any tip moved in the last pass
+  std::vector<std::array<double, 9>> cracks;
+  std::vector<std::array<double, 4>> crack_sif;
+  double fc1_keq = 0.0;
+  bool fc1_moved = false;
+  bool fc1_changed = false;          // the set-up differs from the mesh's (growth or cut bonds)
   int cur = 0;                       // index of the buffer holding u_n
   int64_t steps_done = 0;
   // explicit runs apply a step's FC 3 failure pass at the start of the next
@@ -215,6 +223,22 @@ pdx_status rf_record(pdx_model* m, int64_t row);
 // FC 2 pass on the current state; with `report` it also reads back how many
 // candidates were cut (fc2_kept) and the largest sigma1 (fc2_max)
 pdx_status fc2_pass(pdx_model* m, bool report = false);
+// FC 1 pass on the current state (node stresses already computed): SIFs of
+// every crack from the interaction integral, tip growth where Keq > K_Ic and,
+// with `grow` (quasi-static runs), the PD region and bond states updated
+// (fc1.cpp)
+pdx_status fc1_pass(pdx_model* m, bool grow);
+// PD-region growth and bond cuts of the moved cracks' new segments, then the
+// device model brought up to date (fc1.cpp)
+pdx_status apply_growth(pdx_model* m, const std::vector<std::array<double, 9>>& moved);
+// cracks back to the mesh's pre-cracks and, if a run changed it, the set-up
+// and device model back to the mesh's (fc1.cpp)
+pdx_status fc1_reset(pdx_model* m);
+// the device model re-derived from m->setup after FC 1 changed it, keeping
+// displacements, node stresses and the reaction-force history (capi.cpp)
+pdx_status rebuild_device(pdx_model* m);
+// bond states of m->setup uploaded into the device's state bits (capi.cpp)
+pdx_status upload_bond_states(pdx_model* m);
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);
 extern const int kEqTemps;
 pdx_status explicit_step_launch(pdx_model* m, int mode, int64_t step_index);

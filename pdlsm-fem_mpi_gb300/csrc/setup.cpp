@@ -117,7 +117,9 @@ struct Ctx {
   }
 };
 
-bool update_pde_by_crack(Ctx& cx, const std::array<double, 9>& cr, Error& err) {
+// Crack-cut elements of segment `cr` not found before are appended to
+// cx.crack_elems (updatePDEbyCrack, first half); returns how many.
+size_t update_pde_by_crack(Ctx& cx, const std::array<double, 9>& cr) {
   Setup& s = cx.s;
   int lo[3], hi[3];
   cx.crack_block_range(cr, lo, hi);
@@ -131,12 +133,169 @@ bool update_pde_by_crack(Ctx& cx, const std::array<double, 9>& cr, Error& err) {
               std::find(cx.crack_elems.begin(), cx.crack_elems.end(), e) == cx.crack_elems.end())
             cx.crack_elems.push_back(e);
       }
-  if (cx.crack_elems.size() == old) {
-    err.code = 2;
-    err.msg = "a pre-existing crack cuts no element";
-    return false;
+  return cx.crack_elems.size() - old;
+}
+
+// The second half of updatePDEbyCrack: FE elements whose centres lie within
+// me * min_delta of a crack element found since `old` become PD, appended to
+// s.pde in block order.
+void pde_near_crack_elems(Ctx& cx, size_t old, double me) {
+  Setup& s = cx.s;
+  const Mesh& m = cx.m;
+  const size_t n = cx.crack_elems.size() - old;
+  if (n == 0) return;
+  std::vector<std::array<double, 3>> cc(n);
+  double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+  for (size_t i = 0; i < n; i++) {
+    elem_center(m, cx.crack_elems[old + i], cc[i].data());
+    for (int a = 0; a < 3; a++) { mn[a] = std::min(mn[a], cc[i][a]); mx[a] = std::max(mx[a], cc[i][a]); }
   }
-  return true;
+  int blo[3], bhi[3];
+  for (int i = 0; i < 3; i++) {
+    blo[i] = (int)((mn[i] - s.lbc[i]) / s.block_size);
+    bhi[i] = (int)((mx[i] - s.lbc[i]) / s.block_size);
+  }
+  const double mf = me + 1e-15;
+  const double Rsq = s.min_delta * s.min_delta * mf * mf;
+  for (int x = blo[0] - 1; x < bhi[0] + 2; x++)
+    for (int y = blo[1] - 1; y < bhi[1] + 2; y++)
+      for (int z = blo[2] - 1; z < bhi[2] + 2; z++) {
+        if (!cx.in_range(x, y, z)) continue;
+        for (int e : s.block_elems[cx.bindex(x, y, z)]) {
+          if (cx.algo[e] != 2) continue;
+          double c[3];
+          elem_center(m, e, c);
+          for (size_t i = 0; i < n; i++) {
+            const double dis = (c[0] - cc[i][0]) * (c[0] - cc[i][0]) + (c[1] - cc[i][1]) * (c[1] - cc[i][1]) +
+                               (c[2] - cc[i][2]) * (c[2] - cc[i][2]);
+            if (dis < Rsq) { cx.algo[e] = 1; s.pde.push_back(e); break; }
+          }
+        }
+      }
+}
+
+// PDBEs (element edges in 2D, faces in 3D of PD elements not shared by two PD
+// elements) and node types (2 PD, 1 on a PDBE, 0 FE) of the current s.pde.
+// The set of PDBEs is what the reference keeps after its incremental updates
+// too (an edge or face is shared by at most two elements); the kernels use it
+// through per-node sums of at most two terms in 2D, so its order is free.
+void pdbe_and_node_types(const Mesh& m, Setup& s) {
+  const int D = m.dim;
+  s.pdbe.clear();
+  std::vector<std::array<int, 5>> list;
+  for (int e : s.pde) {
+    const int* c = &m.conn[(size_t)e * 8];
+    if (D == 2) {
+      const int nn = m.elem_nn[e];
+      for (int j = 0; j < nn; j++) {
+        const int a = c[j], b = c[(j + 1) % nn];
+        if (a < b) list.push_back({a, b, 1, 0, 0});
+        else list.push_back({b, a, -1, 0, 0});
+      }
+    } else {
+      const int face[6][4] = {{c[0], c[1], c[2], c[3]}, {c[4], c[5], c[6], c[7]}, {c[0], c[3], c[7], c[4]},
+                              {c[1], c[2], c[6], c[5]}, {c[0], c[4], c[5], c[1]}, {c[3], c[7], c[6], c[2]}};
+      const int sgn[6] = {-1, 1, -1, 1, -1, 1};
+      for (int j = 0; j < 6; j++) {
+        const int pos = (int)(std::min_element(face[j], face[j] + 4) - face[j]);
+        list.push_back({face[j][pos], face[j][(pos + 1) % 4], face[j][(pos + 2) % 4], face[j][(pos + 3) % 4], sgn[j]});
+      }
+    }
+  }
+  std::stable_sort(list.begin(), list.end(), [](const std::array<int, 5>& a, const std::array<int, 5>& b) {
+    return a[0] < b[0];
+  });
+  std::vector<uint8_t> dead(list.size(), 0);
+  for (size_t i = 0; i < list.size(); i++) {
+    if (dead[i]) continue;
+    for (size_t j = i + 1; j < list.size() && list[j][0] == list[i][0]; j++) {
+      if (dead[j]) continue;
+      const bool same = D == 2 ? list[j][1] == list[i][1]
+                               : (list[j][1] == list[i][1] && list[j][2] == list[i][2] && list[j][3] == list[i][3]);
+      if (same) { dead[i] = dead[j] = 1; break; }
+    }
+  }
+  for (size_t i = 0; i < list.size(); i++) {
+    if (dead[i]) continue;
+    const auto& a = list[i];
+    if (D == 2) {
+      if (a[2] == 1) s.pdbe.push_back({a[0], a[1], -1, -1});
+      else s.pdbe.push_back({a[1], a[0], -1, -1});
+    } else {
+      if (a[4] == 1) s.pdbe.push_back({a[0], a[1], a[2], a[3]});
+      else s.pdbe.push_back({a[3], a[2], a[1], a[0]});
+    }
+  }
+  s.node_type.assign(m.n_node, 0);
+  for (int e : s.pde)
+    for (int i = 0; i < m.elem_nn[e]; i++) s.node_type[m.conn[(size_t)e * 8 + i]] = 2;
+  const int pn = D == 2 ? 2 : 4;
+  for (const auto& b : s.pdbe)
+    for (int i = 0; i < pn; i++) s.node_type[b[i]] = 1;
+}
+
+// Members of families f0.. (the union rule of initialPDN_Fami / updatePDN_Fami:
+// j joins k's family when within either node's horizon), appended to
+// s.fam_members / s.fam_off, which hold families 0..f0-1.
+void host_members(const Ctx& cx, int f0, const std::vector<double>& delta_node) {
+  Setup& s = cx.s;
+  const Mesh& m = cx.m;
+  const double md = s.min_delta;
+  for (int f = f0; f < (int)s.fam_node.size(); f++) {
+    const int k = s.fam_node[f];
+    const double dk = s.fam_delta[f];
+    const double* xk = &m.X[(size_t)k * 3];
+    s.fam_members.push_back(k);
+    int ib[3];
+    cx.block_of(xk, ib);
+    for (int x = ib[0] - 1; x < ib[0] + 2; x++)
+      for (int y = ib[1] - 1; y < ib[1] + 2; y++)
+        for (int z = ib[2] - 1; z < ib[2] + 2; z++) {
+          if (!cx.in_range(x, y, z)) continue;
+          for (int j : s.block_nodes[cx.bindex(x, y, z)]) {
+            const double* xm = &m.X[(size_t)j * 3];
+            const double dj = delta_node[j];
+            const double dist = ((xm[0] - xk[0]) * (xm[0] - xk[0]) + (xm[1] - xk[1]) * (xm[1] - xk[1]) +
+                                 (xm[2] - xk[2]) * (xm[2] - xk[2]));
+            if (dist > md * md * 1.0e-16 &&
+                (dist < (dk * dk + md * md * 1.0e-16) || dist < (dj * dj + md * md * 1.0e-16)))
+              s.fam_members.push_back(j);
+          }
+        }
+    s.fam_off.push_back((int64_t)s.fam_members.size());
+  }
+}
+
+std::vector<double> node_horizons(const Mesh& m, const Command& cmd, const Setup& s) {
+  std::vector<double> delta_node(m.n_node);
+  for (int k = 0; k < m.n_node; k++) delta_node[k] = cmd.factor * std::pow(s.vol_node[k], 1.0 / m.dim);
+  return delta_node;
+}
+
+// updateBondstate for one crack segment (2D) or triangle (3D)
+int cut_bonds(const Ctx& cx, const std::array<double, 9>& cr) {
+  Setup& s = cx.s;
+  const int D = cx.m.dim;
+  int lo[3], hi[3], cut = 0;
+  cx.crack_block_range(cr, lo, hi);
+  for (int x = lo[0] - 1; x < hi[0] + 2; x++)
+    for (int y = lo[1] - 1; y < hi[1] + 2; y++)
+      for (int z = lo[2] - 1; z < hi[2] + 2; z++) {
+        if (!cx.in_range(x, y, z)) continue;
+        for (int node : s.block_nodes[cx.bindex(x, y, z)]) {
+          const int f = s.fam_of_node[node];
+          if (f < 0) continue;
+          const int k = s.fam_node[f];
+          for (int64_t p = s.fam_off[f] + 1; p < s.fam_off[f + 1]; p++) {
+            if (s.bond_state[p] != 1) continue;
+            const int mm = s.fam_members[p];
+            const bool c = D == 3 ? seg_tri_3d(cx.X(k), cx.X(mm), cr.data())
+                                  : seg_intersect_2d(cx.X(k), cx.X(mm), &cr[0], &cr[3]);
+            if (c) { s.bond_state[p] = 0; cut++; }
+          }
+        }
+      }
+  return cut;
 }
 
 }  // namespace
@@ -208,93 +367,16 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int de
     if (cx.algo[e] == 1) s.pde.push_back(e);
   for (const auto& cr : m.cracks) {
     const size_t old = cx.crack_elems.size();
-    if (!update_pde_by_crack(cx, cr, err)) return false;
-    const size_t n = cx.crack_elems.size() - old;
-    std::vector<std::array<double, 3>> cc(n);
-    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-    for (size_t i = 0; i < n; i++) {
-      elem_center(m, cx.crack_elems[old + i], cc[i].data());
-      for (int a = 0; a < 3; a++) { mn[a] = std::min(mn[a], cc[i][a]); mx[a] = std::max(mx[a], cc[i][a]); }
+    if (update_pde_by_crack(cx, cr) == 0) {
+      err.code = 2;
+      err.msg = "a pre-existing crack cuts no element";
+      return false;
     }
-    int blo[3], bhi[3];
-    for (int i = 0; i < 3; i++) {
-      blo[i] = (int)((mn[i] - s.lbc[i]) / s.block_size);
-      bhi[i] = (int)((mx[i] - s.lbc[i]) / s.block_size);
-    }
-    const double mf = cmd.me + 1e-15;
-    const double Rsq = s.min_delta * s.min_delta * mf * mf;
-    for (int x = blo[0] - 1; x < bhi[0] + 2; x++)
-      for (int y = blo[1] - 1; y < bhi[1] + 2; y++)
-        for (int z = blo[2] - 1; z < bhi[2] + 2; z++) {
-          if (!cx.in_range(x, y, z)) continue;
-          for (int e : s.block_elems[cx.bindex(x, y, z)]) {
-            if (cx.algo[e] != 2) continue;
-            double c[3];
-            elem_center(m, e, c);
-            for (size_t i = 0; i < n; i++) {
-              const double dis = (c[0] - cc[i][0]) * (c[0] - cc[i][0]) + (c[1] - cc[i][1]) * (c[1] - cc[i][1]) +
-                                 (c[2] - cc[i][2]) * (c[2] - cc[i][2]);
-              if (dis < Rsq) { cx.algo[e] = 1; s.pde.push_back(e); break; }
-            }
-          }
-        }
+    pde_near_crack_elems(cx, old, cmd.me);
   }
   for (int e = 0; e < E; e++)
     if (cx.algo[e] == 2) s.fe.push_back(e);
-  // PDBEs: element edges (2D) / faces (3D) of PD elements not shared by two PD elements
-  {
-    std::vector<std::array<int, 5>> list;
-    for (int e : s.pde) {
-      const int* c = &m.conn[(size_t)e * 8];
-      if (D == 2) {
-        const int nn = m.elem_nn[e];
-        for (int j = 0; j < nn; j++) {
-          const int a = c[j], b = c[(j + 1) % nn];
-          if (a < b) list.push_back({a, b, 1, 0, 0});
-          else list.push_back({b, a, -1, 0, 0});
-        }
-      } else {
-        const int face[6][4] = {{c[0], c[1], c[2], c[3]}, {c[4], c[5], c[6], c[7]}, {c[0], c[3], c[7], c[4]},
-                                {c[1], c[2], c[6], c[5]}, {c[0], c[4], c[5], c[1]}, {c[3], c[7], c[6], c[2]}};
-        const int sgn[6] = {-1, 1, -1, 1, -1, 1};
-        for (int j = 0; j < 6; j++) {
-          const int pos = (int)(std::min_element(face[j], face[j] + 4) - face[j]);
-          list.push_back({face[j][pos], face[j][(pos + 1) % 4], face[j][(pos + 2) % 4], face[j][(pos + 3) % 4], sgn[j]});
-        }
-      }
-    }
-    std::stable_sort(list.begin(), list.end(), [](const std::array<int, 5>& a, const std::array<int, 5>& b) {
-      return a[0] < b[0];
-    });
-    std::vector<uint8_t> dead(list.size(), 0);
-    for (size_t i = 0; i < list.size(); i++) {
-      if (dead[i]) continue;
-      for (size_t j = i + 1; j < list.size() && list[j][0] == list[i][0]; j++) {
-        if (dead[j]) continue;
-        const bool same = D == 2 ? list[j][1] == list[i][1]
-                                 : (list[j][1] == list[i][1] && list[j][2] == list[i][2] && list[j][3] == list[i][3]);
-        if (same) { dead[i] = dead[j] = 1; break; }
-      }
-    }
-    for (size_t i = 0; i < list.size(); i++) {
-      if (dead[i]) continue;
-      const auto& a = list[i];
-      if (D == 2) {
-        if (a[2] == 1) s.pdbe.push_back({a[0], a[1], -1, -1});
-        else s.pdbe.push_back({a[1], a[0], -1, -1});
-      } else {
-        if (a[4] == 1) s.pdbe.push_back({a[0], a[1], a[2], a[3]});
-        else s.pdbe.push_back({a[3], a[2], a[1], a[0]});
-      }
-    }
-  }
-  // node types
-  s.node_type.assign(N, 0);
-  for (int e : s.pde)
-    for (int i = 0; i < m.elem_nn[e]; i++) s.node_type[m.conn[(size_t)e * 8 + i]] = 2;
-  const int pn = D == 2 ? 2 : 4;
-  for (const auto& b : s.pdbe)
-    for (int i = 0; i < pn; i++) s.node_type[b[i]] = 1;
+  pdbe_and_node_types(m, s);
   // families
   s.fam_of_node.assign(N, -1);
   for (int k = 0; k < N; k++)
@@ -313,64 +395,75 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int de
       s.fam_cdv[f] = s.fam_cdv[f] + dv / nn;
     }
   }
-  std::vector<double> delta_node(N);
-  for (int k = 0; k < N; k++) delta_node[k] = cmd.factor * std::pow(s.vol_node[k], 1.0 / D);
-  const double md = s.min_delta;
+  const std::vector<double> delta_node = node_horizons(m, cmd, s);
   if (device >= 0) {
     // the same search, one warp per family, on the model's GPU (k_setup.cu)
-    if (!gpu_family_search(m, s, delta_node, md, device, err)) return false;
-  }
-  if (device < 0) s.fam_off.assign(1, 0);
-  for (int f = 0; f < nf && device < 0; f++) {
-    const int k = s.fam_node[f];
-    const double dk = s.fam_delta[f];
-    const double* xk = &m.X[(size_t)k * 3];
-    s.fam_members.push_back(k);
-    int ib[3];
-    cx.block_of(xk, ib);
-    for (int x = ib[0] - 1; x < ib[0] + 2; x++)
-      for (int y = ib[1] - 1; y < ib[1] + 2; y++)
-        for (int z = ib[2] - 1; z < ib[2] + 2; z++) {
-          if (!cx.in_range(x, y, z)) continue;
-          for (int j : s.block_nodes[cx.bindex(x, y, z)]) {
-            const double* xm = &m.X[(size_t)j * 3];
-            const double dj = delta_node[j];
-            const double dist = ((xm[0] - xk[0]) * (xm[0] - xk[0]) + (xm[1] - xk[1]) * (xm[1] - xk[1]) +
-                                 (xm[2] - xk[2]) * (xm[2] - xk[2]));
-            if (dist > md * md * 1.0e-16 &&
-                (dist < (dk * dk + md * md * 1.0e-16) || dist < (dj * dj + md * md * 1.0e-16)))
-              s.fam_members.push_back(j);
-          }
-        }
-    s.fam_off.push_back((int64_t)s.fam_members.size());
+    if (!gpu_family_search(m, s, delta_node, s.min_delta, device, err)) return false;
+  } else {
+    s.fam_off.assign(1, 0);
+    host_members(cx, 0, delta_node);
   }
   s.bond_state.assign(s.fam_members.size(), 1);
   // pre-crack bond states
-  for (const auto& cr : m.cracks) {
-    int lo[3], hi[3];
-    cx.crack_block_range(cr, lo, hi);
-    for (int x = lo[0] - 1; x < hi[0] + 2; x++)
-      for (int y = lo[1] - 1; y < hi[1] + 2; y++)
-        for (int z = lo[2] - 1; z < hi[2] + 2; z++) {
-          if (!cx.in_range(x, y, z)) continue;
-          for (int node : s.block_nodes[cx.bindex(x, y, z)]) {
-            const int f = s.fam_of_node[node];
-            if (f < 0) continue;
-            const int k = s.fam_node[f];
-            for (int64_t p = s.fam_off[f] + 1; p < s.fam_off[f + 1]; p++) {
-              if (s.bond_state[p] != 1) continue;
-              const int mm = s.fam_members[p];
-              const bool cut = D == 3 ? seg_tri_3d(cx.X(k), cx.X(mm), cr.data())
-                                      : seg_intersect_2d(cx.X(k), cx.X(mm), &cr[0], &cr[3]);
-              if (cut) s.bond_state[p] = 0;
-            }
-          }
-        }
-  }
+  for (const auto& cr : m.cracks) cut_bonds(cx, cr);
+  s.algo = cx.algo;
+  s.crack_elems = cx.crack_elems;
   if (!pattern) return true;   // batch specimens: no CSR pattern (not merged)
   if (device >= 0) return gpu_csr_pattern(m, s, device, err);   // k_setup.cu
   build_csr_pattern(m, s);
   return true;
+}
+
+void grow_pd_region(const Mesh& m, const Command& cmd, Setup& s, const std::vector<std::array<double, 9>>& segs,
+                    bool* grew) {
+  Ctx cx{m, s, s.algo, s.crack_elems};
+  const size_t old_pde = s.pde.size();
+  // a segment that cuts no new element adds no PD element (the reference
+  // reads the bounds of an empty centre list there)
+  for (const auto& seg : segs) {
+    const size_t old = cx.crack_elems.size();
+    if (update_pde_by_crack(cx, seg) > 0) pde_near_crack_elems(cx, old, cmd.me);
+  }
+  s.crack_elems = cx.crack_elems;
+  *grew = s.pde.size() > old_pde;
+  if (!*grew) return;
+  s.algo = cx.algo;
+  s.fe.clear();
+  for (int e = 0; e < m.n_elem; e++)
+    if (s.algo[e] == 2) s.fe.push_back(e);
+  pdbe_and_node_types(m, s);
+  // new PD nodes get families after the existing ones, in the order of the
+  // new PD elements and their nodes (updatePDN_Fami)
+  const int D = m.dim;
+  const int f0 = (int)s.fam_node.size();
+  for (size_t i = old_pde; i < s.pde.size(); i++) {
+    const int e = s.pde[i];
+    for (int a = 0; a < m.elem_nn[e]; a++) {
+      const int k = m.conn[(size_t)e * 8 + a];
+      if (s.fam_of_node[k] >= 0) continue;
+      s.fam_of_node[k] = (int)s.fam_node.size();
+      s.fam_node.push_back(k);
+      s.fam_delta.push_back(cmd.factor * std::pow(s.vol_node[k], 1.0 / D));
+    }
+  }
+  s.fam_cdv.resize(s.fam_node.size(), 0.0);
+  for (size_t i = old_pde; i < s.pde.size(); i++) {
+    const int e = s.pde[i];
+    const double dv = s.vol_elem[e];
+    const int nn = m.elem_nn[e];
+    for (int a = 0; a < nn; a++) {
+      const int f = s.fam_of_node[m.conn[(size_t)e * 8 + a]];
+      s.fam_cdv[f] = s.fam_cdv[f] + dv / nn;
+    }
+  }
+  host_members(cx, f0, node_horizons(m, cmd, s));
+  s.bond_state.resize(s.fam_members.size(), 1);
+  build_csr_pattern(m, s);
+}
+
+int cut_bonds_by_segment(const Mesh& m, Setup& s, const std::array<double, 9>& seg) {
+  Ctx cx{m, s, {}, {}};
+  return cut_bonds(cx, seg);
 }
 
 void build_csr_pattern(const Mesh& m, Setup& s) {

@@ -132,14 +132,18 @@ def write_cmd(path: str, mesh_file: str, mesh: Mesh, *, solver: str, dt: float,
               nsteps: int, save: int, factor: float, nlf: float,
               newmark: Optional[Tuple[float, float]] = None, lumped: bool = True,
               fc: Optional[str] = None, precision: Optional[str] = None,
-              extra: Sequence[str] = (), vtk: str = "BINARY") -> None:
+              extra: Sequence[str] = (), vtk: str = "BINARY", me: Optional[float] = None) -> None:
     """Write a command file with the reference's keywords (``fioFile.cpp:69-462``).
 
     ``fc`` is the text after the ``FC`` keyword; ``FC 3 s0 [seed] [pert]`` is the
     critical-stretch extension (the reference parses flag 3 but never acts on it).
+    ``me`` is SETSOLVING's optional sixth value: crack-cut elements make the FE
+    elements whose centres lie within me times the smallest element size PD.
     """
-    out = [f"MSHFILE {mesh_file}", f"SOLVER {solver}",
-           f"SETSOLVING {_fmt(dt)} {nsteps} {save} {_fmt(factor)} {_fmt(nlf)}"]
+    setsolving = f"SETSOLVING {_fmt(dt)} {nsteps} {save} {_fmt(factor)} {_fmt(nlf)}"
+    if me is not None:
+        setsolving += f" {_fmt(me)}"
+    out = [f"MSHFILE {mesh_file}", f"SOLVER {solver}", setsolving]
     if newmark is not None:
         out.append(f"NEWMARK ON {_fmt(newmark[0])} {_fmt(newmark[1])}")
     else:
@@ -281,6 +285,31 @@ def plate_strip_crack(n: int = 101, L: float = 0.05, strip_frac: float = 0.4,
 
     crack = np.array([[xs0 + 0.25 * h, y_c, 0.0], [xs0 + 0.25 * h + crack_len, y_c, 0.0]])
     return plate2d(n, n, h, pd_mask=pd_mask, cracks=[crack], title=title)
+
+
+def plate_edge_crack(n: int = 31, L: float = 0.03, a_frac: float = 0.41, pd_band: int = 0,
+                     title: str = "plateEdge", KIc: float = 1.0e6, protype: int = 1) -> Mesh:
+    """n x n node square FE plate with an edge pre-crack for FC 1 crack growth.
+
+    The crack starts a quarter element inside the left edge and runs in +x to
+    ``a_frac`` of the width, half an element above the middle node row.  Only
+    the elements it cuts become PD at set-up (and, with ``pd_band`` > 0, the
+    elements whose centres lie within ``pd_band`` elements of the crack line
+    behind its tip); the PD region then grows with the crack.
+    """
+    h = L / (n - 1)
+    ne = n - 1
+    y_c = (ne // 2) * h + 0.5 * h
+    x_tip = a_frac * L
+
+    def pd_mask(cent):
+        if pd_band <= 0:
+            return np.zeros(len(cent), dtype=bool)
+        return (np.abs(cent[:, 1] - y_c) < pd_band * h) & (cent[:, 0] < x_tip)
+
+    crack = np.array([[0.25 * h, y_c, 0.0], [x_tip, y_c, 0.0]])
+    return plate2d(n, n, h, pd_mask=pd_mask, cracks=[crack], title=title,
+                   material=(72e9, 0.22, 2440.0, KIc, 1.0e8), protype=protype)
 
 
 def box_hole(nx: int = 121, ny: int = 61, nz: int = 21, h: float = 1e-3,

@@ -57,7 +57,7 @@ EXPORTED = ["pdx_last_error", "pdx_version", "pdx_model_create_from_cmd", "pdx_m
             "pdx_batch_offsets", "pdx_newmark_init", "pdx_newmark_step", "pdx_learned_setup", "pdx_learned_samples",
             "pdx_learned_train", "pdx_mlp_params", "pdx_mlp_loss_grad", "pdx_learned_probe",
             "pdx_learned_pairs", "pdx_learned_options", "pdx_learned_active",
-            "pdx_quasi_init", "pdx_quasi_step", "pdx_reaction_forces"]
+            "pdx_quasi_init", "pdx_quasi_step", "pdx_reaction_forces", "pdx_crack_state", "pdx_crack_advance"]
 
 _lib: Optional[C.CDLL] = None
 
@@ -107,6 +107,8 @@ def lib() -> C.CDLL:
                        ("pdx_quasi_init", [_P]),
                        ("pdx_reaction_forces", [_P, _D, C.c_int64, C.POINTER(C.c_int64)]),
                        ("pdx_quasi_step", [_P, C.c_int, C.POINTER(SolveInfo)]),
+                       ("pdx_crack_state", [_P, _D, C.c_int, C.POINTER(C.c_int)]),
+                       ("pdx_crack_advance", [_P, _D, C.POINTER(C.c_uint8)]),
                        ("pdx_learned_pairs", [_P, _F, _F, C.POINTER(C.c_int64), C.POINTER(C.c_int)])):
         getattr(L, name).argtypes = args
         getattr(L, name).restype = C.c_int
@@ -186,6 +188,23 @@ class Model:
         if n.value:
             _check(lib().pdx_reaction_forces(self._h, out.ctypes.data_as(_D), n.value, None))
         return out
+
+    def crack_state(self) -> np.ndarray:
+        """FC 1 crack rows (x0, y0, x1, y1, KI, KII, Keq, moved), shape (n_cracks, 8);
+        (x1, y1) is the tip, (x0, y0) the tip before the last growth."""
+        n = C.c_int()
+        _check(lib().pdx_crack_state(self._h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 8))
+        if n.value:
+            _check(lib().pdx_crack_state(self._h, out.ctypes.data_as(_D), n.value, None))
+        return out
+
+    def crack_advance(self, tips, moved) -> None:
+        """Move the cracks flagged in `moved` to `tips` (n_cracks x 2) and grow
+        the PD region and break the bonds across the new segments."""
+        t = np.ascontiguousarray(tips, dtype=np.float64).reshape(-1)
+        mv = np.ascontiguousarray(moved, dtype=np.uint8).reshape(-1)
+        _check(lib().pdx_crack_advance(self._h, t.ctypes.data_as(_D), mv.ctypes.data_as(C.POINTER(C.c_uint8))))
 
     # ---- quasi-static increments ----
     def quasi_init(self) -> None:

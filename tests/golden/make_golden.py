@@ -10,7 +10,7 @@ same models without the reference.
 Needs the reference tree (PDX_REFERENCE, or the checkout that
 __graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
-[--size-only]
+[--size-only] [--fc1-only]
 """
 from __future__ import annotations
 
@@ -192,6 +192,33 @@ def fc2_cases() -> None:
     shutil.rmtree(work)
 
 
+def fc1_cases() -> None:
+    """FC 1 (SIFs by the interaction integral, crack growth, PD-region growth)
+    on a 31 x 31-node FE plate with an edge pre-crack, 24 quasi-static
+    increments with the reference's load-ratio control (RF 2 recorded):
+    pe31_fc1 plane stress, default J-path radius and growth step (FC 1), no
+    neighbour enrichment; pe31_fc1m plane strain, FC 1 4 1.5 and me = 1.5, so
+    that each growth also makes the FE elements next to the new crack
+    elements PD."""
+    work = tempfile.mkdtemp(prefix="golden_fc1_")
+    d2 = os.path.join(work, "pe31")
+    m = meshgen.plate_edge_crack(n=31, KIc=1.0e6, title="pe31")
+    m.ebcs[2].velocity = 2e-7
+    meshgen.write_case(m, d2, "pe31_fc1", solver="QUASI-STATIC", dt=1.0, nsteps=24, save=24, factor=3.015, nlf=1.0,
+                       lumped=False, fc="1", extra=["RF 2", "SOLVE BICGSTAB 1e-13 20000"])
+    mm = meshgen.plate_edge_crack(n=31, KIc=1.0e6, title="pe31m", protype=2)
+    mm.ebcs[2].velocity = 2e-7
+    meshgen.write_case(mm, d2, "pe31_fc1m", solver="QUASI-STATIC", dt=1.0, nsteps=24, save=24, factor=3.015,
+                       nlf=1.0, lumped=False, fc="1 4 1.5", me=1.5, extra=["RF 2", "SOLVE BICGSTAB 1e-13 20000"])
+    copy_inputs(d2, "pe31")
+    keep = ("crack_rows", "region_rows", "pde_final", "fam_node_final", "fam_off_final", "fam_members_final",
+            "bond_state_final", "rf_rows", "u_traj", "sigma_final")
+    for name in ("pe31_fc1", "pe31_fc1m"):
+        d = run(d2, name + ".in", "quasi_fc1")
+        save(name, {k: d[k] for k in keep})
+    shutil.rmtree(work)
+
+
 def rf_cases() -> None:
     """Reaction forces (RF 2: the top edge's essential BC) of the 2D plate over
     60 explicit steps, no failure criterion."""
@@ -310,6 +337,10 @@ if __name__ == "__main__":
         build_driver()
         size_cases()
         sys.exit(0)
+    if "--fc1-only" in sys.argv:
+        build_driver()
+        fc1_cases()
+        sys.exit(0)
     if "--fc2-only" in sys.argv or "--rf-only" in sys.argv or "--ascii-only" in sys.argv:
         build_driver()
         if "--fc2-only" in sys.argv:
@@ -321,4 +352,5 @@ if __name__ == "__main__":
     else:
         main()
         fc2_cases()
+        fc1_cases()
         rf_cases()

@@ -1,0 +1,123 @@
+"""FC 1: SIFs from the interaction integral, crack growth, PD-region growth
+and the load-ratio control of the quasi-static loop, against the reference
+itself (tests/golden/pe31_fc1*.npz, made by make_golden.py's fc1_cases from
+the reference's own b_cracPropag_qusiaStatic_BYKeq run through its
+quasi-static loop).
+
+Two 31 x 31-node FE plates with an edge pre-crack, 24 increments each:
+pe31_fc1 plane stress with the default path radius and growth step;
+pe31_fc1m plane strain with FC 1 4 1.5 and me = 1.5 (growth also makes the
+FE elements next to the new crack elements PD).  The crack first grows at
+increment 19 (pe31_fc1) or 18 (pe31_fc1m) and then at every increment, with
+the load held."""
+import numpy as np
+import pytest
+
+from conftest import case_cmd, golden, rel
+
+import pdx
+
+CASES = ["pe31_fc1", "pe31_fc1m"]
+
+
+def _moves(g):
+    """Per increment the tips after the FC 1 pass and which cracks moved."""
+    tips = g["crack_rows"][:, :, 1:3]
+    prev = np.concatenate([tips[:1], tips[:-1]])
+    return tips, np.any(tips != prev, axis=2)
+
+
+def test_fc1_goldens_grow_the_crack_and_the_pd_region():
+    for name in CASES:
+        g = golden(name)
+        tips, moved = _moves(g)
+        region = g["region_rows"]
+        n_moves = int(moved.sum())
+        assert n_moves >= 5
+        # a moved tip holds the load (addLoad false) and grows the PD region
+        np.testing.assert_array_equal(region[:, 2] == 0, moved.any(axis=1))
+        assert region[-1, 0] > region[0, 0] and region[-1, 1] > region[0, 1]
+        # the tip moves by dcf * min_delta along the kink angle, mostly along +x
+        step = np.linalg.norm(np.diff(tips[:, 0], axis=0), axis=1)
+        assert np.all((step == 0) | (np.abs(step - step.max()) < 1e-12))
+        assert tips[-1, 0, 0] > tips[0, 0, 0]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_crack_advance_reproduces_the_reference_region_growth(built, name):
+    """The reference's tip sequence replayed through pdx_crack_advance on a
+    host-only model: PD elements (in the reference's civ_pdeIDX order),
+    families (appended in its order), members and bond states after the
+    last growth are identical."""
+    g = golden(name)
+    tips, moved = _moves(g)
+    m = pdx.Model(case_cmd("pe31", name), device=-1)
+    n_fam0 = m.array_len("fam_off") - 1
+    for i in range(tips.shape[0]):
+        if moved[i].any():
+            m.crack_advance(tips[i], moved[i])
+            assert m.array_len("pde_idx") == int(g["region_rows"][i, 0])
+            assert m.array_len("fam_off") - 1 == int(g["region_rows"][i, 1])
+    np.testing.assert_array_equal(m.array("pde_idx"), g["pde_final"])
+    np.testing.assert_array_equal(m.array("fam_off"), g["fam_off_final"])
+    np.testing.assert_array_equal(m.array("fam_members"), g["fam_members_final"])
+    np.testing.assert_array_equal(m.array("bond_state0"), g["bond_state_final"])
+    assert m.array_len("fam_off") - 1 > n_fam0
+    cs = m.crack_state()
+    np.testing.assert_array_equal(cs[:, 2:4], tips[-1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_fc1_quasi_static_run_matches_reference(built, name):
+    """All 24 increments through pdx_quasi_step: per increment the tips
+    (to 1e-9 of the plate), KI and KII (1e-6 of the largest |K|), Keq
+    against K_Ic (the same growth decisions), the PD-region size and the
+    free displacements (1e-8); after the last increment the PD elements,
+    families, members and bond states exactly, and the reaction forces."""
+    g = golden(name)
+    rows, region = g["crack_rows"], g["region_rows"]
+    with pdx.Model(case_cmd("pe31", name), device=0, precision=0) as m:
+        free = m.array("eq") >= 0
+        kmax = np.abs(rows[:, :, 3:5]).max()
+        worst_u = worst_k = 0.0
+        m.quasi_init()
+        for i in range(rows.shape[0]):
+            info = m.quasi_step(2)
+            assert info.converged
+            cs = m.crack_state()
+            # a tip moves along the kink angle from KII/KI: 1e-9 of the plate
+            assert np.abs(cs[:, 2:4] - rows[i, :, 1:3]).max() <= 1e-9 * 0.03, f"increment {i + 1}"
+            worst_k = max(worst_k, float(np.abs(cs[:, 4:6] - rows[i, :, 3:5]).max()) / kmax)
+            np.testing.assert_array_equal(cs[:, 7] == 1, region[i, 2] == 0)
+            assert m.array_len("pde_idx") == int(region[i, 0])
+            assert m.array_len("fam_off") - 1 == int(region[i, 1])
+            u, _, _, bs = m.state()
+            worst_u = max(worst_u, rel(u.reshape(-1)[free], g["u_traj"][i].reshape(-1)[free]))
+        rf = m.reaction_forces()
+        np.testing.assert_array_equal(m.array("pde_idx"), g["pde_final"])
+        np.testing.assert_array_equal(m.array("fam_off"), g["fam_off_final"])
+        np.testing.assert_array_equal(m.array("fam_members"), g["fam_members_final"])
+        np.testing.assert_array_equal(bs, g["bond_state_final"])
+    print(f"\n[{name}] worst free-displacement error {worst_u:.2e}, worst K error {worst_k:.2e} of max |K|, "
+          f"{int(g['region_rows'][-1, 0])} PD elements, {int((bs == 0).sum())} broken bonds")
+    assert worst_u < 1e-8
+    assert worst_k < 1e-6
+    ref_rf = g["rf_rows"]
+    assert rf.shape[0] == ref_rf.shape[0] + 1
+    assert np.abs(rf[1:, 1:4] - ref_rf[:, 2:5]).max() <= 1e-7 * np.abs(ref_rf[:, 2:5]).max()
+
+
+@pytest.mark.gpu
+def test_fc1_run_writes_the_crack_path_file(built, tmp_path):
+    """pdx_run on an FC 1 deck writes <title>_cp.out with the reference's
+    header and one row per increment (scientific, 4 digits)."""
+    with pdx.Model(case_cmd("pe31", "pe31_fc1"), device=0, precision=0) as m:
+        m.run(str(tmp_path))
+    lines = open(tmp_path / "pe31_cp.out").read().splitlines()
+    assert lines[0] == "crack ID\t tip_x\t tip_y \t KI \tKII \t Keq"
+    assert len(lines) == 1 + 24
+    g = golden("pe31_fc1")
+    last = lines[-1].split("\t")
+    assert float(last[1]) == pytest.approx(g["crack_rows"][-1, 0, 1], rel=1e-3)
+    assert float(last[3]) == pytest.approx(g["crack_rows"][-1, 0, 3], rel=1e-3)
