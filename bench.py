@@ -321,6 +321,57 @@ def bench_quasi(args):
     return line
 
 
+def bench_fc1(args):
+    """FC 1 crack growth (meshgen.fc1_bench_case): quasi-static increments of an n x n-node FE plate with an
+    edge pre-crack (only the crack-cut elements PD at the start), K_Ic = 1 MPa m^0.5, top edge pulled 1e-6 m per
+    load step.  Each
+    increment assembles and solves K du = f (two-level BiCGStab, method 8, whose coarse inverse is re-formed
+    after every PD-region growth), evaluates the crack tip's SIFs on the interaction-integral path and, from
+    the first increment with Keq > K_Ic on, moves the tip, grows the PD region, breaks the bonds across the
+    new segment and re-derives the device model.  One untimed run of 3 increments, then all increments timed
+    on the host clock (the FC 1 pass and the rebuild are host work around the GPU kernels)."""
+    import meshgen
+    import pdx
+    tmp = tempfile.mkdtemp(prefix="pdx_bench_")
+    n = args.fc1_n
+    nsteps = args.fc1_increments
+    mesh, kw = meshgen.fc1_bench_case(n=n, nsteps=nsteps)
+    cmd = meshgen.write_case(mesh, tmp, "fc1plate", **kw)
+    method = 8
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        m.quasi_init()
+        for _ in range(3):
+            m.quasi_step(method)
+        m.quasi_init()
+        wall, solve, moved, its = [], [], [], []
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            i = m.quasi_step(method)
+            wall.append(time.perf_counter() - t0)
+            solve.append(i.seconds)
+            its.append(i.iterations)
+            moved.append(bool(m.crack_state()[0, 7]))
+        cs = m.crack_state()
+        n_pde, n_fam, n_eq = m.array_len("pde_idx"), m.array_len("fam_off") - 1, m.info.n_eq
+    wall, solve, moved = np.array(wall), np.array(solve), np.array(moved)
+    grow = wall[moved] if moved.any() else np.zeros(1)
+    load = wall[~moved] if (~moved).any() else np.zeros(1)
+    return {"metric": "FC 1 quasi-static increment time (s per increment, crack-growth increments)",
+            "value": float(grow.mean()), "unit": "s", "n_gpus": 1, "steps": nsteps, "warmup": 3,
+            "ms_per_step": float(grow.mean()) * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded meshgen plate_edge_crack)",
+            "config": {"workload": f"fc1: {n}x{n}-node FE plate, edge pre-crack to 0.41 W, FC 1 (mr 6, dcf 1), "
+                                   f"K_Ic 1e6, top edge +1e-6 m per load step, {n_eq} equations",
+                       "solve": "two-level BiCGStab (method 8) to 1e-10"},
+            "growth_increments": int(moved.sum()), "load_increments": int((~moved).sum()),
+            "s_per_load_increment": float(load.mean()), "s_per_growth_increment": float(grow.mean()),
+            "solve_s_per_increment": float(solve.mean()), "iterations_per_increment": float(np.mean(its)),
+            "host_and_rebuild_s_per_growth_increment": float((grow - solve[moved]).mean()) if moved.any() else None,
+            "pd_elements_final": int(n_pde), "families_final": int(n_fam),
+            "tip_final": [float(cs[0, 2]), float(cs[0, 3])], "keq_final": float(cs[0, 6]),
+            "cpu_baseline": None}
+
+
 # Steps per timed window.  Under the reference's failure model (PDLSM bond
 # coefficients of the intact family kept while bonds break) C2 and C4 as
 # configured run away after crack growth starts: C2 from about step 280 (the
@@ -441,7 +492,9 @@ def main():
                     help="lanes per PD family (-1: timed on the model by the library's autotuner, the default; "
                          "0: the library's fixed default)")
     ap.add_argument("--fe-lanes", type=int, default=-1, help="lanes per FE-only node (-1: timed, 0: fixed default)")
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--fc1-n", type=int, default=201, help="fc1: nodes per side of the plate")
+    ap.add_argument("--fc1-increments", type=int, default=15, help="fc1: quasi-static increments timed")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "fc1"],
                     help="c2: 3D box with hole (default); c1: 2D strip plate; c4: batch of uneven 2D plates in "
                          "one launch; c3: quasi-static increments, Krylov methods beside a CPU direct solve; "
                          "c5: implicit Newmark, learned vs plain preconditioner")
@@ -462,6 +515,9 @@ def main():
         return
     if args.workload == "c3":
         print(json.dumps(bench_quasi(args)))
+        return
+    if args.workload == "fc1":
+        print(json.dumps(bench_fc1(args)))
         return
     ws, rank, local = dist_env()
     dist = None

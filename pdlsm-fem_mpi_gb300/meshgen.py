@@ -312,6 +312,18 @@ def plate_edge_crack(n: int = 31, L: float = 0.03, a_frac: float = 0.41, pd_band
                    material=(72e9, 0.22, 2440.0, KIc, 1.0e8), protype=protype)
 
 
+def fc1_bench_case(n: int = 201, nsteps: int = 15):
+    """FC 1 crack growth: n x n-node FE plate (30 mm), edge pre-crack to 0.41 W,
+    K_Ic = 1 MPa m^0.5, top edge pulled 1e-6 m per load step, default FC 1
+    (mr 6, dcf 1), reaction forces of the pulled edge; returns (mesh, write_case
+    keywords).  At n = 201 the crack first grows at increment 5."""
+    mesh = plate_edge_crack(n=n, KIc=1.0e6, title="pe201" if n == 201 else f"pe{n}")
+    mesh.ebcs[2].velocity = 1e-6
+    kw = dict(solver="QUASI-STATIC", dt=1.0, nsteps=nsteps, save=nsteps, factor=3.015, nlf=1.0, lumped=False,
+              fc="1", extra=["RF 2", "SOLVE BICGSTAB 1e-10 20000"])
+    return mesh, kw
+
+
 def box_hole(nx: int = 121, ny: int = 61, nz: int = 21, h: float = 1e-3,
              radius: float = 8e-3, pd_x: int = 40, pd_y: int = 40,
              title: str = "boxHole") -> Mesh:

@@ -216,6 +216,17 @@ def fc1_cases() -> None:
     for name in ("pe31_fc1", "pe31_fc1m"):
         d = run(d2, name + ".in", "quasi_fc1")
         save(name, {k: d[k] for k in keep})
+    # the FC 1 bench plate (201 x 201 nodes, 15 increments): crack path,
+    # region growth and final families and bonds; its inputs are regenerated
+    # by the test (meshgen.fc1_bench_case) and pinned by digest
+    d201 = os.path.join(work, "pe201")
+    mesh, kw = meshgen.fc1_bench_case()
+    meshgen.write_case(mesh, d201, "pe201_fc1", **kw)
+    d = run(d201, "pe201_fc1.in", "quasi_fc1")
+    out = {k: d[k] for k in ("crack_rows", "region_rows", "pde_final", "fam_off_final", "fam_members_final",
+                             "bond_state_final", "rf_rows")}
+    out["input_sha256"] = input_digest(d201, "pe201_fc1")
+    save("pe201_fc1", out)
     shutil.rmtree(work)
 
 

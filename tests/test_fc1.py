@@ -121,3 +121,63 @@ def test_fc1_run_writes_the_crack_path_file(built, tmp_path):
     last = lines[-1].split("\t")
     assert float(last[1]) == pytest.approx(g["crack_rows"][-1, 0, 1], rel=1e-3)
     assert float(last[3]) == pytest.approx(g["crack_rows"][-1, 0, 3], rel=1e-3)
+
+
+def _bench_plate(tmp_path):
+    """The 201 x 201-node FC 1 bench plate, regenerated and checked against
+    the digest of the inputs the reference ran."""
+    import hashlib
+    import meshgen
+    mesh, kw = meshgen.fc1_bench_case()
+    cmd = meshgen.write_case(mesh, str(tmp_path), "pe201_fc1", **kw)
+    h = hashlib.sha256()
+    for ext in (".in", ".lis"):
+        h.update(open(str(tmp_path / ("pe201_fc1" + ext)), "rb").read())
+    g = golden("pe201_fc1")
+    assert h.hexdigest() == str(g["input_sha256"])
+    return cmd, g
+
+
+def test_crack_advance_reproduces_the_reference_region_growth_on_the_bench_plate(built, tmp_path):
+    cmd, g = _bench_plate(tmp_path)
+    tips, moved = _moves(g)
+    m = pdx.Model(cmd, device=-1)
+    for i in range(tips.shape[0]):
+        if moved[i].any():
+            m.crack_advance(tips[i], moved[i])
+    np.testing.assert_array_equal(m.array("pde_idx"), g["pde_final"])
+    np.testing.assert_array_equal(m.array("fam_off"), g["fam_off_final"])
+    np.testing.assert_array_equal(m.array("fam_members"), g["fam_members_final"])
+    np.testing.assert_array_equal(m.array("bond_state0"), g["bond_state_final"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", [2, 8])
+def test_fc1_bench_plate_matches_reference(built, tmp_path, method):
+    """The 201 x 201-node bench plate (80,199 equations), 15 increments with
+    BiCGStab (method 2) and with the two-level BiCGStab (method 8, whose
+    coarse inverse is re-formed after each growth): the reference's ten
+    growth steps and its arrest at increment 14, tips to 1e-9 of the plate,
+    KI and KII to 1e-6 of the largest |K|, and the final PD elements,
+    families and bonds exactly."""
+    cmd, g = _bench_plate(tmp_path)
+    rows, region = g["crack_rows"], g["region_rows"]
+    kmax = np.abs(rows[:, :, 3:5]).max()
+    worst_k = 0.0
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        m.quasi_init()
+        for i in range(rows.shape[0]):
+            assert m.quasi_step(method).converged
+            cs = m.crack_state()
+            assert np.abs(cs[:, 2:4] - rows[i, :, 1:3]).max() <= 1e-9 * 0.03, f"increment {i + 1}"
+            worst_k = max(worst_k, float(np.abs(cs[:, 4:6] - rows[i, :, 3:5]).max()) / kmax)
+            np.testing.assert_array_equal(cs[:, 7] == 1, region[i, 2] == 0)
+        _, _, _, bs = m.state()
+        np.testing.assert_array_equal(m.array("pde_idx"), g["pde_final"])
+        np.testing.assert_array_equal(m.array("fam_off"), g["fam_off_final"])
+        np.testing.assert_array_equal(bs, g["bond_state_final"])
+        rf = m.reaction_forces()
+    print(f"\n[pe201_fc1, method {method}] worst K error {worst_k:.2e} of max |K|")
+    assert worst_k < 1e-6
+    ref_rf = g["rf_rows"]
+    assert np.abs(rf[1:, 1:4] - ref_rf[:, 2:5]).max() <= 1e-6 * np.abs(ref_rf[:, 2:5]).max()
