@@ -1,6 +1,7 @@
 // The reference-side binding of the C ABI: the bodies a maintainer of the
-// reference (QibangLiu/PDLSM-FEM_mpi) puts in place of its four inner seams so
-// that its solver loops call this library.  Each body replaces the member
+// reference (QibangLiu/PDLSM-FEM_mpi) puts in place of its four inner seams
+// (and of its FC 1 crack-growth step) so that its solver loops call this
+// library.  Each body replaces the member
 // function of the same name in SourceFiles/Solver/pdsolve.cpp or
 // calMatrixOperations.cpp; everything else in the reference stays as it is.
 //
@@ -80,4 +81,36 @@ void pdsolve::pdfemAssembleEquasSys_CSRformat(datModel& o_dat, int numEq) {
   if (!cdp_KuGlo) cdp_KuGlo = new double[info.nnz];
   if (!cdp_FGlo) cdp_FGlo = new double[numEq];
   pdx_or_exit(pdx_assemble_csr(g_pdx, 1, nullptr, cip_ia, cip_ja, cdp_KuGlo, cdp_FGlo), 1);
+}
+
+// Seam 5: pdsolve::b_cracPropag_qusiaStatic_BYKeq (pdsolve.cpp:7375-7495), for
+// a quasi-static loop whose increments run through pdx_quasi_step (which ends
+// with the FC 1 pass on the GPU model: SIFs, tip growth, PD-region growth and
+// bond cuts).  The body copies the library's crack segments into the
+// reference's crack records, writes the crack-path row the reference writes
+// and returns whether a tip moved, with KEQ the last crack's Keq (the value
+// failureProcess scales the next load step by).
+bool pdsolve::b_cracPropag_qusiaStatic_BYKeq(datModel& o_dat, ofstream& cracPath, double& KEQ) {
+  int nc = 0;
+  pdx_or_exit(pdx_crack_state(g_pdx, nullptr, 0, &nc), 1);
+  std::vector<double> rows((size_t)nc * 8);
+  pdx_or_exit(pdx_crack_state(g_pdx, rows.data(), nc, nullptr), 1);
+  bool moved = false;
+  for (int ck = 0; ck < nc && ck < o_dat.ci_numCrack; ck++) {
+    const double* r = &rows[(size_t)ck * 8];
+    o_dat.cdp_crack[ck][0][0] = r[0];
+    o_dat.cdp_crack[ck][0][1] = r[1];
+    o_dat.cdp_crack[ck][1][0] = r[2];
+    o_dat.cdp_crack[ck][1][1] = r[3];
+    KEQ = r[6];
+    moved = moved || r[7] != 0.0;
+  }
+  if (ci_rank == 0 && nc > 0) {
+    const double* last = &rows[(size_t)(nc - 1) * 8];
+    for (int ck = 0; ck < nc; ck++)
+      cracPath << ck << "\t" << rows[(size_t)ck * 8 + 2] << "\t" << rows[(size_t)ck * 8 + 3] << "\t" << last[4]
+               << "\t" << last[5] << "\t" << last[6] << " \"***\"\t";
+    cracPath << endl;
+  }
+  return moved;
 }

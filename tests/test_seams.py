@@ -2,7 +2,8 @@
 
 tests/integration/seams.cpp holds the bodies a maintainer of the reference
 puts in place of its four inner seams (calinternalForce_CSRformat,
-timeIntegration_LM, cluster_PARDISO_64Solver, pdfemAssembleEquasSys_CSRformat).
+timeIntegration_LM, cluster_PARDISO_64Solver, pdfemAssembleEquasSys_CSRformat)
+and of its FC 1 crack-growth step (b_cracPropag_qusiaStatic_BYKeq).
 Compiling it with the reference's HeaderFiles/Solver, the MPI/MKL shim headers
 and include/pdx.h checks that the ABI's prototypes take the reference's
 argument types (long long CSR indices, Vector::cdp_vecCoeff) without casts.
