@@ -100,7 +100,11 @@ pdx_status pdx_model_get_info(const pdx_model* m, pdx_model_info* info);
  * class | 1 << 14 when the PD part reads the node's FP32 record, -1 none),
  * "lat_blk" (f32, per class 9 blocks of 2 x 2 by lattice offset
  * (dx + 1) + 3 (dy + 1)), "fe_rest" (int32: the FE-only items, in "feonly"
- * order, that no tile covers). */
+ * order, that no tile covers); the assembly's scatter map (int32): "rel_bond"
+ * (per bond, the offset of the neighbour's first column in its node's rows),
+ * "rel_self" (per family, the node's own), "rel_fe" (8 per node-element
+ * adjacency entry), with "fe_adj_ptr", "fe_adj" (element << 3 | local node)
+ * and "fe_conn" (8 node ids per FE element, in "fe_idx" order). */
 pdx_status pdx_model_array_len(const pdx_model* m, const char* name, int64_t* count);
 pdx_status pdx_model_array(const pdx_model* m, const char* name, void* dst, int64_t count);
 

@@ -14,7 +14,6 @@
 namespace pdx {
 
 const int kEqTemps = 8;
-bool prepare_model(pdx_model* m, Error& err);
 
 namespace {
 thread_local std::string g_err;
@@ -340,7 +339,8 @@ pdx_status rebuild_device(pdx_model* m) {
   m->newmark_ready = false;
   m->prep = Prepared();
   Error err{0, ""};
-  if (!prepare_model(m, err)) return set_error(err.code == 6 ? PDX_ERR_SINGULAR : PDX_ERR_PARSE, err.msg);
+  // a rebuild serves the quasi-static FC 1 loop: no explicit step tables
+  if (!prepare_model(m, err, false)) return set_error(err.code == 6 ? PDX_ERR_SINGULAR : PDX_ERR_PARSE, err.msg);
   st = upload_model(m);
   if (st) return st;
   for (int i = 0; i < 2; i++) cudaMemcpyAsync(m->d_u[i], u.data(), nd * 8, cudaMemcpyHostToDevice, m->stream);
@@ -823,6 +823,12 @@ static bool array_ref(const pdx_model* m, const std::string& n, const void** ptr
   if (n == "tile_cls") return set(p.tile_cls.data(), p.tile_cls.size(), 2);
   if (n == "lat_blk") return set(p.lat_blk.data(), p.lat_blk.size(), 4);
   if (n == "fe_rest") return set(p.fe_rest.data(), p.fe_rest.size(), 4);
+  if (n == "rel_bond") return set(p.rel_bond.data(), p.rel_bond.size(), 4);
+  if (n == "rel_self") return set(p.rel_self.data(), p.rel_self.size(), 4);
+  if (n == "rel_fe") return set(p.rel_fe.data(), p.rel_fe.size(), 4);
+  if (n == "fe_adj_ptr") return set(p.fe_adj_ptr.data(), p.fe_adj_ptr.size(), 4);
+  if (n == "fe_adj") return set(p.fe_adj.data(), p.fe_adj.size(), 4);
+  if (n == "fe_conn") return set(p.fe_conn.data(), p.fe_conn.size(), 4);
   if (n == "bcflag") return set(p.bcflag.data(), p.bcflag.size(), 1);
   if (n == "dtv") return set(p.dtv.data(), p.dtv.size(), 8);
   if (n == "material") {

@@ -277,7 +277,14 @@ pdx_status apply_growth(pdx_model* m, const std::vector<std::array<double, 9>>& 
   int cut = 0;
   for (const auto& seg : moved) cut += cut_bonds_by_segment(m->mesh, m->setup, seg);
   if (grew || cut > 0) m->fc1_changed = true;
-  if (!m->has_device) return PDX_OK;
+  if (!m->has_device) {
+    // a host-only model keeps its host arrays in step with the set-up
+    if (!grew && cut == 0) return PDX_OK;
+    m->prep = Prepared();
+    Error err{0, ""};
+    if (!prepare_model(m, err, false)) return set_error(PDX_ERR_INVALID, err.msg);
+    return PDX_OK;
+  }
   if (grew) return rebuild_device(m);
   if (cut > 0) return upload_bond_states(m);
   return PDX_OK;

@@ -112,6 +112,7 @@ struct Setup {
   // crack-cut elements found so far (civ_CracEleIDX), kept for FC 1 growth
   std::vector<int> algo;
   std::vector<int> crack_elems;
+  std::vector<int> node_elem_ptr, node_elem;   // elements around each node (n_node + 1 offsets)
 };
 
 struct Model;

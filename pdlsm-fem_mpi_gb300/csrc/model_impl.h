@@ -212,6 +212,10 @@ struct pdx_model {
 
 namespace pdx {
 pdx_status set_error(pdx_status code, const std::string& msg);
+// host arrays the kernels need, from m->setup (prepare.cpp); step_tables =
+// false leaves out the explicit step's FE-only node stencils and tiles (the
+// step then takes the element path for those nodes)
+bool prepare_model(pdx_model* m, Error& err, bool step_tables = true);
 pdx_status cuda_check(cudaError_t e, const char* what);
 void write_vtk(const pdx_model* m, const std::string& path, const std::vector<double>& u_all,
                const std::vector<double>& sigma, const std::vector<double>& phi, bool binary);

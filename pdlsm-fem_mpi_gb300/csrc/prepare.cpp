@@ -337,7 +337,7 @@ void build_fe_tiles(const Mesh& me, const Setup& s, Prepared& p) {
   p.n_tiles = n_tiles;
 }
 
-bool prepare_model(pdx_model* m, Error& err) {
+bool prepare_model(pdx_model* m, Error& err, bool step_tables) {
   const Mesh& me = m->mesh;
   const Setup& s = m->setup;
   const Command& c = m->cmd;
@@ -554,8 +554,12 @@ bool prepare_model(pdx_model* m, Error& err) {
     if (p.fe_adj_ptr[k + 1] - p.fe_adj_ptr[k] > kMaxFeAdj && D == 3) {
       err.code = 3; err.msg = "more than 8 FE elements around a node"; return false;
     }
-  build_stencils(me, p);
-  build_fe_tiles(me, s, p);
+  // node stencils and lattice tiles of FE-only nodes: tables of the explicit
+  // step only (without them it takes the element path, same results)
+  if (step_tables) {
+    build_stencils(me, p);
+    build_fe_tiles(me, s, p);
+  }
   // traction BCs: unit forces per node and NBC
   {
     std::map<std::pair<int, int>, std::array<double, 3>> acc;
@@ -587,29 +591,30 @@ bool prepare_model(pdx_model* m, Error& err) {
     }
   }
   // scatter map: offset of every neighbour's first column inside a node's rows
-  // (none without a CSR pattern: batch specimens)
+  // (none without a CSR pattern: batch specimens).  Equations are numbered in
+  // node order, so a row's columns are sorted by node, and the offset of node
+  // n's first column in node k's rows is the number of the row's columns
+  // below n's first equation (eq_start[n]); all rows of a node have the same
+  // columns.  A node without a row (every DOF prescribed) is never written.
   if (!s.csr_ia.empty()) {
-    std::vector<std::vector<int>> inter(N);
-    for (int f = 0; f < nf; f++)
-      inter[s.fam_node[f]].assign(s.fam_members.begin() + s.fam_off[f], s.fam_members.begin() + s.fam_off[f + 1]);
-    for (int i = 0; i < nfe; i++)
-      for (int a = 0; a < nen; a++)
-        for (int b = 0; b < nen; b++) inter[p.fe_conn[(size_t)i * 8 + a]].push_back(p.fe_conn[(size_t)i * 8 + b]);
-    std::vector<std::vector<int>> off(N);
+    std::vector<int64_t> eq_start((size_t)N + 1, 0);
+    std::vector<int64_t> first_row(N, -1);
     for (int k = 0; k < N; k++) {
-      auto& v = inter[k];
-      std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
-      off[k].resize(v.size());
-      int o = 0;
-      for (size_t j = 0; j < v.size(); j++) {
-        off[k][j] = o;
-        for (int d = 0; d < D; d++) o += s.eq[(size_t)v[j] * D + d] >= 0 ? 1 : 0;
+      int64_t c = 0;
+      for (int d = 0; d < D; d++) {
+        const int e = s.eq[(size_t)k * D + d];
+        if (e < 0) continue;
+        if (first_row[k] < 0) first_row[k] = e;
+        c++;
       }
+      eq_start[k + 1] = eq_start[k] + c;
     }
-    auto lookup = [&](int k, int n) {
-      auto it = std::lower_bound(inter[k].begin(), inter[k].end(), n);
-      return off[k][it - inter[k].begin()];
+    auto lookup = [&](int k, int n) -> int {
+      const int64_t r = first_row[k];
+      if (r < 0) return 0;
+      const int64_t* b = s.csr_ja.data() + s.csr_ia[r];
+      const int64_t* e = s.csr_ja.data() + s.csr_ia[r + 1];
+      return (int)(std::lower_bound(b, e, eq_start[n]) - b);
     };
     p.rel_bond.assign(nb, 0);
     p.rel_self.assign(nf, 0);

@@ -298,6 +298,54 @@ int cut_bonds(const Ctx& cx, const std::array<double, 9>& cr) {
   return cut;
 }
 
+// The CSR pattern after the element types of the nodes in `nodes` (sorted,
+// unique) changed: only those nodes' rows change (a row holds the node's own
+// family members and the nodes of the FE elements around it), so their
+// column sets are recomputed and every other row is copied.
+void update_csr_rows(const Ctx& cx, const std::vector<int>& nodes) {
+  Setup& s = cx.s;
+  const Mesh& m = cx.m;
+  const int D = m.dim;
+  std::vector<std::vector<int>> cols(nodes.size());
+  for (size_t i = 0; i < nodes.size(); i++) {
+    const int k = nodes[i];
+    std::vector<int>& v = cols[i];
+    const int f = s.fam_of_node[k];
+    if (f >= 0) v.assign(s.fam_members.begin() + s.fam_off[f], s.fam_members.begin() + s.fam_off[f + 1]);
+    for (int q = s.node_elem_ptr[k]; q < s.node_elem_ptr[k + 1]; q++) {
+      const int e = s.node_elem[q];
+      if (s.algo[e] != 2) continue;
+      const int* c = &m.conn[(size_t)e * 8];
+      v.insert(v.end(), c, c + m.elem_nn[e]);
+    }
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+  }
+  std::vector<int64_t> ia((size_t)s.n_eq + 1, 0), ja;
+  ja.reserve(s.csr_ja.size() + 64 * nodes.size());
+  size_t next = 0;
+  for (int k = 0; k < m.n_node; k++) {
+    const bool changed = next < nodes.size() && nodes[next] == k;
+    for (int d = 0; d < D; d++) {
+      const int row = s.eq[(size_t)k * D + d];
+      if (row < 0) continue;
+      if (changed) {
+        for (int j : cols[next])
+          for (int jj = 0; jj < D; jj++) {
+            const int col = s.eq[(size_t)j * D + jj];
+            if (col >= 0) ja.push_back(col);
+          }
+      } else {
+        ja.insert(ja.end(), s.csr_ja.begin() + s.csr_ia[row], s.csr_ja.begin() + s.csr_ia[row + 1]);
+      }
+      ia[(size_t)row + 1] = (int64_t)ja.size();
+    }
+    if (changed) next++;
+  }
+  s.csr_ia.swap(ia);
+  s.csr_ja.swap(ja);
+}
+
 }  // namespace
 
 bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int device, bool pattern) {
@@ -408,6 +456,17 @@ bool build_setup(const Mesh& m, const Command& cmd, Setup& s, Error& err, int de
   for (const auto& cr : m.cracks) cut_bonds(cx, cr);
   s.algo = cx.algo;
   s.crack_elems = cx.crack_elems;
+  // elements around each node, for the CSR rows an FC 1 growth changes
+  s.node_elem_ptr.assign((size_t)N + 1, 0);
+  for (int e = 0; e < E; e++)
+    for (int a = 0; a < m.elem_nn[e]; a++) s.node_elem_ptr[m.conn[(size_t)e * 8 + a] + 1]++;
+  for (int k = 0; k < N; k++) s.node_elem_ptr[k + 1] += s.node_elem_ptr[k];
+  s.node_elem.assign(s.node_elem_ptr[N], 0);
+  {
+    std::vector<int> fill(s.node_elem_ptr.begin(), s.node_elem_ptr.end() - 1);
+    for (int e = 0; e < E; e++)
+      for (int a = 0; a < m.elem_nn[e]; a++) s.node_elem[fill[m.conn[(size_t)e * 8 + a]]++] = e;
+  }
   if (!pattern) return true;   // batch specimens: no CSR pattern (not merged)
   if (device >= 0) return gpu_csr_pattern(m, s, device, err);   // k_setup.cu
   build_csr_pattern(m, s);
@@ -458,7 +517,12 @@ void grow_pd_region(const Mesh& m, const Command& cmd, Setup& s, const std::vect
   }
   host_members(cx, f0, node_horizons(m, cmd, s));
   s.bond_state.resize(s.fam_members.size(), 1);
-  build_csr_pattern(m, s);
+  std::vector<int> touched;
+  for (size_t i = old_pde; i < s.pde.size(); i++)
+    for (int a = 0; a < m.elem_nn[s.pde[i]]; a++) touched.push_back(m.conn[(size_t)s.pde[i] * 8 + a]);
+  std::sort(touched.begin(), touched.end());
+  touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+  update_csr_rows(cx, touched);
 }
 
 int cut_bonds_by_segment(const Mesh& m, Setup& s, const std::array<double, 9>& seg) {

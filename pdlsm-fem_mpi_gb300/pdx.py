@@ -147,7 +147,8 @@ _ARRAY_DTYPES = {"eq": np.int32, "vol_node": np.float64, "vol_elem": np.float64,
                  "X": np.float64, "conn": np.int32, "elem_nn": np.int32, "bcflag": np.uint8, "dtv": np.float64,
                  "material": np.float64, "feonly": np.int32, "st_cls": np.int32, "st_nbr": np.int32,
                  "st_blk": np.float64, "tile_rows": np.int32, "tile_cls": np.int16, "lat_blk": np.float32,
-                 "fe_rest": np.int32}
+                 "fe_rest": np.int32, "rel_bond": np.int32, "rel_self": np.int32, "rel_fe": np.int32,
+                 "fe_adj_ptr": np.int32, "fe_adj": np.int32, "fe_conn": np.int32}
 
 
 class Model:

@@ -67,6 +67,57 @@ def test_crack_advance_reproduces_the_reference_region_growth(built, name):
     np.testing.assert_array_equal(cs[:, 2:4], tips[-1])
 
 
+def _pattern_from_definition(m):
+    """CSR pattern and scatter-map offsets from their definition: node k's
+    rows hold its family members and the nodes of the FE elements around it;
+    the offset of neighbour n counts the active DOFs of the row's nodes
+    below n."""
+    D = m.dim
+    eq = m.array("eq").reshape(-1, D)
+    N = eq.shape[0]
+    off, mem = m.array("fam_off"), m.array("fam_members")
+    conn, nn = m.array("conn").reshape(-1, 8), m.array("elem_nn")
+    rows = [set() for _ in range(N)]
+    for f in range(len(off) - 1):
+        rows[mem[off[f]]].update(mem[off[f]:off[f + 1]].tolist())
+    for e in m.array("fe_idx"):
+        el = conn[e, :nn[e]].tolist()
+        for a in el:
+            rows[a].update(el)
+    ia, ja = [0], []
+    for k in range(N):
+        cols = [c for j in sorted(rows[k]) for c in eq[j] if c >= 0]
+        for d in range(D):
+            if eq[k, d] >= 0:
+                ja.extend(cols)
+                ia.append(len(ja))
+    return np.array(ia), np.array(ja), rows, (eq >= 0).sum(axis=1)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_grown_model_keeps_pattern_and_scatter_map_consistent(built, name):
+    """After the reference's growth sequence, the CSR pattern (only the rows
+    of the new PD elements' nodes are rebuilt) and the assembly's scatter map
+    equal their definitions."""
+    g = golden(name)
+    tips, moved = _moves(g)
+    m = pdx.Model(case_cmd("pe31", name), device=-1)
+    for i in range(tips.shape[0]):
+        if moved[i].any():
+            m.crack_advance(tips[i], moved[i])
+    ia, ja, rows, nact = _pattern_from_definition(m)
+    np.testing.assert_array_equal(m.array("csr_ia"), ia)
+    np.testing.assert_array_equal(m.array("csr_ja"), ja)
+    off, mem, rel_bond = m.array("fam_off"), m.array("fam_members"), m.array("rel_bond")
+    b = 0
+    for f in range(len(off) - 1):
+        k = mem[off[f]]
+        for q in range(off[f] + 1, off[f + 1]):
+            if nact[k]:
+                assert rel_bond[b] == sum(nact[j] for j in rows[k] if j < mem[q])
+            b += 1
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", CASES)
 def test_fc1_quasi_static_run_matches_reference(built, name):

@@ -191,3 +191,47 @@ def test_step_at_a_time_entry_points_need_a_device():
         assert e.value.code in (4, 8)
     assert host.learned_active() is False
     assert host.learned_samples() == 0
+
+
+@pytest.mark.parametrize("case,cmd", CASES + [("pe31", "pe31_fc1")])
+def test_scatter_map_offsets_count_the_columns_of_lower_nodes(built, case, cmd):
+    """The assembly's scatter map against its definition: the offset of
+    neighbour n in node k's rows is the number of active DOFs of the nodes
+    below n among k's row nodes (k's family members and the nodes of the FE
+    elements around k, sorted, without repeats)."""
+    m = pdx.Model(case_cmd(case, cmd), device=-1)
+    D = m.dim
+    eq = m.array("eq").reshape(-1, D)
+    nact = (eq >= 0).sum(axis=1)
+    off, mem = m.array("fam_off"), m.array("fam_members")
+    fe_conn = m.array("fe_conn").reshape(-1, 8)
+    nen = 4 if D == 2 else 8
+    N = eq.shape[0]
+    rows = [set() for _ in range(N)]
+    for f in range(len(off) - 1):
+        rows[mem[off[f]]].update(mem[off[f]:off[f + 1]].tolist())
+    for el in fe_conn:
+        for a in el[:nen]:
+            rows[a].update(el[:nen].tolist())
+
+    def rel(k, n):
+        return int(sum(nact[j] for j in rows[k] if j < n))
+
+    rel_bond, rel_self = m.array("rel_bond"), m.array("rel_self")
+    b = 0
+    for f in range(len(off) - 1):
+        k = mem[off[f]]
+        if nact[k]:
+            assert rel_self[f] == rel(k, k)
+        for q in range(off[f] + 1, off[f + 1]):
+            if nact[k]:
+                assert rel_bond[b] == rel(k, mem[q])
+            b += 1
+    ptr, adj, rfe = m.array("fe_adj_ptr"), m.array("fe_adj"), m.array("rel_fe").reshape(-1, 8)
+    for k in range(N):
+        if not nact[k]:
+            continue
+        for j in range(ptr[k], ptr[k + 1]):
+            el = fe_conn[adj[j] >> 3]
+            for a in range(nen):
+                assert rfe[j, a] == rel(k, el[a])
