@@ -10,7 +10,7 @@ same models without the reference.
 Needs the reference tree (PDX_REFERENCE, or the checkout that
 __graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
-[--size-only] [--fc1-only]
+[--size-only] [--fc1-only] [--fc1-examples]
 """
 from __future__ import annotations
 
@@ -230,6 +230,35 @@ def fc1_cases() -> None:
     shutil.rmtree(work)
 
 
+# examples/DCT, the third FC 1 deck, is meshed with 3-node triangles, which
+# the library does not read
+FC1_EXAMPLES = (("DiagPlate", "DiagPlate_quasistatic_FC1"), ("plateCrack", "platCrack_quasiStatic_FC1"))
+
+
+def fc1_example_cases() -> None:
+    """The reference's own FC 1 example decks (examples/DiagPlate, plateCrack:
+    5.8k and 7.1k-node plates, two cracks each, 54 and 60 increments)
+    run through its quasi-static loop: crack path, PD-region growth and final
+    families and bonds, with a digest of the deck files.  The decks stay in the
+    reference tree; the tests read them there and skip without it."""
+    import hashlib
+    work = tempfile.mkdtemp(prefix="golden_fc1ex_")
+    for folder, name in FC1_EXAMPLES:
+        src = os.path.join(REF, "examples", folder)
+        dst = os.path.join(work, folder)
+        shutil.copytree(src, dst)
+        d = run(dst, name + ".in", "quasi_fc1")
+        h = hashlib.sha256()
+        lis = [ln.split()[1] for ln in open(os.path.join(src, name + ".in")) if ln.startswith("MSHFILE")][0]
+        for f in (name + ".in", lis):
+            h.update(open(os.path.join(src, f), "rb").read())
+        out = {k: d[k] for k in ("crack_rows", "region_rows", "pde_final", "fam_off_final", "fam_members_final",
+                                 "bond_state_final")}
+        out["input_sha256"] = np.array(h.hexdigest())
+        save("ex_" + folder + "_fc1", out)
+    shutil.rmtree(work)
+
+
 def rf_cases() -> None:
     """Reaction forces (RF 2: the top edge's essential BC) of the 2D plate over
     60 explicit steps, no failure criterion."""
@@ -351,6 +380,10 @@ if __name__ == "__main__":
     if "--fc1-only" in sys.argv:
         build_driver()
         fc1_cases()
+        sys.exit(0)
+    if "--fc1-examples" in sys.argv:
+        build_driver()
+        fc1_example_cases()
         sys.exit(0)
     if "--fc2-only" in sys.argv or "--rf-only" in sys.argv or "--ascii-only" in sys.argv:
         build_driver()

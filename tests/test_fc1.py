@@ -232,3 +232,45 @@ def test_fc1_bench_plate_matches_reference(built, tmp_path, method):
     assert worst_k < 1e-6
     ref_rf = g["rf_rows"]
     assert np.abs(rf[1:, 1:4] - ref_rf[:, 2:5]).max() <= 1e-6 * np.abs(ref_rf[:, 2:5]).max()
+
+
+# The reference's third FC 1 deck, examples/DCT, is meshed with 3-node
+# triangles, which this library does not read.
+EXAMPLES = [("DiagPlate", "DiagPlate_quasistatic_FC1"), ("plateCrack", "platCrack_quasiStatic_FC1")]
+
+
+@pytest.mark.parametrize("folder,name", EXAMPLES)
+def test_crack_advance_on_the_reference_example_decks(built, folder, name):
+    """The reference's own FC 1 example decks (read in the reference tree;
+    skipped without it): their crack paths, as the reference's loop produced
+    them (tests/golden/ex_*_fc1.npz), replayed through pdx_crack_advance give
+    the reference's PD elements, families, members and bond states: two
+    cracks growing from a plate's centre in opposite directions (DiagPlate,
+    48 growth increments, 54 in all; plateCrack), inside a PD region laid out
+    along the crack path in advance."""
+    import hashlib
+    import os
+    from conftest import reference_tree
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    g = golden("ex_" + folder + "_fc1")
+    src = os.path.join(ref, "examples", folder)
+    cmd = os.path.join(src, name + ".in")
+    lis = [ln.split()[1] for ln in open(cmd) if ln.startswith("MSHFILE")][0]
+    h = hashlib.sha256()
+    for f in (cmd, os.path.join(src, lis)):
+        h.update(open(f, "rb").read())
+    assert h.hexdigest() == str(g["input_sha256"])
+    tips, moved = _moves(g)
+    m = pdx.Model(cmd, device=-1)
+    for i in range(tips.shape[0]):
+        if moved[i].any():
+            m.crack_advance(tips[i], moved[i])
+            assert m.array_len("pde_idx") == int(g["region_rows"][i, 0])
+    np.testing.assert_array_equal(m.array("pde_idx"), g["pde_final"])
+    np.testing.assert_array_equal(m.array("fam_off"), g["fam_off_final"])
+    np.testing.assert_array_equal(m.array("fam_members"), g["fam_members_final"])
+    np.testing.assert_array_equal(m.array("bond_state0"), g["bond_state_final"])
+    print(f"\n[{folder}] {int(moved.any(axis=1).sum())} growth increments, {m.array_len('pde_idx')} PD elements, "
+          f"{int((m.array('bond_state0') == 0).sum())} broken bonds")
