@@ -317,7 +317,7 @@ static pdx_status upload_model(pdx_model* m) {
   return PDX_OK;
 }
 
-pdx_status rebuild_device(pdx_model* m) {
+pdx_status rebuild_device(pdx_model* m, bool keep_twolevel) {
   const size_t nd = (size_t)m->mesh.n_node * m->mesh.dim;
   std::vector<double> u(nd), sig((size_t)m->mesh.n_node * 6), rf;
   cudaMemcpyAsync(u.data(), m->d_u[0], nd * 8, cudaMemcpyDeviceToHost, m->stream);
@@ -333,7 +333,8 @@ pdx_status rebuild_device(pdx_model* m) {
     m->graph = nullptr;
   }
   learned_destroy(m);
-  twolevel_destroy(m);
+  if (keep_twolevel && m->twolevel) m->twolevel->dev.keep_stale = true;
+  else twolevel_destroy(m);
   m->buf.free_all();
   m->d_vel = m->d_acc = nullptr;
   m->newmark_ready = false;

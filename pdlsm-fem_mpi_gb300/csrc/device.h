@@ -290,6 +290,12 @@ struct TwoLevelDev {
   // host side: the fingerprint of the values whose coarse inverse M holds
   bool have_inverse = false;
   unsigned long long inverse_of = 0;
+  // host side: keep_stale lets the inverse serve a changed matrix (set after
+  // a local change such as an FC 1 growth step) while a solve needs at most
+  // 1.5 times the iterations of the first solve with it (its_ref)
+  bool keep_stale = false;
+  bool formed = false;        // the last set-up formed the inverse
+  int its_ref = 0;
 };
 cudaError_t twolevel_setup(const DevCsr& A, TwoLevelDev& t, cudaStream_t s, bool* usable);
 cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method, double rtol, int max_iter,

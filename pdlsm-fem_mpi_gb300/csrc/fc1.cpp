@@ -273,6 +273,7 @@ pdx_status fc1_pass(pdx_model* m, bool grow) {
 
 pdx_status apply_growth(pdx_model* m, const std::vector<std::array<double, 9>>& moved) {
   bool grew = false;
+  const int f0 = (int)m->setup.fam_node.size();
   grow_pd_region(m->mesh, m->cmd, m->setup, moved, &grew);
   int cut = 0;
   for (const auto& seg : moved) cut += cut_bonds_by_segment(m->mesh, m->setup, seg);
@@ -285,8 +286,27 @@ pdx_status apply_growth(pdx_model* m, const std::vector<std::array<double, 9>>& 
     if (!prepare_model(m, err, false)) return set_error(PDX_ERR_INVALID, err.msg);
     return PDX_OK;
   }
-  if (grew) return rebuild_device(m);
-  if (cut > 0) return upload_bond_states(m);
+  if (grew) {
+    // Method 8's coarse grid stays valid while no coupling is longer than a
+    // coarse cell: only the new families add couplings.  Its inverse then
+    // keeps serving the locally changed matrix (formed anew once the
+    // iterations grow by half).
+    bool keep = m->twolevel != nullptr;
+    const Setup& s = m->setup;
+    for (int f = f0; keep && f < (int)s.fam_node.size(); f++) {
+      const double* xk = &m->mesh.X[(size_t)s.fam_node[f] * 3];
+      for (int64_t q = s.fam_off[f] + 1; keep && q < s.fam_off[f + 1]; q++) {
+        const double* xm = &m->mesh.X[(size_t)s.fam_members[q] * 3];
+        for (int a = 0; a < 2; a++)
+          if (std::fabs(xm[a] - xk[a]) * 1.001 > m->twolevel->cell_len[a]) keep = false;
+      }
+    }
+    return rebuild_device(m, keep);
+  }
+  if (cut > 0) {
+    if (m->twolevel) m->twolevel->dev.keep_stale = true;
+    return upload_bond_states(m);
+  }
   return PDX_OK;
 }
 

@@ -1096,11 +1096,13 @@ cudaError_t twolevel_setup(const DevCsr& A, TwoLevelDev& t, cudaStream_t s, bool
   cudaMemcpyAsync(&h, t.hash, sizeof(h), cudaMemcpyDeviceToHost, s);
   cudaError_t e0 = cudaStreamSynchronize(s);
   if (e0 != cudaSuccess) return e0;
-  if (t.have_inverse && h == t.inverse_of) {
+  t.formed = false;
+  if (t.have_inverse && (h == t.inverse_of || t.keep_stale)) {
     *usable = true;
     return cudaSuccess;
   }
   t.have_inverse = false;
+  t.formed = true;
   k_tl_ap<<<(int)((A.n * 32 + 255) / 256), 256, 0, s>>>(A.n, A.ia, A.ja, A.a, t);
   k_tl_init<<<1024, 256, 0, s>>>(t);
   k_tl_coarse<<<nc, 64, 0, s>>>(t);
@@ -1205,6 +1207,12 @@ cudaError_t krylov_solve(const DevCsr& A, const double* b, double* x, int method
     iters = bicg_core<double>(c, n, avg, A.ia, A.ja, A.a, b, x, dinv, rtol, max_iter, 0, dscal, w, part2, ticket,
                               two_level ? tl : nullptr);
     if (method == 8 && !two_level) method = 2;
+    if (method == 8 && tl) {
+      // an inverse kept for a changed matrix is formed anew once it costs
+      // half as many iterations again as when it was formed
+      if (tl->formed) tl->its_ref = iters;
+      else if (tl->keep_stale && iters > tl->its_ref + tl->its_ref / 2) tl->have_inverse = false;
+    }
     cudaFreeAsync(part2, s);
     for (int k : {1, 2, 4, 5, 6, 7}) cudaFreeAsync(w[k], s);
   } else if (method == 3 || method == 7) {

@@ -257,6 +257,7 @@ pdx_status twolevel_prepare(pdx_model* m) {
   }
   TwoLevelHost* T = new TwoLevelHost();
   m->twolevel = T;
+  for (int a = 0; a < 2; a++) T->cell_len[a] = (hi[a] - lo[a]) / std::max(1, cells_out[a]);
   TwoLevelDev& t = T->dev;
   cudaStream_t s = m->stream;
   t.nc = nc;

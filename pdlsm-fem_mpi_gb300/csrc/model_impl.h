@@ -107,6 +107,7 @@ struct Learned;
 struct TwoLevelHost {
   DevBuf buf;
   TwoLevelDev dev;
+  double cell_len[2] = {0.0, 0.0};   // coarse cell size per axis (no coupling may be longer)
 };
 
 }  // namespace pdx
@@ -239,8 +240,10 @@ pdx_status apply_growth(pdx_model* m, const std::vector<std::array<double, 9>>& 
 // and device model back to the mesh's (fc1.cpp)
 pdx_status fc1_reset(pdx_model* m);
 // the device model re-derived from m->setup after FC 1 changed it, keeping
-// displacements, node stresses and the reaction-force history (capi.cpp)
-pdx_status rebuild_device(pdx_model* m);
+// displacements, node stresses and the reaction-force history; with
+// keep_twolevel, method 8's coarse grid and inverse stay for the next solves
+// (capi.cpp)
+pdx_status rebuild_device(pdx_model* m, bool keep_twolevel = false);
 // bond states of m->setup uploaded into the device's state bits (capi.cpp)
 pdx_status upload_bond_states(pdx_model* m);
 pdx_status assemble_device(pdx_model* m, int mode, const double* d_v_all, int nbc_row);

@@ -274,3 +274,25 @@ def test_crack_advance_on_the_reference_example_decks(built, folder, name):
     np.testing.assert_array_equal(m.array("bond_state0"), g["bond_state_final"])
     print(f"\n[{folder}] {int(moved.any(axis=1).sum())} growth increments, {m.array_len('pde_idx')} PD elements, "
           f"{int((m.array('bond_state0') == 0).sum())} broken bonds")
+
+
+@pytest.mark.gpu
+def test_static_solve_reports_the_sifs_of_the_quasi_static_increment(built, tmp_path):
+    """A static solve with FC 1 evaluates the cracks once (the static
+    solver's failure pass): with the top edge held at 2e-7 m it is the second
+    increment of pe31_fc1 (the first carries no load), so KI, KII and Keq
+    equal the reference's for that increment, and the tip does not move."""
+    import meshgen
+    m0 = meshgen.plate_edge_crack(n=31, KIc=1.0e6, title="pe31")
+    m0.ebcs[2].value = 2e-7
+    m0.ebcs[2].velocity = None
+    cmd = meshgen.write_case(m0, str(tmp_path), "pe31_static", solver="STATIC", dt=1.0, nsteps=1, save=1,
+                             factor=3.015, nlf=1.0, lumped=False, fc="1", extra=["SOLVE BICGSTAB 1e-13 20000"])
+    g = golden("pe31_fc1")
+    with pdx.Model(cmd, device=0, precision=0) as m:
+        m.run(str(tmp_path / "out"))
+        cs = m.crack_state()
+    ref = g["crack_rows"][1, 0]
+    assert cs[0, 7] == 0
+    np.testing.assert_allclose(cs[0, 2:4], ref[1:3], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(cs[0, 4:7], ref[3:6], rtol=1e-7)
