@@ -206,14 +206,22 @@ class Model:
         t = np.ascontiguousarray(tips, dtype=np.float64).reshape(-1)
         mv = np.ascontiguousarray(moved, dtype=np.uint8).reshape(-1)
         _check(lib().pdx_crack_advance(self._h, t.ctypes.data_as(_D), mv.ctypes.data_as(C.POINTER(C.c_uint8))))
+        self._refresh_info()
+
+    def _refresh_info(self) -> None:
+        """FC 1 growth changes the family and bond counts and the CSR size."""
+        _check(lib().pdx_model_get_info(self._h, C.byref(self.info)))
 
     # ---- quasi-static increments ----
     def quasi_init(self) -> None:
         _check(lib().pdx_quasi_init(self._h))
+        self._refresh_info()
 
     def quasi_step(self, method: int = 1) -> "SolveInfo":
         info = SolveInfo()
         _check(lib().pdx_quasi_step(self._h, method, C.byref(info)))
+        if self.info.fail_flag == 1:
+            self._refresh_info()
         return info
 
     # ---- implicit Newmark and the learned preconditioner ----
@@ -379,6 +387,7 @@ class Model:
 
     def run(self, results_dir: str) -> None:
         _check(lib().pdx_run(self._h, results_dir.encode()))
+        self._refresh_info()
 
 
 def solve_csr(ia: np.ndarray, ja: np.ndarray, a: np.ndarray, b: np.ndarray, method: int = 2,

@@ -296,3 +296,34 @@ def test_static_solve_reports_the_sifs_of_the_quasi_static_increment(built, tmp_
     assert cs[0, 7] == 0
     np.testing.assert_allclose(cs[0, 2:4], ref[1:3], rtol=0, atol=1e-15)
     np.testing.assert_allclose(cs[0, 4:7], ref[3:6], rtol=1e-7)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fc1_oracle_reproduces_the_reference_sifs(built, name):
+    """The CPU restatement (oracle/fc1_oracle.py) pinned against the
+    reference: on the reference's own displacements of every increment, with
+    the set-up grown as the reference grew it, it gives the reference's KI
+    and KII (1e-9 of the largest |K|), its growth decisions and its new tips."""
+    import orc
+    from fc1_oracle import Fc1Oracle
+    g = golden(name)
+    rows = g["crack_rows"]
+    tips, moved = _moves(g)
+    mr, dcf = (4.0, 1.5) if name == "pe31_fc1m" else (6.0, 1.0)
+    m = pdx.Model(case_cmd("pe31", name), device=-1)
+    kmax = np.abs(rows[:, :, 3:5]).max()
+    worst = 0.0
+    ev = None
+    for i in range(rows.shape[0]):
+        if ev is None:
+            ev = Fc1Oracle(m, orc.Oracle(m), mr=mr, dcf=dcf)
+        cs = m.crack_state()[0]
+        KI, KII, _, keq, new_tip = ev.evaluate([cs[0:2], cs[2:4]], g["u_traj"][i], m.array("bond_state0"))
+        worst = max(worst, abs(KI - rows[i, 0, 3]) / kmax, abs(KII - rows[i, 0, 4]) / kmax)
+        assert (new_tip is not None) == bool(moved[i, 0]), f"increment {i + 1}"
+        if moved[i].any():
+            np.testing.assert_allclose(new_tip, tips[i, 0], rtol=0, atol=1e-12)
+            m.crack_advance(tips[i], moved[i])
+            ev = None
+    print(f"\n[{name}] oracle vs reference: worst K difference {worst:.2e} of max |K|")
+    assert worst < 1e-9
