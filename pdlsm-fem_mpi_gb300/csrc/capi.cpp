@@ -229,15 +229,18 @@ static pdx_status upload_model(pdx_model* m) {
       int mk = 0;
       for (int a = 0; a < me.elem_nn[e]; a++)
         if (std::binary_search(rfn.begin(), rfn.end(), me.conn[(size_t)e * 8 + a])) mk |= 1 << a;
-      if (!mk || me.elem_nn[e] != nen) continue;
+      if (!mk) continue;
+      // a triangle takes the 4-node layout with its third node repeated
+      const bool tri = me.elem_nn[e] == 3;
       double xN[8][3];
       for (int a = 0; a < nen; a++) {
-        const int node = me.conn[(size_t)e * 8 + a];
+        const int node = me.conn[(size_t)e * 8 + (tri && a == 3 ? 2 : a)];
         conn.push_back(node);
         for (int c = 0; c < 3; c++) xN[a][c] = me.X[(size_t)node * 3 + c];
       }
       std::vector<double> K((size_t)nd * nd);
-      if (D == 2) ke_quad4(xN, p.D.data(), K.data());
+      if (D == 2 && tri) ke_tri3(xN, p.D.data(), K.data());
+      else if (D == 2) ke_quad4(xN, p.D.data(), K.data());
       else ke_hex8(xN, p.D.data(), K.data());
       ke.insert(ke.end(), K.begin(), K.end());
       mask.push_back(mk);

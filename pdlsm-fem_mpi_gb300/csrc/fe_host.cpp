@@ -145,6 +145,7 @@ double elem_volume(const Mesh& m, int e) {
   auto X = [&](int j, int a) { return m.X[(size_t)c[j] * 3 + a]; };
   if (m.dim == 2) {
     double a1[3][3] = {{1, X(0, 0), X(0, 1)}, {1, X(1, 0), X(1, 1)}, {1, X(2, 0), X(2, 1)}};
+    if (m.elem_nn[e] == 3) return 0.5 * std::fabs(det33(a1));   // pdfemEleTri3N::eleVolume
     double a2[3][3] = {{1, X(2, 0), X(2, 1)}, {1, X(3, 0), X(3, 1)}, {1, X(0, 0), X(0, 1)}};
     return 0.5 * std::fabs(det33(a1)) + 0.5 * std::fabs(det33(a2));
   }
@@ -164,6 +165,12 @@ double elem_volume(const Mesh& m, int e) {
 
 void elem_center(const Mesh& m, int e, double xc[3]) {
   const int nn = m.elem_nn[e];
+  if (nn == 3) {   // pdfemEleTri3N::eleCenter
+    const int* c = &m.conn[(size_t)e * 8];
+    for (int a = 0; a < 3; a++)
+      xc[a] = (m.X[(size_t)c[0] * 3 + a] + m.X[(size_t)c[1] * 3 + a] + m.X[(size_t)c[2] * 3 + a]) / 3.0;
+    return;
+  }
   const double w = nn == 4 ? 0.25 : 0.125;
   xc[0] = xc[1] = xc[2] = 0;
   for (int j = 0; j < nn; j++)
@@ -259,6 +266,49 @@ void b_gauss_quad4(const double xN[4][3], double* B) {
       std::memcpy(B + (size_t)cnt * 24, b, sizeof(b));
       cnt++;
     }
+}
+
+// 3-node triangle (constant strain, pdfemEleTri3N.cpp): B = [b; c] / 2A with
+// b_i = y_j - y_k, c_i = x_k - x_j over the cyclic (i, j, k).  The element is
+// stored in the 4-node tables with its third node repeated in the fourth slot,
+// whose rows and columns stay zero.
+namespace {
+void b_tri3(const double xN[4][3], double B[3][8]) {
+  double a[3][3] = {{1, xN[0][0], xN[0][1]}, {1, xN[1][0], xN[1][1]}, {1, xN[2][0], xN[2][1]}};
+  const double V2 = 2.0 * (0.5 * std::fabs(det33(a)));
+  const double b[3] = {xN[1][1] - xN[2][1], xN[2][1] - xN[0][1], xN[0][1] - xN[1][1]};
+  const double c[3] = {-xN[1][0] + xN[2][0], -xN[2][0] + xN[0][0], -xN[0][0] + xN[1][0]};
+  std::memset(B, 0, sizeof(double) * 24);
+  for (int i = 0; i < 3; i++) {
+    B[0][2 * i] = b[i] / V2;
+    B[1][2 * i + 1] = c[i] / V2;
+    B[2][2 * i] = c[i] / V2;
+    B[2][2 * i + 1] = b[i] / V2;
+  }
+}
+}  // namespace
+
+void ke_tri3(const double xN[4][3], const double* D, double* Ke) {
+  std::memset(Ke, 0, sizeof(double) * 64);
+  double B[3][8];
+  b_tri3(xN, B);
+  double a[3][3] = {{1, xN[0][0], xN[0][1]}, {1, xN[1][0], xN[1][1]}, {1, xN[2][0], xN[2][1]}};
+  add_btdb<3, 8>(B, D, 0.5 * std::fabs(det33(a)), Ke);
+}
+
+void me_tri3(const double xN[4][3], double rho, double* Me) {
+  std::memset(Me, 0, sizeof(double) * 64);
+  double a[3][3] = {{1, xN[0][0], xN[0][1]}, {1, xN[1][0], xN[1][1]}, {1, xN[2][0], xN[2][1]}};
+  const double fac = rho * (0.5 * std::fabs(det33(a))) / 12.0;
+  for (int r = 0; r < 6; r++)
+    for (int c = 0; c < 6; c++)
+      if ((r - c) % 2 == 0) Me[r * 8 + c] = r == c ? 2 * fac : fac;
+}
+
+void b_gauss_tri3(const double xN[4][3], double* B) {
+  double b[3][8];
+  b_tri3(xN, b);
+  for (int g = 0; g < 4; g++) std::memcpy(B + (size_t)g * 24, b, sizeof(b));
 }
 
 void b_gauss_hex8(const double xN[8][3], double* B) {

@@ -68,7 +68,9 @@ bool read_mesh(const std::string& path, Mesh& m, Error& err) {
     if (!fin) return fail(err, 2, "bad element record " + std::to_string(e + 1));
     if (m.dim == 3 && !(nid[2] != nid[3] && nid[4] != nid[5]))
       return fail(err, 3, "tetrahedral elements are not supported");
-    if (m.dim == 2 && nid[3] == nid[2]) return fail(err, 3, "triangular elements are not supported");
+    // a 2D record whose fourth node repeats the third is a 3-node triangle
+    // (datModel.cpp reads it into pdfemEleTri3N)
+    if (m.dim == 2 && nid[3] == nid[2]) nn = 3;
     if (algo != 1 && algo != 2) return fail(err, 2, "element algorithm type must be 1 (PD) or 2 (FE)");
     m.elem_nn[e] = nn;
     m.elem_algo[e] = algo;

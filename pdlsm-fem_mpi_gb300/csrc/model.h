@@ -158,6 +158,11 @@ void me_hex8(const double xN[8][3], double rho, double* Me);
 // strain-displacement matrices at the stress-extrapolation Gauss points, in
 // the order used by eleFitStresses (pdfemEleQuad4N.cpp:73-131, pdfemEleBrick8N.cpp).
 void b_gauss_quad4(const double xN[4][3], double* B /*4 x 3 x 8*/);
+// 3-node triangle in the 4-node layout (fourth slot = third node, zero rows
+// and columns): constant-strain stiffness, consistent mass, B at every point
+void ke_tri3(const double xN[4][3], const double* D, double* Ke /*8x8*/);
+void me_tri3(const double xN[4][3], double rho, double* Me /*8x8*/);
+void b_gauss_tri3(const double xN[4][3], double* B /*4 x 3 x 8*/);
 void b_gauss_hex8(const double xN[8][3], double* B /*8 x 6 x 24*/);
 void extrap_L(int dim, double* L /*4x4 or 8x8*/);
 void nbc_unit_force(int dim, const double xN[4][3], double* Fe /*2x2 or 4x3*/);

@@ -494,10 +494,12 @@ bool prepare_model(pdx_model* m, Error& err, bool step_tables) {
   std::unordered_map<std::vector<int64_t>, int, VecHash> classes;
   for (int i = 0; i < nfe; i++) {
     const int e = s.fe[i];
+    const bool tri = me.elem_nn[e] == 3;   // stored with its third node repeated in the fourth slot
     double xN[8][3];
     for (int j = 0; j < nen; j++) {
-      p.fe_conn[(size_t)i * 8 + j] = me.conn[(size_t)e * 8 + j];
-      for (int a = 0; a < 3; a++) xN[j][a] = me.X[(size_t)me.conn[(size_t)e * 8 + j] * 3 + a];
+      const int n = me.conn[(size_t)e * 8 + (tri && j == 3 ? 2 : j)];
+      p.fe_conn[(size_t)i * 8 + j] = n;
+      for (int a = 0; a < 3; a++) xN[j][a] = me.X[(size_t)n * 3 + a];
     }
     double Le = 0;
     for (int j = 1; j < nen; j++)
@@ -508,6 +510,7 @@ bool prepare_model(pdx_model* m, Error& err, bool step_tables) {
     for (int j = 1; j < nen; j++)
       for (int a = 0; a < 3; a++) key.push_back(std::llround((xN[j][a] - xN[0][a]) / q));
     key.push_back(std::llround(std::log2(q) * 1e6));
+    key.push_back(me.elem_nn[e]);
     auto it = classes.find(key);
     int cls;
     if (it == classes.end()) {
@@ -517,9 +520,15 @@ bool prepare_model(pdx_model* m, Error& err, bool step_tables) {
       if (D == 2) {
         double x4[4][3];
         std::memcpy(x4, xN, sizeof(x4));
-        ke_quad4(x4, p.D.data(), K.data());
-        me_quad4(x4, me.rho, Me.data());
-        b_gauss_quad4(x4, B.data());
+        if (tri) {
+          ke_tri3(x4, p.D.data(), K.data());
+          me_tri3(x4, me.rho, Me.data());
+          b_gauss_tri3(x4, B.data());
+        } else {
+          ke_quad4(x4, p.D.data(), K.data());
+          me_quad4(x4, me.rho, Me.data());
+          b_gauss_quad4(x4, B.data());
+        }
       } else {
         ke_hex8(xN, p.D.data(), K.data());
         me_hex8(xN, me.rho, Me.data());
@@ -536,16 +545,18 @@ bool prepare_model(pdx_model* m, Error& err, bool step_tables) {
   p.n_cls = (int)classes.size();
   p.L.assign((size_t)ngp * ngp, 0.0);
   extrap_L(D, p.L.data());
-  // node -> FE element adjacency, in FE element order
+  // node -> FE element adjacency, in FE element order (a triangle's repeated
+  // fourth slot is not an adjacency: its rows are zero)
+  auto slots = [&](int i) { return me.elem_nn[s.fe[i]] == 3 ? 3 : nen; };
   p.fe_adj_ptr.assign(N + 1, 0);
   for (int i = 0; i < nfe; i++)
-    for (int j = 0; j < nen; j++) p.fe_adj_ptr[p.fe_conn[(size_t)i * 8 + j] + 1]++;
+    for (int j = 0; j < slots(i); j++) p.fe_adj_ptr[p.fe_conn[(size_t)i * 8 + j] + 1]++;
   for (int k = 0; k < N; k++) p.fe_adj_ptr[k + 1] += p.fe_adj_ptr[k];
   p.fe_adj.assign(p.fe_adj_ptr[N], 0);
   {
     std::vector<int> fill(p.fe_adj_ptr.begin(), p.fe_adj_ptr.end() - 1);
     for (int i = 0; i < nfe; i++)
-      for (int j = 0; j < nen; j++) {
+      for (int j = 0; j < slots(i); j++) {
         const int n = p.fe_conn[(size_t)i * 8 + j];
         p.fe_adj[fill[n]++] = (i << 3) | j;
       }

@@ -15,6 +15,12 @@
 namespace pdx {
 
 namespace {
+// VTK cell type of an element with nn nodes (the reference's ci_eleType):
+// triangle 5, quadrilateral 9, hexahedron 12
+int vtk_cell_type(int nn) { return nn == 3 ? 5 : nn == 4 ? 9 : 12; }
+}  // namespace
+
+namespace {
 
 void put_be32(std::ofstream& f, const void* p) {
   uint32_t v;
@@ -58,7 +64,7 @@ void write_vtk(const pdx_model* m, const std::string& path, const std::vector<do
     f << std::endl;
     f << "CELL_TYPES " << E << std::endl;
     for (int e = 0; e < E; e++) {
-      const int t = me.elem_nn[e] == 4 ? 9 : 12;
+      const int t = vtk_cell_type(me.elem_nn[e]);
       put_be32(f, &t);
     }
     f << std::endl;
@@ -98,7 +104,7 @@ void write_vtk(const pdx_model* m, const std::string& path, const std::vector<do
   }
   f << std::endl;
   f << "CELL_TYPES " << E << std::endl;
-  for (int e = 0; e < E; e++) f << (me.elem_nn[e] == 4 ? 9 : 12) << std::endl;
+  for (int e = 0; e < E; e++) f << vtk_cell_type(me.elem_nn[e]) << std::endl;
   f << "POINT_DATA " << N << std::endl;
   f << "VECTORS " << "U " << "float" << std::endl;
   for (int k = 0; k < N; k++) {

@@ -312,6 +312,30 @@ def plate_edge_crack(n: int = 31, L: float = 0.03, a_frac: float = 0.41, pd_band
                    material=(72e9, 0.22, 2440.0, KIc, 1.0e8), protype=protype)
 
 
+def split_triangles(mesh: Mesh, select: Optional[Callable[[np.ndarray], np.ndarray]] = None) -> Mesh:
+    """Split the 2D quadrilaterals whose centres ``select`` accepts (all without
+    it) into two 3-node triangles each, along alternating diagonals; a triangle
+    is written as four node ids with the third repeated (the reference's
+    pdfemEleTri3N records).  Element order: each split quad's two triangles in
+    its place; algorithm types carry over."""
+    X, el = mesh.X, mesh.elems
+    cent = X[el - 1].mean(axis=1)
+    pick = np.ones(len(el), dtype=bool) if select is None else np.asarray(select(cent), dtype=bool)
+    rows, algo = [], []
+    for e in range(len(el)):
+        a, b, c, d = (int(v) for v in el[e])
+        if not pick[e]:
+            rows.append([a, b, c, d])
+            algo.append(mesh.algo[e])
+            continue
+        if e % 2 == 0:
+            rows += [[a, b, c, c], [a, c, d, d]]
+        else:
+            rows += [[a, b, d, d], [b, c, d, d]]
+        algo += [mesh.algo[e], mesh.algo[e]]
+    return dataclasses.replace(mesh, elems=np.array(rows, dtype=np.int64), algo=np.array(algo, dtype=np.int64))
+
+
 def fc1_bench_case(n: int = 201, nsteps: int = 15):
     """FC 1 crack growth: n x n-node FE plate (30 mm), edge pre-crack to 0.41 W,
     K_Ic = 1 MPa m^0.5, top edge pulled 1e-6 m per load step, default FC 1

@@ -10,7 +10,7 @@ same models without the reference.
 Needs the reference tree (PDX_REFERENCE, or the checkout that
 __graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
-[--size-only] [--fc1-only] [--fc1-examples]
+[--size-only] [--fc1-only] [--fc1-examples] [--tri-only]
 """
 from __future__ import annotations
 
@@ -230,14 +230,50 @@ def fc1_cases() -> None:
     shutil.rmtree(work)
 
 
-# examples/DCT, the third FC 1 deck, is meshed with 3-node triangles, which
-# the library does not read
-FC1_EXAMPLES = (("DiagPlate", "DiagPlate_quasistatic_FC1"), ("plateCrack", "platCrack_quasiStatic_FC1"))
+def tri_cases() -> None:
+    """3-node triangles: the 2D plate with its left half split into triangles
+    (t21: set-up, 60 explicit steps with FC 3, a static solve) and the 31 x 31
+    edge-cracked FC 1 plate split into triangles everywhere (te31_fc1: 24
+    quasi-static increments of crack and PD-region growth)."""
+    work = tempfile.mkdtemp(prefix="golden_tri_")
+    d2 = os.path.join(work, "t21")
+    half = 0.5 * 0.05
+
+    def left(c):
+        return c[:, 0] < half
+
+    m = meshgen.split_triangles(plate_case(), left)
+    m.title = "t21"
+    meshgen.write_case(m, d2, "t21_explicit", solver="DYNAMIC", dt=5e-8, nsteps=60, save=20,
+                       factor=3.015, nlf=1.0, fc="3 2e-4")
+    ms = meshgen.split_triangles(plate_case(), left)
+    ms.title = "t21"
+    ms.ebcs[2].value = 1e-5
+    ms.ebcs[2].velocity = None
+    meshgen.write_case(ms, d2, "t21s", solver="STATIC", dt=1.0, nsteps=1, save=1, factor=3.015, nlf=1.0,
+                       lumped=False)
+    mt = meshgen.split_triangles(meshgen.plate_edge_crack(n=31, KIc=1.0e6, title="te31"))
+    mt.ebcs[2].velocity = 2e-7
+    meshgen.write_case(mt, d2, "te31_fc1", solver="QUASI-STATIC", dt=1.0, nsteps=24, save=24, factor=3.015,
+                       nlf=1.0, lumped=False, fc="1", extra=["RF 2", "SOLVE BICGSTAB 1e-13 20000"])
+    copy_inputs(d2, "t21")
+    save("t21_setup", run(d2, "t21_explicit.in", "setup"))
+    save("t21_explicit", run(d2, "t21_explicit.in", "explicit", "2e-4", "20"))
+    save("t21_static", run(d2, "t21s.in", "static"))
+    d = run(d2, "te31_fc1.in", "quasi_fc1")
+    save("te31_fc1", {k: d[k] for k in ("crack_rows", "region_rows", "pde_final", "fam_off_final",
+                                          "fam_members_final", "bond_state_final", "rf_rows", "u_traj")})
+    shutil.rmtree(work)
+
+
+FC1_EXAMPLES = (("DCT", "DCT_quasiStatic_FC1"), ("DiagPlate", "DiagPlate_quasistatic_FC1"),
+                ("plateCrack", "platCrack_quasiStatic_FC1"))
 
 
 def fc1_example_cases() -> None:
-    """The reference's own FC 1 example decks (examples/DiagPlate, plateCrack:
-    5.8k and 7.1k-node plates, two cracks each, 54 and 60 increments)
+    """The reference's own FC 1 example decks (examples/DCT, DiagPlate,
+    plateCrack: 5.7k-7.1k-node plates, DCT meshed with triangles and
+    quadrilaterals, one or two cracks, 54-136 increments)
     run through its quasi-static loop: crack path, PD-region growth and final
     families and bonds, with a digest of the deck files.  The decks stay in the
     reference tree; the tests read them there and skip without it."""
@@ -380,6 +416,10 @@ if __name__ == "__main__":
     if "--fc1-only" in sys.argv:
         build_driver()
         fc1_cases()
+        sys.exit(0)
+    if "--tri-only" in sys.argv:
+        build_driver()
+        tri_cases()
         sys.exit(0)
     if "--fc1-examples" in sys.argv:
         build_driver()

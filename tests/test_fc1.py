@@ -234,9 +234,8 @@ def test_fc1_bench_plate_matches_reference(built, tmp_path, method):
     assert np.abs(rf[1:, 1:4] - ref_rf[:, 2:5]).max() <= 1e-6 * np.abs(ref_rf[:, 2:5]).max()
 
 
-# The reference's third FC 1 deck, examples/DCT, is meshed with 3-node
-# triangles, which this library does not read.
-EXAMPLES = [("DiagPlate", "DiagPlate_quasistatic_FC1"), ("plateCrack", "platCrack_quasiStatic_FC1")]
+EXAMPLES = [("DCT", "DCT_quasiStatic_FC1"), ("DiagPlate", "DiagPlate_quasistatic_FC1"),
+            ("plateCrack", "platCrack_quasiStatic_FC1")]
 
 
 @pytest.mark.parametrize("folder,name", EXAMPLES)
@@ -244,10 +243,11 @@ def test_crack_advance_on_the_reference_example_decks(built, folder, name):
     """The reference's own FC 1 example decks (read in the reference tree;
     skipped without it): their crack paths, as the reference's loop produced
     them (tests/golden/ex_*_fc1.npz), replayed through pdx_crack_advance give
-    the reference's PD elements, families, members and bond states: two
-    cracks growing from a plate's centre in opposite directions (DiagPlate,
-    48 growth increments, 54 in all; plateCrack), inside a PD region laid out
-    along the crack path in advance."""
+    the reference's PD elements, families, members and bond states: a disk
+    meshed with triangles and quadrilaterals (DCT, one crack), and two cracks
+    growing from a plate's centre in opposite directions (DiagPlate, 48
+    growth increments of 54; plateCrack), inside a PD region laid out along
+    the crack path in advance."""
     import hashlib
     import os
     from conftest import reference_tree

@@ -127,12 +127,19 @@ def test_duplicate_dof_and_unsupported_elements(built, tmp_path):
     with pytest.raises(pdx.PdxError) as e:
         pdx.Model(str(tmp_path / "d.in"), device=-1)
     assert "repeatly" in str(e.value)
+    # a 2D record repeating its third node is a 3-node triangle (read); a 3D
+    # record collapsing a face (a tetrahedron or prism) is refused
     tri = meshgen.plate_strip_crack(n=11, L=0.01)
     tri.elems[0, 3] = tri.elems[0, 2]
     meshgen.write_lis(tri, str(tmp_path / "t.lis"))
     _write(tmp_path / "t.in", "MSHFILE t.lis\nSOLVER DYNAMIC\n")
+    assert pdx.Model(str(tmp_path / "t.in"), device=-1).array("elem_nn")[0] == 3
+    tet = meshgen.box3d(4, 4, 4, 1e-3, pd_mask=lambda c: c[:, 0] < 0)
+    tet.elems[0, 3] = tet.elems[0, 2]
+    meshgen.write_lis(tet, str(tmp_path / "h.lis"))
+    _write(tmp_path / "h.in", "MSHFILE h.lis\nSOLVER DYNAMIC\n")
     with pytest.raises(pdx.PdxError) as e:
-        pdx.Model(str(tmp_path / "t.in"), device=-1)
+        pdx.Model(str(tmp_path / "h.in"), device=-1)
     assert e.value.code == 3
 
 
@@ -193,7 +200,7 @@ def test_step_at_a_time_entry_points_need_a_device():
     assert host.learned_samples() == 0
 
 
-@pytest.mark.parametrize("case,cmd", CASES + [("pe31", "pe31_fc1")])
+@pytest.mark.parametrize("case,cmd", CASES + [("pe31", "pe31_fc1"), ("t21", "t21_explicit")])
 def test_scatter_map_offsets_count_the_columns_of_lower_nodes(built, case, cmd):
     """The assembly's scatter map against its definition: the offset of
     neighbour n in node k's rows is the number of active DOFs of the nodes
@@ -205,7 +212,7 @@ def test_scatter_map_offsets_count_the_columns_of_lower_nodes(built, case, cmd):
     nact = (eq >= 0).sum(axis=1)
     off, mem = m.array("fam_off"), m.array("fam_members")
     fe_conn = m.array("fe_conn").reshape(-1, 8)
-    nen = 4 if D == 2 else 8
+    nen = 4 if D == 2 else 8   # a triangle repeats its third node in the fourth slot
     N = eq.shape[0]
     rows = [set() for _ in range(N)]
     for f in range(len(off) - 1):
