@@ -140,10 +140,10 @@ def cpu_sample_batch(cmds, target_s: float = 15.0, threads: int = 0):
     """Oracle on the first specimens of a batch, each from its initial state, until target_s of CPU work."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import orc
-    import pdx
+    import orc_setup
     bonds_steps, el, used = 0, 0.0, 0
     for c in cmds:
-        host = pdx.Model(c, device=-1)
+        host = orc_setup.load(c)      # the oracle's own set-up, not the library's
         o = orc.Oracle(host, nthreads=threads)
         t = time.perf_counter()
         o.explicit(nsteps=3)
@@ -421,11 +421,12 @@ def algorithmic_bytes(model) -> dict:
 def cpu_sample(cmd: str, target_s: float = 15.0, threads: int = 0, window: int = 1 << 30):
     """Oracle (CPU restatement of the reference path) on a bounded number of
     steps, in runs of at most `window` steps from the initial state (the
-    window of the GPU timing)."""
+    window of the GPU timing).  Its set-up is the oracle's own
+    (orc_setup), so this leg loads no product code."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import orc
-    import pdx
-    host = pdx.Model(cmd, device=-1)
+    import orc_setup
+    host = orc_setup.load(cmd)
     o = orc.Oracle(host, nthreads=threads)
     t = time.perf_counter()
     o.explicit(nsteps=1)
