@@ -81,8 +81,6 @@ class Oracle:
             a[name] = np.ascontiguousarray(model.array(name))
         self.a = a
         info = model.info
-        if info.dim == 2 and np.any(a["elem_nn"] == 3):
-            raise NotImplementedError("the oracle's FE path takes 4-node quadrilaterals, not triangles")
         mat = a["material"]
         self.dim = info.dim
         self.n_node = info.n_node

@@ -46,6 +46,7 @@ struct orc_ctx {
   double L[64];
   double* mass;   /* n_node */
   int* fam_of;    /* n_node */
+  int* conn4;     /* n_elem*8: the model's connectivity, a 2D triangle's third node repeated in slot 4 */
 };
 
 /* ------------------------------------------------------------------ */
@@ -168,6 +169,44 @@ static double bmat(int dim, const double (*xN)[3], double p, double q, double r,
   return det;
 }
 
+/* 3-node triangle (pdfemEleTri3N.cpp) in the 4-node layout, fourth slot zero:
+   K = ((B^T D) B) V with the constant-strain B, consistent mass rho V / 12
+   (2 on the diagonal, 1 between like components), B at every stress point. */
+static void triangle_matrices(const orc_ctx* c, const double (*xN)[3], double* Ke, double* Me, double* Bg) {
+  const double mat[3][3] = {{1, xN[0][0], xN[0][1]}, {1, xN[1][0], xN[1][1]}, {1, xN[2][0], xN[2][1]}};
+  const double V = 0.5 * fabs(det3(mat));
+  const double b[3] = {xN[1][1] - xN[2][1], xN[2][1] - xN[0][1], xN[0][1] - xN[1][1]};
+  const double cc[3] = {-xN[1][0] + xN[2][0], -xN[2][0] + xN[0][0], -xN[0][0] + xN[1][0]};
+  double B[3][8];
+  memset(B, 0, sizeof(B));
+  for (int i = 0; i < 3; i++) {
+    B[0][2 * i] = b[i] / (2.0 * V);
+    B[1][2 * i + 1] = cc[i] / (2.0 * V);
+    B[2][2 * i] = cc[i] / (2.0 * V);
+    B[2][2 * i + 1] = b[i] / (2.0 * V);
+  }
+  double BtD[8][3];
+  for (int i = 0; i < 8; i++)
+    for (int k = 0; k < 3; k++) {
+      double s = 0;
+      for (int a = 0; a < 3; a++) s += B[a][i] * c->D[a * 3 + k];
+      BtD[i][k] = s;
+    }
+  memset(Ke, 0, sizeof(double) * 64);
+  memset(Me, 0, sizeof(double) * 64);
+  for (int i = 0; i < 8; i++)
+    for (int j = 0; j < 8; j++) {
+      double s = 0;
+      for (int k = 0; k < 3; k++) s += BtD[i][k] * B[k][j];
+      Ke[i * 8 + j] = s * V;
+    }
+  const double fac = c->m.rho * V / 12.0;
+  for (int r = 0; r < 6; r++)
+    for (int q = 0; q < 6; q++)
+      if ((r - q) % 2 == 0) Me[r * 8 + q] = r == q ? 2 * fac : fac;
+  for (int g = 0; g < 4; g++) memcpy(Bg + (size_t)g * 24, B, sizeof(B));
+}
+
 static void element_matrices(const orc_ctx* c, const double (*xN)[3], double* Ke, double* Me, double* Bg) {
   const int dim = c->m.dim, nv = c->nv, nd = c->nd, nen = c->nen;
   const double g = 1.0 / sqrt(3.0), gp[2] = {-g, g};
@@ -224,6 +263,11 @@ orc_ctx* orc_create(const orc_model* m, int nthreads) {
   c->nen = dim == 2 ? 4 : 8;
   c->nd = c->nen * dim;
   c->nmem = m->fam_off[m->n_fam];
+  c->conn4 = (int*)malloc(sizeof(int) * (size_t)m->n_elem * 8);
+  memcpy(c->conn4, m->conn, sizeof(int) * (size_t)m->n_elem * 8);
+  for (int e = 0; e < m->n_elem; e++)
+    if (dim == 2 && m->elem_nn[e] == 3) c->conn4[8 * e + 3] = c->conn4[8 * e + 2];
+  c->m.conn = c->conn4;
   const double E = m->E, nu = m->nu;
   c->mu = 0.5 * E / (1 + nu);
   memset(c->D, 0, sizeof(c->D));
@@ -388,9 +432,13 @@ orc_ctx* orc_create(const orc_model* m, int nthreads) {
     const int e = m->fe_idx[i];
     double xN[8][3];
     for (int j = 0; j < c->nen; j++)
-      for (int a = 0; a < 3; a++) xN[j][a] = m->X[3 * m->conn[8 * e + j] + a];
-    element_matrices(c, (const double(*)[3])xN, c->Ke + (size_t)i * nd * nd, c->Me + (size_t)i * nd * nd,
-                     c->Bgp + (size_t)i * ngp * nv * nd);
+      for (int a = 0; a < 3; a++) xN[j][a] = m->X[3 * c->conn4[8 * e + j] + a];
+    if (dim == 2 && m->elem_nn[e] == 3)
+      triangle_matrices(c, (const double(*)[3])xN, c->Ke + (size_t)i * nd * nd, c->Me + (size_t)i * nd * nd,
+                        c->Bgp + (size_t)i * ngp * nv * nd);
+    else
+      element_matrices(c, (const double(*)[3])xN, c->Ke + (size_t)i * nd * nd, c->Me + (size_t)i * nd * nd,
+                       c->Bgp + (size_t)i * ngp * nv * nd);
   }
   if (dim == 2) {
     double a = 1 + 0.5 * sqrt(3.0), b = -0.5, cc = 1 - 0.5 * sqrt(3.0);
@@ -414,7 +462,7 @@ orc_ctx* orc_create(const orc_model* m, int nthreads) {
 void orc_destroy(orc_ctx* c) {
   if (!c) return;
   free(c->A); free(c->Gw); free(c->gv); free(c->dv); free(c->Kb); free(c->cvec);
-  free(c->Ke); free(c->Me); free(c->Bgp); free(c->mass); free(c->fam_of);
+  free(c->Ke); free(c->Me); free(c->Bgp); free(c->mass); free(c->fam_of); free(c->conn4);
   free(c);
 }
 
@@ -624,7 +672,7 @@ void orc_stress(const orc_ctx* c, const uint8_t* bs, const double* u, double* si
         sg[g][r] = a;
       }
     }
-    for (int j = 0; j < nen; j++) {
+    for (int j = 0; j < m->elem_nn[e]; j++) {   /* a triangle's repeated slot is not a node of it */
       const int node = m->conn[8 * e + j];
       for (int r = 0; r < nv; r++) {
         double a = 0;

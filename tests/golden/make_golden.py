@@ -258,6 +258,13 @@ def tri_cases() -> None:
                        nlf=1.0, lumped=False, fc="1", extra=["RF 2", "SOLVE BICGSTAB 1e-13 20000"])
     copy_inputs(d2, "t21")
     save("t21_setup", run(d2, "t21_explicit.in", "setup"))
+    save("t21_coeffs", run(d2, "t21_explicit.in", "coeffs"))
+    u = np.random.default_rng(1).standard_normal((m.n_node, 2)) * 1e-6
+    ufile = os.path.join(work, "u_t21.bin")
+    u.astype(np.float64).tofile(ufile)
+    fr = run(d2, "t21_explicit.in", "force", ufile)
+    fr["u_all"] = u
+    save("t21_force", fr)
     save("t21_explicit", run(d2, "t21_explicit.in", "explicit", "2e-4", "20"))
     save("t21_static", run(d2, "t21s.in", "static"))
     d = run(d2, "te31_fc1.in", "quasi_fc1")

@@ -8,7 +8,8 @@ from conftest import case_cmd, golden, rel
 import orc
 import pdx
 
-CASES = [("p21", "p21_explicit"), ("b13", "b13_explicit")]
+# t21: the p21 plate with its left half in 3-node triangles
+CASES = [("p21", "p21_explicit"), ("b13", "b13_explicit"), ("t21", "t21_explicit")]
 
 
 @pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
@@ -60,7 +61,7 @@ def test_lumped_mass(oracle_case):
     np.testing.assert_array_equal(o.lumped_mass(), golden(case + "_explicit")["mass"])
 
 
-@pytest.mark.parametrize("case,cmd", [("p21", "p21s"), ("b13", "b13s")])
+@pytest.mark.parametrize("case,cmd", [("p21", "p21s"), ("b13", "b13s"), ("t21", "t21s")])
 def test_static_assembly(built, case, cmd):
     gs = golden(case + "_static")
     m = pdx.Model(case_cmd(case, cmd), device=-1)
