@@ -297,6 +297,10 @@ def fc1_example_cases() -> None:
             h.update(open(os.path.join(src, f), "rb").read())
         out = {k: d[k] for k in ("crack_rows", "region_rows", "pde_final", "fam_off_final", "fam_members_final",
                                  "bond_state_final")}
+        # the displacements of the first growth increment and of the last one
+        grow = np.nonzero(d["region_rows"][:, 2] == 0)[0]
+        sel = np.array(sorted({int(grow[0]) if len(grow) else 0, d["u_traj"].shape[0] - 1}))
+        out["u_sel"], out["u_sel_inc"] = d["u_traj"][sel], sel
         out["input_sha256"] = np.array(h.hexdigest())
         save("ex_" + folder + "_fc1", out)
     shutil.rmtree(work)

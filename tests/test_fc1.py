@@ -327,3 +327,44 @@ def test_fc1_oracle_reproduces_the_reference_sifs(built, name):
             ev = None
     print(f"\n[{name}] oracle vs reference: worst K difference {worst:.2e} of max |K|")
     assert worst < 1e-9
+
+
+@pytest.mark.parametrize("folder,name", EXAMPLES)
+def test_fc1_oracle_on_the_reference_example_decks(built, folder, name):
+    """The FC 1 restatement on the reference's own example decks (read in the
+    reference tree; skipped without it), at the first growth increment and
+    the last, on the reference's displacements and with the set-up grown as
+    the reference grew it: every crack's growth decision and new tip, and
+    the KI and KII the reference writes (its last crack's)."""
+    import os
+    import orc
+    from conftest import reference_tree
+    from fc1_oracle import Fc1Oracle
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    g = golden("ex_" + folder + "_fc1")
+    cmd = os.path.join(ref, "examples", folder, name + ".in")
+    fc = [ln.split() for ln in open(cmd) if ln.split()[:2] == ["FC", "1"]][0]
+    mr, dcf = (float(fc[2]), float(fc[3])) if len(fc) > 3 else (6.0, 1.0)
+    rows = g["crack_rows"]
+    tips, moved = _moves(g)
+    kmax = np.abs(rows[:, :, 3:5]).max()
+    m = pdx.Model(cmd, device=-1)
+    checked = 0
+    for i in range(rows.shape[0]):
+        if i in set(g["u_sel_inc"].tolist()):
+            u = g["u_sel"][list(g["u_sel_inc"]).index(i)]
+            ev = Fc1Oracle(m, orc.Oracle(m), mr=mr, dcf=dcf)
+            cs = m.crack_state()
+            res = [ev.evaluate([c[0:2], c[2:4]], u, m.array("bond_state0")) for c in cs]
+            for ck, (_, _, _, _, new_tip) in enumerate(res):
+                assert (new_tip is not None) == bool(moved[i, ck]), f"increment {i + 1}, crack {ck}"
+                if new_tip is not None:
+                    np.testing.assert_allclose(new_tip, tips[i, ck], rtol=0, atol=1e-12)
+            KI, KII = res[-1][0], res[-1][1]
+            assert abs(KI - rows[i, 0, 3]) <= 1e-9 * kmax and abs(KII - rows[i, 0, 4]) <= 1e-9 * kmax
+            checked += 1
+        if moved[i].any():
+            m.crack_advance(tips[i], moved[i])
+    assert checked == len(g["u_sel_inc"])
