@@ -368,3 +368,27 @@ def test_fc1_oracle_on_the_reference_example_decks(built, folder, name):
         if moved[i].any():
             m.crack_advance(tips[i], moved[i])
     assert checked == len(g["u_sel_inc"])
+
+
+def test_crack_api_edge_cases(built, tmp_path):
+    """pdx_crack_state / pdx_crack_advance on host-only models: the
+    pre-cracks as read, no growth without a moved crack, a 2D model without
+    cracks, and a 3D model refused."""
+    import meshgen
+    m = pdx.Model(case_cmd("pe31", "pe31_fc1"), device=-1)
+    cs = m.crack_state()
+    assert cs.shape == (1, 8)
+    np.testing.assert_allclose(cs[0, :4], [0.25e-3, 0.0155, 0.41 * 0.03, 0.0155], rtol=1e-12)
+    assert np.all(cs[0, 4:] == 0)
+    before = m.array("pde_idx").copy()
+    m.crack_advance(np.array([[0.02, 0.0155]]), np.array([0], dtype=np.uint8))
+    np.testing.assert_array_equal(m.array("pde_idx"), before)
+    np.testing.assert_array_equal(m.crack_state(), cs)
+    plain = meshgen.plate2d(11, 11, 1e-3, pd_mask=lambda c: c[:, 0] < 0.005, title="nc")
+    cmd = meshgen.write_case(plain, str(tmp_path), "nc", solver="QUASI-STATIC", dt=1.0, nsteps=2, save=2,
+                             factor=3.015, nlf=1.0, lumped=False, fc="1")
+    assert pdx.Model(cmd, device=-1).crack_state().shape == (0, 8)
+    box = pdx.Model(case_cmd("b13", "b13_explicit"), device=-1)
+    with pytest.raises(pdx.PdxError) as e:
+        box.crack_advance(np.zeros((1, 2)), np.ones(1, dtype=np.uint8))
+    assert e.value.code == 3
