@@ -232,7 +232,8 @@ def fc1_cases() -> None:
 
 def tri_cases() -> None:
     """3-node triangles: the 2D plate with its left half split into triangles
-    (t21: set-up, 60 explicit steps with FC 3, a static solve) and the 31 x 31
+    (t21: set-up, coefficients, internal force, 60 explicit steps with FC 3, a
+    static solve, 5 Newmark steps) and the 31 x 31
     edge-cracked FC 1 plate split into triangles everywhere (te31_fc1: 24
     quasi-static increments of crack and PD-region growth)."""
     work = tempfile.mkdtemp(prefix="golden_tri_")
@@ -252,6 +253,11 @@ def tri_cases() -> None:
     ms.ebcs[2].velocity = None
     meshgen.write_case(ms, d2, "t21s", solver="STATIC", dt=1.0, nsteps=1, save=1, factor=3.015, nlf=1.0,
                        lumped=False)
+    mn = meshgen.split_triangles(plate_case(), left)
+    mn.title = "t21"
+    mn.ebcs[2].velocity = 0.5
+    meshgen.write_case(mn, d2, "t21_newmark", solver="DYNAMIC", dt=2e-7, nsteps=5, save=5,
+                       factor=3.015, nlf=1.0, lumped=False, newmark=(0.5, 0.25))
     mt = meshgen.split_triangles(meshgen.plate_edge_crack(n=31, KIc=1.0e6, title="te31"))
     mt.ebcs[2].velocity = 2e-7
     meshgen.write_case(mt, d2, "te31_fc1", solver="QUASI-STATIC", dt=1.0, nsteps=24, save=24, factor=3.015,
@@ -267,6 +273,7 @@ def tri_cases() -> None:
     save("t21_force", fr)
     save("t21_explicit", run(d2, "t21_explicit.in", "explicit", "2e-4", "20"))
     save("t21_static", run(d2, "t21s.in", "static"))
+    save("t21_newmark", run(d2, "t21_newmark.in", "newmark"))
     d = run(d2, "te31_fc1.in", "quasi_fc1")
     save("te31_fc1", {k: d[k] for k in ("crack_rows", "region_rows", "pde_final", "fam_off_final",
                                           "fam_members_final", "bond_state_final", "rf_rows", "u_traj")})

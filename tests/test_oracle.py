@@ -78,7 +78,7 @@ def test_static_assembly(built, case, cmd):
     assert rel(sig, gs["sigma"]) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["p21", "b13"])
+@pytest.mark.parametrize("case", ["p21", "b13", "t21"])
 def test_newmark_matrix(built, case):
     gn = golden(case + "_newmark")
     m = pdx.Model(case_cmd(case, case + "_newmark"), device=-1)
