@@ -143,12 +143,14 @@ def test_assembly_matches_reference(built, case, cmd, mode):
     assert rel(a, oa) < 1e-12
 
 
-def test_newmark_matrix_matches_reference(built):
-    gn = golden("p21_newmark")
-    host = pdx.Model(case_cmd("p21", "p21_newmark"), device=-1)
+@pytest.mark.parametrize("case", ["p21", "t21"])
+def test_newmark_matrix_matches_reference(built, case):
+    """K_N = beta dt^2 K + M and its load; t21 has triangles (consistent mass rho V / 12)."""
+    gn = golden(case + "_newmark")
+    host = pdx.Model(case_cmd(case, case + "_newmark"), device=-1)
     up = host.array("u0").reshape(-1).copy()
     up += host.array("dtv").reshape(-1, 3)[:, :2].reshape(-1) * (host.array("eq") < 0)
-    with pdx.Model(case_cmd("p21", "p21_newmark"), device=0, precision=0) as m:
+    with pdx.Model(case_cmd(case, case + "_newmark"), device=0, precision=0) as m:
         ia, ja, a, f = m.assemble(3, up)
     assert rel(a, gn["KN_a"]) < 1e-12
     assert rel(f, gn["FN"]) < 1e-12
