@@ -24,7 +24,7 @@ typedef enum pdx_status {
   PDX_OK = 0,
   PDX_ERR_IO = 1,           /* a file cannot be opened or written */
   PDX_ERR_PARSE = 2,        /* malformed command or mesh file, bad keyword value */
-  PDX_ERR_UNSUPPORTED = 3,  /* input outside this library's scope (Tri3/Tet4, FC 1, ...) */
+  PDX_ERR_UNSUPPORTED = 3,  /* input outside this library's scope (Tet4, FC 1 in dynamic runs, ...) */
   PDX_ERR_INVALID = 4,      /* bad argument (null pointer, wrong size, wrong state) */
   PDX_ERR_CUDA = 5,         /* a CUDA runtime call failed */
   PDX_ERR_SINGULAR = 6,     /* a PDLSM moment matrix is singular (reference: dgesv info > 0) */
@@ -299,25 +299,31 @@ pdx_status pdx_batch_offsets(const pdx_model* m, int64_t* node_off, int64_t* mem
 
 /* Runs the solver the command file selects (pdsolve::pdfemSolver,
  * pdsolve.cpp:5073-5103) and writes the reference's outputs under
- * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM). */
+ * results_dir: <title>_<step>.vtk, <title>RF.out (static: _static/_PD/_FEM),
+ * and for quasi-static runs <title>_cp.out (the FC 1 crack path). */
 pdx_status pdx_run(pdx_model* m, const char* results_dir);
 
 /* Quasi-static increments one at a time, the loop body of
  * pdfemQuasiStaticSolver_CSRformat (pdsolve.cpp:6464-6590) with the direct
  * PARDISO solve replaced by a Krylov method: pdx_quasi_init resets the state
- * (initial DOF values, pre-crack bond states); each pdx_quasi_step assembles
+ * (initial DOF values, pre-crack bond states, and with FC 1 the pre-cracks
+ * and the PD region as read); each pdx_quasi_step assembles
  * K and f_ext - K u through the scatter map, solves K du = f_ext - K u to the
  * command file's tolerance with `method` (as pdx_solve_opts, or 8 in 2D: the
  * two-level BiCGStab of pdx_newmark_step; BiCGStab and then GMRES(30) take
  * over if it does not converge), updates u, applies FC 3 or FC 2 bond
- * failure, recomputes the stresses, records the reaction forces and advances
+ * failure or the FC 1 crack pass (SIFs, tip growth, PD-region growth and
+ * bond cuts behind a moved tip, pdx_crack_state), recomputes the stresses,
+ * records the reaction forces and advances
  * the prescribed DOFs by the reference's quasi-static rule
  * (setVaryEssentialBC, pdsolve.cpp:5263-5311): a varying EBC whose value is
  * 0 takes dt * velocity; after that, with FC 0 / FC 3 (load ratio 1) it
  * holds, so increment 1 solves the unloaded state and increment 2 the loaded
  * one; with FC 2 the load steps by the ratio 1.001 sigma_ult / max sigma1
  * (capped by the velocity) after an increment that cut no bond and holds
- * after one that did.  info->seconds is the device time of the solve. */
+ * after one that did; with FC 1 it steps by 1.001 K_Ic / Keq (last crack)
+ * when no tip moved and holds when one did.  info->seconds is the device time
+ * of the solve. */
 pdx_status pdx_quasi_init(pdx_model* m);
 pdx_status pdx_quasi_step(pdx_model* m, int method, pdx_solve_info* info);
 
