@@ -343,7 +343,7 @@ def bench_fc1(args):
         for _ in range(3):
             m.quasi_step(method)
         m.quasi_init()
-        wall, solve, moved, its = [], [], [], []
+        wall, solve, moved, its, ki = [], [], [], [], []
         for _ in range(nsteps):
             t0 = time.perf_counter()
             i = m.quasi_step(method)
@@ -351,6 +351,7 @@ def bench_fc1(args):
             solve.append(i.seconds)
             its.append(i.iterations)
             moved.append(bool(m.crack_state()[0, 7]))
+            ki.append(float(m.crack_state()[0, 4]))
         cs = m.crack_state()
         n_pde, n_fam, n_eq = m.array_len("pde_idx"), m.array_len("fam_off") - 1, m.info.n_eq
     wall, solve, moved = np.array(wall), np.array(solve), np.array(moved)
@@ -369,7 +370,47 @@ def bench_fc1(args):
             "host_and_rebuild_s_per_growth_increment": float((grow - solve[moved]).mean()) if moved.any() else None,
             "pd_elements_final": int(n_pde), "families_final": int(n_fam),
             "tip_final": [float(cs[0, 2]), float(cs[0, 3])], "keq_final": float(cs[0, 6]),
-            "cpu_baseline": None}
+            "cpu_baseline": fc1_cpu_baseline(args, cmd, ki[1] if len(ki) > 1 else None)}
+
+
+def fc1_cpu_baseline(args, cmd, ki_gpu):
+    if args.no_cpu_baseline:
+        return None
+    t, ki = cpu_sample_fc1(cmd)
+    return {"value": t, "unit": "s per increment", "cores": 1, "kind": "port",
+            "sample": "the loaded increment (the first load step) by the oracle on one host thread: assembly, "
+                      "K du = f by SuperLU (stand-in for the reference's PARDISO), node stresses, FC 1 SIFs",
+            "ki_rel_diff_vs_gpu": None if ki_gpu is None else abs(ki - ki_gpu) / max(abs(ki), 1e-300)}
+
+
+def cpu_sample_fc1(cmd: str):
+    """The FC 1 plate's loaded increment (its first load step) on the host
+    cores by the oracle: its own set-up and assembly (orc_setup, orc), K du = f
+    by SuperLU (SciPy spsolve, one thread; the reference factorises with
+    PARDISO), node stresses and the FC 1 evaluation (fc1_oracle).  Returns the
+    seconds and the crack's KI."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import orc
+    import orc_setup
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from fc1_oracle import Fc1Oracle
+    host = orc_setup.load(cmd, pattern=True)
+    o = orc.Oracle(host)
+    D = host.dim
+    eq = host.array("eq")
+    u = host.array("u0").copy()
+    pres = eq < 0
+    u[pres] += host.array("dtv").reshape(-1, 3)[:, :D].reshape(-1)[pres]
+    t0 = time.perf_counter()
+    ia, ja, a, f = o.assemble(u)
+    n = len(ia) - 1
+    du = spla.spsolve(sp.csr_matrix((a, ja, ia), shape=(n, n)).tocsc(), f)
+    u[eq >= 0] += du[eq[eq >= 0]]
+    cr = host.mesh.cracks[0]
+    ev = Fc1Oracle(host, o, mr=host.cmd.mr, dcf=host.cmd.dcf)
+    KI = ev.evaluate([cr[0][:2], cr[1][:2]], u.reshape(-1, D), host.array("bond_state0"))[0]
+    return time.perf_counter() - t0, KI
 
 
 # Steps per timed window.  Under the reference's failure model (PDLSM bond

@@ -112,7 +112,7 @@ def read_mesh(path: str) -> SimpleNamespace:
 
 def read_command(path: str):
     c = SimpleNamespace(solver=-1, dt=1.0, nsteps=1, factor=3.0, nlf=0.33, me=0.0, fail_flag=0, s0=0.0,
-                        s0_seed=0, s0_pert=0.0)
+                        s0_seed=0, s0_pert=0.0, mr=6.0, dcf=1.0)
     mesh = None
     base = os.path.dirname(path) or "."
     for line in open(path):
@@ -147,6 +147,8 @@ def read_command(path: str):
         elif k == "FC" and len(t) >= 2:
             f = int(t[1])
             c.fail_flag = f
+            if f == 1 and len(t) > 3:
+                c.mr, c.dcf = float(t[2]), float(t[3])
             if f == 3 and len(t) < 3:
                 c.fail_flag = 0            # a bare FC 3 breaks nothing, as the reference
             elif f == 3:
@@ -483,12 +485,48 @@ def build(mesh, cmd) -> dict:
             "csr_ia": np.zeros(0, dtype=np.int64), "csr_ja": np.zeros(0, dtype=np.int64)}
 
 
-class HostModel:
-    """The set-up arrays of a command file, with the interface orc.Oracle reads."""
+def csr_pattern(mesh, a: dict):
+    """setCSRIndexes_gloStiffMat (pdsolve.cpp:959-1121): node k's rows hold the
+    columns of its own family members and of the nodes of the FE elements
+    around it, by node and then component; rows are the equations."""
+    D, N = mesh.dim, mesh.n_node
+    off, mem = a["fam_off"], a["fam_members"].astype(np.int64)
+    nf = len(off) - 1
+    rk = [np.repeat(mem[off[:-1]], np.diff(off))]
+    rj = [mem]
+    for e in a["fe_idx"]:
+        nodes = mesh.conn[e, :mesh.elem_nn[e]]
+        rk.append(np.repeat(nodes, len(nodes)))
+        rj.append(np.tile(nodes, len(nodes)))
+    pairs = np.unique(np.stack([np.concatenate(rk), np.concatenate(rj)], 1), axis=0) if nf or len(a["fe_idx"]) \
+        else np.zeros((0, 2), dtype=np.int64)
+    eq = a["eq"].astype(np.int64).reshape(N, D)
+    cols = eq[pairs[:, 1]]                                     # (n_pairs, D), -1 where prescribed
+    ia = np.zeros(int((eq >= 0).sum()) + 1, dtype=np.int64)
+    ja = []
+    start = np.searchsorted(pairs[:, 0], np.arange(N + 1))
+    for k in range(N):
+        c = cols[start[k]:start[k + 1]].reshape(-1)
+        c = c[c >= 0]
+        for d in range(D):
+            r = eq[k, d]
+            if r < 0:
+                continue
+            ja.append(c)
+            ia[r + 1] = len(c)
+    return np.cumsum(ia), (np.concatenate(ja) if ja else np.zeros(0, dtype=np.int64))
 
-    def __init__(self, cmd_path: str):
+
+class HostModel:
+    """The set-up arrays of a command file, with the interface orc.Oracle reads
+    (the CSR pattern only with pattern=True: the explicit loop does not use it)."""
+
+    def __init__(self, cmd_path: str, pattern: bool = False):
         mesh, cmd = read_command(cmd_path)
+        self.mesh, self.cmd = mesh, cmd
         self.arrays = build(mesh, cmd)
+        if pattern:
+            self.arrays["csr_ia"], self.arrays["csr_ja"] = csr_pattern(mesh, self.arrays)
         a = self.arrays
         n_fam = len(a["fam_off"]) - 1
         self.info = SimpleNamespace(dim=mesh.dim, n_node=mesh.n_node, n_elem=mesh.n_elem,
@@ -501,5 +539,5 @@ class HostModel:
         return self.arrays[name]
 
 
-def load(cmd_path: str) -> HostModel:
-    return HostModel(cmd_path)
+def load(cmd_path: str, pattern: bool = False) -> HostModel:
+    return HostModel(cmd_path, pattern)

@@ -66,3 +66,13 @@ def test_timed_windows_stay_inside_the_bounded_steps():
     assert bench.STEP_WINDOW["c2"] <= 280 and bench.STEP_WINDOW["c4"] <= 225
     assert bench.STEP_WINDOW["c1"] >= 1000
     assert set(bench.WINDOW_REASON) == set(bench.STEP_WINDOW)
+
+
+def test_fc1_cpu_baseline_reproduces_the_reference_sif():
+    """The FC 1 bench's CPU leg (oracle set-up and assembly, SuperLU, FC 1
+    oracle; no product code) on the 31 x 31 plate: its KI for the loaded
+    increment equals the reference's."""
+    from conftest import case_cmd, golden
+    t, ki = bench.cpu_sample_fc1(case_cmd("pe31", "pe31_fc1"))
+    ref = golden("pe31_fc1")["crack_rows"][1, 0, 3]
+    assert t > 0 and abs(ki - ref) <= 1e-10 * abs(ref)
