@@ -309,6 +309,8 @@ def fc1_example_cases() -> None:
         sel = np.array(sorted({int(grow[0]) if len(grow) else 0, d["u_traj"].shape[0] - 1}))
         out["u_sel"], out["u_sel_inc"] = d["u_traj"][sel], sel
         out["input_sha256"] = np.array(h.hexdigest())
+        # the reference's set-up of the deck as digests (DOFs, families, bonds, CSR pattern)
+        out.update({"setup_" + k: v for k, v in setup_digests(run(dst, name + ".in", "setup")).items()})
         save("ex_" + folder + "_fc1", out)
     shutil.rmtree(work)
 

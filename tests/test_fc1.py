@@ -392,3 +392,30 @@ def test_crack_api_edge_cases(built, tmp_path):
     with pytest.raises(pdx.PdxError) as e:
         box.crack_advance(np.zeros((1, 2)), np.ones(1, dtype=np.uint8))
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("folder,name", EXAMPLES)
+def test_example_deck_setups_match_reference(built, folder, name):
+    """The library's host set-up and the oracle's own (orc_setup) of the
+    reference's FC 1 example decks (read in the reference tree; skipped
+    without it) against the reference's set-up, as SHA-256 digests of DOFs,
+    families, members, bond states and the CSR pattern."""
+    import hashlib
+    import os
+    import orc_setup
+    from conftest import reference_tree
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    g = golden("ex_" + folder + "_fc1")
+    cmd = os.path.join(ref, "examples", folder, name + ".in")
+
+    def digest(a):
+        return hashlib.sha256(np.asarray(a, dtype=np.int64).reshape(-1).astype("<i8").tobytes()).hexdigest()
+    names = ("eq", "fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja")
+    lib_model = pdx.Model(cmd, device=-1)
+    oracle_model = orc_setup.load(cmd, pattern=True)
+    for n in names:
+        ref_digest = str(g["setup_" + n + "_sha256"])
+        assert digest(lib_model.array(n)) == ref_digest, ("library", n)
+        assert digest(oracle_model.array(n)) == ref_digest, ("oracle", n)
