@@ -283,8 +283,9 @@ def build(mesh, cmd) -> dict:
     for e in range(E):                                      # element order, as the reference adds
         k = m.elem_nn[e]
         vol_node[m.conn[e, :k]] += vol_elem[e] / k
-    min_delta = vol_elem.min() ** (1.0 / D)
-    max_delta = vol_elem.max() ** (1.0 / D)
+    # C's pow (math.pow), as the reference: numpy's vectorised power may differ in the last bit
+    min_delta = math.pow(float(vol_elem.min()), 1.0 / D)
+    max_delta = math.pow(float(vol_elem.max()), 1.0 / D)
     lbc, rtc = m.X[0].copy(), m.X[0].copy()
     for j in range(D):
         lbc[j], rtc[j] = m.X[:, j].min(), m.X[:, j].max()
@@ -413,7 +414,7 @@ def build(mesh, cmd) -> dict:
     fam_node = np.nonzero(node_type)[0]
     fam_of = -np.ones(N, dtype=np.int64)
     fam_of[fam_node] = np.arange(len(fam_node))
-    delta_node = c.factor * vol_node ** (1.0 / D)
+    delta_node = np.array([c.factor * math.pow(float(v), 1.0 / D) for v in vol_node])
     fam_delta = delta_node[fam_node]
     fam_cdv = np.zeros(len(fam_node))
     for e in pde:

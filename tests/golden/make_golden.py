@@ -11,6 +11,7 @@ Needs the reference tree (PDX_REFERENCE, or the checkout that
 __graft_entry__.build() recorded) and SciPy; it is run by
 hand, not by the tests:  python tests/golden/make_golden.py [--fc2-only] [--rf-only] [--ascii-only]
 [--size-only] [--fc1-only] [--fc1-examples] [--tri-only]
+[--example-setups]
 """
 from __future__ import annotations
 
@@ -315,6 +316,31 @@ def fc1_example_cases() -> None:
     shutil.rmtree(work)
 
 
+def example_setup_cases() -> None:
+    """The reference's set-up (DOFs, families, members, bond states, CSR
+    pattern) of every example deck whose mesh file is in the reference tree,
+    as SHA-256 digests keyed by folder and deck; the tests read the decks in
+    the tree and skip without it."""
+    out = {}
+    work = tempfile.mkdtemp(prefix="golden_exsetup_")
+    for folder in sorted(os.listdir(os.path.join(REF, "examples"))):
+        src = os.path.join(REF, "examples", folder)
+        for f in sorted(os.listdir(src)):
+            if not f.endswith(".in"):
+                continue
+            mesh = [ln.split()[1] for ln in open(os.path.join(src, f)) if ln.startswith("MSHFILE")]
+            if not mesh or not os.path.exists(os.path.join(src, mesh[0])):
+                continue
+            dst = os.path.join(work, folder)
+            if not os.path.exists(dst):
+                shutil.copytree(src, dst)
+            key = folder + "__" + f[:-3]
+            for k, v in setup_digests(run(dst, f, "setup")).items():
+                out[key + "__" + k] = v
+    save("ex_setups", out)
+    shutil.rmtree(work)
+
+
 def rf_cases() -> None:
     """Reaction forces (RF 2: the top edge's essential BC) of the 2D plate over
     60 explicit steps, no failure criterion."""
@@ -440,6 +466,10 @@ if __name__ == "__main__":
     if "--tri-only" in sys.argv:
         build_driver()
         tri_cases()
+        sys.exit(0)
+    if "--example-setups" in sys.argv:
+        build_driver()
+        example_setup_cases()
         sys.exit(0)
     if "--fc1-examples" in sys.argv:
         build_driver()

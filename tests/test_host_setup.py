@@ -242,3 +242,35 @@ def test_scatter_map_offsets_count_the_columns_of_lower_nodes(built, case, cmd):
             el = fe_conn[adj[j] >> 3]
             for a in range(nen):
                 assert rfe[j, a] == rel(k, el[a])
+
+
+def _example_decks():
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ex_setups.npz"))
+    return sorted({(k.split("__")[0], k.split("__")[1]) for k in g.files})
+
+
+@pytest.mark.parametrize("folder,deck", _example_decks())
+def test_every_reference_example_deck_sets_up_as_the_reference(built, folder, deck):
+    """Every example deck of the reference whose mesh is in its tree (read
+    there; skipped without it): the library's host set-up and the oracle's
+    own give the reference's DOFs, families, members, bond states and CSR
+    pattern (SHA-256 digests, tests/golden/ex_setups.npz)."""
+    import hashlib
+    import sys
+    from conftest import REPO, reference_tree
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import orc_setup
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    g = golden("ex_setups")
+    cmd = os.path.join(ref, "examples", folder, deck + ".in")
+
+    def digest(a):
+        return hashlib.sha256(np.asarray(a, dtype=np.int64).reshape(-1).astype("<i8").tobytes()).hexdigest()
+    lib_model = pdx.Model(cmd, device=-1)
+    oracle_model = orc_setup.load(cmd, pattern=True)
+    for n in ("eq", "fam_off", "fam_members", "bond_state0", "csr_ia", "csr_ja"):
+        want = str(g[f"{folder}__{deck}__{n}_sha256"])
+        assert digest(lib_model.array(n)) == want, ("library", n)
+        assert digest(oracle_model.array(n)) == want, ("oracle", n)
