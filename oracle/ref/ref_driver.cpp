@@ -10,6 +10,7 @@
 //   ref_driver force    <cmd.in> <outdir> <u_all.bin>
 //   ref_driver explicit <cmd.in> <outdir> <s0 or 0> <dump_every>
 //   ref_driver static   <cmd.in> <outdir>
+//   ref_driver assemble <cmd.in> <outdir>          (the static K and F only)
 //   ref_driver newmark  <cmd.in> <outdir>
 //   ref_driver quasi    <cmd.in> <outdir>
 //   ref_driver explicit_fc2 <cmd.in> <outdir> <every>  (FC 2 after every step)
@@ -349,7 +350,7 @@ void run_explicit(datModel& d, pdsolve& sol, Dumper& out, double s0, int every, 
   out.i64("bond_state_final", bond_states(d));
 }
 
-void run_static(datModel& d, pdsolve& sol, Dumper& out) {
+void run_static(datModel& d, pdsolve& sol, Dumper& out, bool solve = true) {
   d.ci_solvFlag = 1;
   int neq = num_eq(d);
   sol.pdfemAssembleEquasSys_CSRformat(d, neq);
@@ -358,6 +359,7 @@ void run_static(datModel& d, pdsolve& sol, Dumper& out) {
   out.i64("K_ja", std::vector<long long>(sol.cip_ja, sol.cip_ja + nnz));
   out.f64("K_a", std::vector<double>(sol.cdp_KuGlo, sol.cdp_KuGlo + nnz));
   out.f64("F", std::vector<double>(sol.cdp_FGlo, sol.cdp_FGlo + neq));
+  if (!solve) return;
   long long n = neq;
   int comm = 0;
   Vector* Ug = new Vector(neq);
@@ -572,6 +574,7 @@ int main(int argc, char** argv) {
   } else if (mode == "explicit_fc2") {
     run_explicit(dat, sol, out, 0.0, std::atoi(argv[4]), true);
   } else if (mode == "static") run_static(dat, sol, out);
+  else if (mode == "assemble") run_static(dat, sol, out, false);
   else if (mode == "newmark") run_newmark(dat, sol, out);
   else if (mode == "newmark_fc2") run_newmark(dat, sol, out, true);
   else if (mode == "quasi") run_quasi(dat, sol, out);

@@ -338,6 +338,22 @@ def example_setup_cases() -> None:
             for k, v in setup_digests(run(dst, f, "setup")).items():
                 out[key + "__" + k] = v
     save("ex_setups", out)
+    # the static decks: the reference's load vector F and its stiffness applied
+    # to a seeded vector x (K x), so the oracle's assembly is checked entry
+    # by entry without storing K
+    st = {}
+    for folder, deck in (("DiagPlate", "DiagPlate_static"), ("plateCrack", "platCrack_Static"),
+                         ("plateHole", "platHole_Static")):
+        d = run(os.path.join(work, folder), deck + ".in", "assemble")
+        n = len(d["F"])
+        x = np.random.default_rng(7).standard_normal(n)
+        ia, ja, a = d["K_ia"], d["K_ja"], d["K_a"]
+        kx = np.zeros(n)
+        for r in range(n):
+            kx[r] = a[ia[r]:ia[r + 1]] @ x[ja[ia[r]:ia[r + 1]]]
+        st[folder + "__" + deck + "__F"] = d["F"]
+        st[folder + "__" + deck + "__Kx"] = kx
+    save("ex_static", st)
     shutil.rmtree(work)
 
 

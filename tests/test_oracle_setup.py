@@ -52,3 +52,29 @@ def test_oracle_setup_matches_reference_at_configuration_size(tmp_path, name):
     h = orc_setup.load(cmd)
     res = _digests_equal(h, golden("c1_size" if name == "c1" else "c2_setup"))
     assert res and all(res.values()), res
+
+
+@pytest.mark.parametrize("folder,deck", [("DiagPlate", "DiagPlate_static"), ("plateCrack", "platCrack_Static"),
+                                         ("plateHole", "platHole_Static")])
+def test_oracle_static_assembly_on_reference_example_decks(folder, deck):
+    """The oracle (own set-up, CSR pattern and assembly) on the reference's
+    static example decks (read in the reference tree; skipped without it):
+    the load vector and the stiffness applied to a seeded vector equal the
+    reference's (tests/golden/ex_static.npz)."""
+    from conftest import reference_tree
+    import orc
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    g = golden("ex_static")
+    h = orc_setup.load(os.path.join(ref, "examples", folder, deck + ".in"), pattern=True)
+    o = orc.Oracle(h)
+    v = h.array("u0").copy()
+    v[h.array("eq") >= 0] = 0.0
+    ia, ja, a, f = o.assemble(v)
+    n = len(ia) - 1
+    x = np.random.default_rng(7).standard_normal(n)
+    kx = np.array([a[ia[r]:ia[r + 1]] @ x[ja[ia[r]:ia[r + 1]]] for r in range(n)])
+    want_f, want_kx = g[f"{folder}__{deck}__F"], g[f"{folder}__{deck}__Kx"]
+    assert np.linalg.norm(f - want_f) <= 1e-12 * np.linalg.norm(want_f)
+    assert np.linalg.norm(kx - want_kx) <= 1e-12 * np.linalg.norm(want_kx)
